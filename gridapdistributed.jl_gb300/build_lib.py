@@ -1,0 +1,71 @@
+"""Builds libgdgpu.so (the C-ABI library) in-tree with nvcc for sm_103a.
+
+Translation units compile in parallel into ``_build/`` and link into
+``lib/libgdgpu.so`` next to this file.  Usable as a script or through ``build()``.
+"""
+from __future__ import annotations
+
+import concurrent.futures as cf
+import os
+import subprocess
+import sys
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+CSRC = HERE / "csrc"
+BUILD = HERE / "_build"
+LIBDIR = HERE / "lib"
+LIB = LIBDIR / "libgdgpu.so"
+
+ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+NVCC_FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr",
+              "-Xptxas", "-v"] + ARCH
+
+
+def _nvcc() -> str:
+    for cand in (os.environ.get("NVCC"), "/usr/local/cuda/bin/nvcc", "nvcc"):
+        if cand and (os.path.isabs(cand) and os.path.exists(cand) or not os.path.isabs(cand)):
+            return cand
+    return "nvcc"
+
+
+def sources():
+    return sorted(CSRC.glob("*.cu"))
+
+
+def _compile(src: Path) -> tuple[Path, str]:
+    obj = BUILD / (src.stem + ".o")
+    dep_mtime = max(p.stat().st_mtime for p in list(CSRC.glob("*.h")) + [src] + [HERE.parent / "include" / "gdgpu.h"])
+    if obj.exists() and obj.stat().st_mtime > dep_mtime:
+        return obj, ""
+    cmd = [_nvcc(), *NVCC_FLAGS, "-I", str(HERE.parent / "include"), "-c", str(src), "-o", str(obj)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+    return obj, r.stderr
+
+
+def build(verbose: bool = False) -> Path:
+    BUILD.mkdir(exist_ok=True)
+    LIBDIR.mkdir(exist_ok=True)
+    srcs = sources()
+    logs = []
+    with cf.ThreadPoolExecutor(max_workers=min(8, len(srcs))) as ex:
+        results = list(ex.map(_compile, srcs))
+    objs = [o for o, _ in results]
+    logs = [l for _, l in results if l]
+    newest = max(o.stat().st_mtime for o in objs)
+    if not LIB.exists() or LIB.stat().st_mtime < newest:
+        cmd = [_nvcc(), "-shared", *ARCH, "-o", str(LIB), *map(str, objs), "-lcudart"]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
+    if verbose:
+        for l in logs:
+            print(l, file=sys.stderr)
+    (BUILD / "ptxas.log").write_text("\n".join(logs))
+    return LIB
+
+
+if __name__ == "__main__":
+    print(build(verbose="-v" in sys.argv))

@@ -1,0 +1,239 @@
+// Internal definitions shared by the translation units of libgdgpu.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/gdgpu.h"
+
+namespace gd {
+
+constexpr int kMaxDim = 3;
+constexpr int kMaxOrder = 3;
+
+// ---------------------------------------------------------------------------------
+// Error handling: every C entry point returns a status and keeps a message per thread.
+// ---------------------------------------------------------------------------------
+void set_error(const std::string& msg);
+int fail(int code, const std::string& msg);
+
+#define GD_CUDA_TRY(expr)                                                                  \
+  do {                                                                                     \
+    cudaError_t _e = (expr);                                                               \
+    if (_e != cudaSuccess)                                                                 \
+      return ::gd::fail(GD_ERR_CUDA, std::string(#expr) + ": " + cudaGetErrorString(_e));  \
+  } while (0)
+
+#define GD_TRY(expr)                 \
+  do {                               \
+    int _s = (expr);                 \
+    if (_s != GD_OK) return _s;      \
+  } while (0)
+
+// ---------------------------------------------------------------------------------
+// Geometry of the partitioned Cartesian mesh, passed by value to kernels.
+// ---------------------------------------------------------------------------------
+struct Geom {
+  int dim;
+  int k;             // polynomial order (1 for a bare model)
+  int nparts;
+  int np[kMaxDim];   // parts per direction
+  int64_t n[kMaxDim];   // cells per direction
+  int64_t N[kMaxDim];   // lattice nodes per direction = k*n+1
+  int64_t bl[kMaxDim];  // cells of the first (np-rem) parts along d
+  int64_t brem[kMaxDim];
+  int dsides[2 * kMaxDim];
+  double h[kMaxDim];
+  double x0[kMaxDim];
+};
+
+// One part as seen by the kernels (array in device memory).
+struct DevPart {
+  int64_t own_lo[kMaxDim], own_hi[kMaxDim];   // owned cells [lo,hi)
+  int64_t loc_lo[kMaxDim], loc_hi[kMaxDim];   // owned+ghost cells [lo,hi)
+  int64_t nb[kMaxDim];                         // local node box extents
+  int64_t nnodes;        // prod(nb)
+  int64_t node_off;      // offset in concatenated per-node arrays
+  int64_t lid_off;       // offset in concatenated per-free-dof arrays
+  int64_t nfree;         // local free dofs
+  int64_t n_own;         // owned free dofs
+  int64_t first_gdof;    // first owned gid
+  int64_t lcell_off;     // offset in concatenated per-local-cell arrays
+  int64_t nlcells;
+  // assembler data
+  int64_t grow_off, n_grow;   // ghost rows of this part in the concatenated row space
+  int64_t gcol_off, n_gcol;   // ghost columns (per-part lists concatenated)
+};
+
+// Part coordinate along d of global cell index c (_local_range, PArraysExtras.jl:72-84):
+// the first np-rem parts hold bl cells, the last rem parts bl+1.
+__host__ __device__ inline int cell_part_coord(const Geom& g, int d, int64_t c) {
+  int64_t l = g.bl[d];
+  int64_t B = (g.np[d] - g.brem[d]) * l;
+  if (c < B) return (int)(c / l);
+  return (int)((g.np[d] - g.brem[d]) + (c - B) / (l + 1));
+}
+
+__host__ __device__ inline int part_of_coords(const Geom& g, const int* pc) {
+  int p = 0;
+  for (int d = g.dim - 1; d >= 0; --d) p = p * g.np[d] + pc[d];
+  return p;
+}
+
+// Owner rank of a lattice node: max owner over the cells around it
+// (FESpaces.jl:145-183).  Owner part coordinates are monotone in the cell index,
+// so the max is reached at the highest cell index touching the node.
+__host__ __device__ inline int node_owner(const Geom& g, const int64_t* X) {
+  int pc[kMaxDim];
+  for (int d = 0; d < g.dim; ++d) {
+    int64_t c = X[d] / g.k;
+    if (c > g.n[d] - 1) c = g.n[d] - 1;
+    pc[d] = cell_part_coord(g, d, c);
+  }
+  return part_of_coords(g, pc);
+}
+
+__host__ __device__ inline int cell_owner(const Geom& g, const int64_t* c) {
+  int pc[kMaxDim];
+  for (int d = 0; d < g.dim; ++d) pc[d] = cell_part_coord(g, d, c[d]);
+  return part_of_coords(g, pc);
+}
+
+__host__ __device__ inline bool node_is_dirichlet(const Geom& g, const int64_t* X) {
+  for (int d = 0; d < g.dim; ++d) {
+    if (g.dsides[2 * d] && X[d] == 0) return true;
+    if (g.dsides[2 * d + 1] && X[d] == g.N[d] - 1) return true;
+  }
+  return false;
+}
+
+__host__ __device__ inline int64_t lattice_lin(const Geom& g, const int64_t* X) {
+  int64_t r = 0;
+  for (int d = g.dim - 1; d >= 0; --d) r = r * g.N[d] + X[d];
+  return r;
+}
+
+__host__ __device__ inline void lattice_coords(const Geom& g, int64_t lin, int64_t* X) {
+  for (int d = 0; d < g.dim; ++d) {
+    X[d] = lin % g.N[d];
+    lin /= g.N[d];
+  }
+}
+
+__host__ __device__ inline int64_t cell_lin(const Geom& g, const int64_t* c) {
+  int64_t r = 0;
+  for (int d = g.dim - 1; d >= 0; --d) r = r * g.n[d] + c[d];
+  return r;
+}
+
+// ---------------------------------------------------------------------------------
+// Device scratch helpers (implemented in gd_util.cu)
+// ---------------------------------------------------------------------------------
+template <typename T>
+struct DBuf {
+  T* p = nullptr;
+  size_t n = 0;
+};
+
+int dalloc_bytes(void** p, size_t bytes);
+void dfree(void* p);
+
+template <typename T>
+int dalloc(DBuf<T>& b, size_t n) {
+  if (b.p) dfree(b.p);
+  b.p = nullptr;
+  b.n = n;
+  if (n == 0) return GD_OK;
+  return dalloc_bytes((void**)&b.p, n * sizeof(T));
+}
+template <typename T>
+void dfreeb(DBuf<T>& b) {
+  if (b.p) dfree(b.p);
+  b.p = nullptr;
+  b.n = 0;
+}
+
+// Exclusive scan of int32 flags/counts into int64 (out has n+1 entries; out[n] = total).
+int exclusive_scan_i32(const int32_t* in, int64_t* out, int64_t n, cudaStream_t s);
+
+}  // namespace gd
+
+// ---------------------------------------------------------------------------------
+// Opaque objects of the C ABI
+// ---------------------------------------------------------------------------------
+struct gd_ctx {
+  int device = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+};
+
+struct gd_model {
+  gd_ctx* ctx = nullptr;
+  gd::Geom geom{};   // k = 1
+  double domain[2 * gd::kMaxDim] = {0};
+  std::vector<gd::DevPart> parts;   // boxes only
+};
+
+struct gd_space {
+  gd_model* model = nullptr;
+  gd::Geom geom{};
+  int ncomp = 1;
+  std::vector<gd::DevPart> parts;   // host copy
+  gd::DBuf<gd::DevPart> d_parts;
+  int64_t total_nodes = 0;          // concatenated local node boxes
+  int64_t total_lids = 0;           // concatenated local free dofs
+  int64_t ngdofs = 0;
+  // per concatenated local node: free lid (>=0) or -(dirichlet id + 1)
+  gd::DBuf<int32_t> node_lid;
+  // per concatenated free dof
+  gd::DBuf<int32_t> lid_node;     // local node index in the part's box
+  gd::DBuf<int32_t> lid_owner;
+  gd::DBuf<int32_t> lid_ownidx;   // index among the part's owned dofs (own: valid)
+  gd::DBuf<int64_t> lid_gid;
+  // Dirichlet values on the global lattice (dense) or null
+  gd::DBuf<double> u_dir;
+  bool has_dirichlet_values = false;
+  // table: lexicographic cell-local node -> Gridap cell-local node index
+  std::vector<int> lex_to_gridap;
+};
+
+struct gd_asm {
+  gd_space* trial = nullptr;
+  gd_space* test = nullptr;
+  int strategy = GD_SUB_ASSEMBLED_ROWS;
+  bool symbolic_done = false;
+  bool numeric_done = false;
+  std::vector<gd::DevPart> parts;   // with ghost row / col data
+  gd::DBuf<gd::DevPart> d_parts;
+  int64_t ngdofs = 0;
+  int64_t nrows_total = 0;          // ngdofs owned rows + all ghost rows
+  int64_t nnz_total = 0;
+  int64_t nnz_own = 0;              // entries of the owned rows (prefix of the arrays)
+  int64_t total_gcols = 0;
+  int code_bytes = 1;
+  // concatenated row space: [owned rows of all parts in gid order][ghost rows of part 0]...
+  gd::DBuf<int64_t> rowptr;       // nrows_total + 1
+  gd::DBuf<int32_t> row_node;     // global lattice node of each row
+  gd::DBuf<int32_t> row_part;     // part that stores the row
+  gd::DBuf<int32_t> colidx;       // local column id (per part numbering)
+  gd::DBuf<int32_t> colgid;       // global column id (owned rows only are meaningful)
+  gd::DBuf<uint8_t> code;         // stencil offset code of each entry (1 or 2 bytes)
+  gd::DBuf<double> vals;
+  gd::DBuf<double> rhs;           // nrows_total (ghost rows zero)
+  // ghost rows: per concatenated ghost row: lid in its part
+  gd::DBuf<int32_t> grow_lid;
+  // ghost cols: per concatenated ghost col: lid in its part, gid, owner
+  gd::DBuf<int32_t> gcol_lid;
+  // per concatenated local node: local column id or -1
+  gd::DBuf<int32_t> node_col;
+  // reference element tables (device)
+  gd::DBuf<double> Khat, Mhat, Fhat;
+  int ref_degree = -1;
+  gd::DBuf<double> kappa_dev, f_dev;   // staging for host inputs
+  // solver workspace
+  gd::DBuf<double> w;              // vectors
+  gd::DBuf<double> dred;           // reduction partials
+  gd::DBuf<double> dinv;
+};

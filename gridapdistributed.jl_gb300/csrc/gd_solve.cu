@@ -1,0 +1,342 @@
+// A14-A16: mul!, the solve behind `\`, and FEFunction's consistent!.
+//
+// The owned rows of all parts, stored first and in gid order, form the global
+// matrix (global DOF ids are part-contiguous, FESpaces.jl:186-208), so SpMV runs over
+// them with global column ids and needs no halo exchange: on one device the
+// owner->ghost copy of consistent! is a gather from the global vector.
+// The reference's `\` gathers A and b to one part and runs a sparse LU
+// (PartitionedArrays 0.3); here the solve is Jacobi-preconditioned CG in FP64 with
+// deterministic two-stage reductions.
+#include <chrono>
+#include <cmath>
+#include <string>
+
+#include "gd_internal.h"
+
+namespace gd {
+
+constexpr int kSpmvThreads = 256;
+constexpr int kGroup = 8;                      // lanes per row
+constexpr int kRowsPerSpmvBlock = kSpmvThreads / kGroup;
+constexpr int kVecThreads = 256;
+constexpr int kMaxPartials = 1024;             // blocks that write partial sums
+
+struct Scalars {
+  double rz, pq, alpha, beta, rr, bb, rz_new;
+  int32_t done;
+};
+
+__device__ inline double block_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) sh[wid] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+  __syncthreads();
+  return s;   // valid in thread 0
+}
+
+// y = A x over owned rows; optional partial dot(y, w) per block (grid-stride over row groups)
+__global__ void __launch_bounds__(kSpmvThreads)
+k_spmv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+       const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y,
+       const double* __restrict__ w, double* __restrict__ partial) {
+  __shared__ double sh[kSpmvThreads / 32];
+  const int g = threadIdx.x / kGroup, l = threadIdx.x % kGroup;
+  double dot = 0.0;
+  // the loop bound is uniform across a warp so the shuffles see all 32 lanes
+  const int64_t stride = (int64_t)gridDim.x * kRowsPerSpmvBlock;
+  for (int64_t base = (int64_t)blockIdx.x * kRowsPerSpmvBlock + (g & ~(32 / kGroup - 1)); base < n; base += stride) {
+    const int64_t r = base + (g & (32 / kGroup - 1));
+    const bool valid = r < n;
+    const int64_t e0 = valid ? rowptr[r] : 0, e1 = valid ? rowptr[r + 1] : 0;
+    double s = 0.0;
+    for (int64_t e = e0 + l; e < e1; e += kGroup) s += val[e] * __ldg(x + col[e]);
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
+    if (l == 0 && valid) {
+      y[r] = s;
+      if (w) dot += s * w[r];
+    }
+  }
+  if (partial) {
+    double t = block_sum(dot, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  }
+}
+
+// r = b - A x (partial of r.r)
+__global__ void __launch_bounds__(kSpmvThreads)
+k_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+           const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ b,
+           double* __restrict__ r_out, double* __restrict__ partial_rr, double* __restrict__ partial_bb) {
+  __shared__ double sh[kSpmvThreads / 32];
+  const int g = threadIdx.x / kGroup, l = threadIdx.x % kGroup;
+  double rr = 0.0, bb = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * kRowsPerSpmvBlock;
+  for (int64_t base = (int64_t)blockIdx.x * kRowsPerSpmvBlock + (g & ~(32 / kGroup - 1)); base < n; base += stride) {
+    const int64_t r = base + (g & (32 / kGroup - 1));
+    const bool valid = r < n;
+    const int64_t e0 = valid ? rowptr[r] : 0, e1 = valid ? rowptr[r + 1] : 0;
+    double s = 0.0;
+    for (int64_t e = e0 + l; e < e1; e += kGroup) s += val[e] * __ldg(x + col[e]);
+#pragma unroll
+    for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
+    if (l == 0 && valid) {
+      double rv = b[r] - s;
+      if (r_out) r_out[r] = rv;
+      rr += rv * rv;
+      bb += b[r] * b[r];
+    }
+  }
+  double t = block_sum(rr, sh);
+  if (threadIdx.x == 0) partial_rr[blockIdx.x] = t;
+  t = block_sum(bb, sh);
+  if (threadIdx.x == 0) partial_bb[blockIdx.x] = t;
+}
+
+__global__ void k_dinv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                       const double* __restrict__ val, double* __restrict__ dinv, int32_t* __restrict__ bad) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  double d = 0.0;
+  for (int64_t e = rowptr[r]; e < rowptr[r + 1]; ++e)
+    if (col[e] == r) d = val[e];
+  if (!(d > 0.0) || !isfinite(d)) {
+    atomicAdd(bad, 1);
+    dinv[r] = 0.0;
+  } else {
+    dinv[r] = 1.0 / d;
+  }
+}
+
+// z = dinv*r, p = z, partial of r.z and r.r
+__global__ void k_pcg_init(int64_t n, const double* __restrict__ dinv, const double* __restrict__ r,
+                           double* __restrict__ z, double* __restrict__ p, double* __restrict__ prz,
+                           double* __restrict__ prr) {
+  __shared__ double sh[kVecThreads / 32];
+  double a = 0.0, b = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double zi = dinv[i] * r[i];
+    z[i] = zi;
+    p[i] = zi;
+    a += r[i] * zi;
+    b += r[i] * r[i];
+  }
+  double t = block_sum(a, sh);
+  if (threadIdx.x == 0) prz[blockIdx.x] = t;
+  t = block_sum(b, sh);
+  if (threadIdx.x == 0) prr[blockIdx.x] = t;
+}
+
+// x += alpha p; r -= alpha q; z = dinv r; partials r.z, r.r
+__global__ void k_pcg_update(int64_t n, const Scalars* __restrict__ sc, double* __restrict__ x,
+                             double* __restrict__ r, double* __restrict__ z, const double* __restrict__ p,
+                             const double* __restrict__ q, const double* __restrict__ dinv,
+                             double* __restrict__ prz, double* __restrict__ prr) {
+  __shared__ double sh[kVecThreads / 32];
+  const double alpha = sc->alpha;
+  double a = 0.0, b = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    x[i] += alpha * p[i];
+    double ri = r[i] - alpha * q[i];
+    r[i] = ri;
+    double zi = dinv[i] * ri;
+    z[i] = zi;
+    a += ri * zi;
+    b += ri * ri;
+  }
+  double t = block_sum(a, sh);
+  if (threadIdx.x == 0) prz[blockIdx.x] = t;
+  t = block_sum(b, sh);
+  if (threadIdx.x == 0) prr[blockIdx.x] = t;
+}
+
+__global__ void k_pcg_pupdate(int64_t n, const Scalars* __restrict__ sc, const double* __restrict__ z,
+                              double* __restrict__ p) {
+  const double beta = sc->beta;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    p[i] = z[i] + beta * p[i];
+}
+
+// one block: fixed-order sums of partials and the CG scalars
+// mode 0: init (rz, rr); 1: alpha from pq; 2: beta from rz_new, rr
+__global__ void k_pcg_scalars(int mode, int nb, const double* __restrict__ pa, const double* __restrict__ pb,
+                              Scalars* __restrict__ sc) {
+  __shared__ double sh[kVecThreads / 32];
+  double a = 0.0, b = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) {
+    a += pa[i];
+    if (pb) b += pb[i];
+  }
+  double sa = block_sum(a, sh);
+  double sb = block_sum(b, sh);
+  if (threadIdx.x != 0) return;
+  if (mode == 0) {
+    sc->rz = sa;
+    sc->rr = sb;
+  } else if (mode == 1) {
+    sc->pq = sa;
+    sc->alpha = sa != 0.0 ? sc->rz / sa : 0.0;
+  } else {
+    sc->beta = sc->rz != 0.0 ? sa / sc->rz : 0.0;
+    sc->rz = sa;
+    sc->rr = sb;
+  }
+}
+
+__global__ void k_gather_local(int64_t n, const int64_t* __restrict__ lid_gid, const double* __restrict__ xg,
+                               double* __restrict__ xl) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) xl[i] = xg[lid_gid[i]];
+}
+
+static int grid_for(int64_t n, int per_block) {
+  int64_t b = (n + per_block - 1) / per_block;
+  if (b > kMaxPartials) b = kMaxPartials;
+  if (b < 1) b = 1;
+  return (int)b;
+}
+
+}  // namespace gd
+
+using namespace gd;
+
+static int check_ready(const gd_asm* A, const char* fn) {
+  if (!A) return fail(GD_ERR_ARG, std::string(fn) + ": null assembler");
+  if (!A->numeric_done) return fail(GD_ERR_STATE, std::string(fn) + ": run gd_assemble_numeric first");
+  return GD_OK;
+}
+
+extern "C" int gd_spmv(gd_asm* A, const double* x, double* y, int where) {
+  GD_TRY(check_ready(A, "gd_spmv"));
+  if (!x || !y) return fail(GD_ERR_ARG, "gd_spmv: null vector");
+  cudaStream_t st = A->test->model->ctx->stream;
+  const int64_t n = A->ngdofs;
+  const double* dx = x;
+  double* dy = y;
+  DBuf<double> tx, ty;
+  if (where == GD_HOST) {
+    GD_TRY(dalloc(tx, n));
+    GD_TRY(dalloc(ty, n));
+    GD_CUDA_TRY(cudaMemcpyAsync(tx.p, x, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    dx = tx.p;
+    dy = ty.p;
+  }
+  k_spmv<<<grid_for(n, kRowsPerSpmvBlock), kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, dy,
+                                                                  nullptr, nullptr);
+  GD_CUDA_TRY(cudaGetLastError());
+  if (where == GD_HOST) GD_CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  dfreeb(tx);
+  dfreeb(ty);
+  return GD_OK;
+}
+
+extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x, int where, gd_solve_stats* stats) {
+  GD_TRY(check_ready(A, "gd_solve"));
+  if (method != GD_SOLVE_JACOBI_PCG) return fail(GD_ERR_UNSUPPORTED, "gd_solve: unknown method");
+  if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve: bad argument");
+  cudaStream_t st = A->test->model->ctx->stream;
+  const int64_t n = A->ngdofs;
+  auto t0 = std::chrono::steady_clock::now();
+  // workspace: x r z p q (5n) + dinv (n); partial sums + scalars in dred
+  if (A->w.n < (size_t)(5 * n)) GD_TRY(dalloc(A->w, 5 * std::max<int64_t>(n, 1)));
+  if (A->dinv.n < (size_t)n) GD_TRY(dalloc(A->dinv, std::max<int64_t>(n, 1)));
+  if (!A->dred.p) GD_TRY(dalloc(A->dred, 4096));
+  double* dx = A->w.p;
+  double* dr = dx + n;
+  double* dz = dr + n;
+  double* dp = dz + n;
+  double* dq = dp + n;
+  double* pa = A->dred.p + 16;
+  double* pb = pa + kMaxPartials;
+  Scalars* sc = (Scalars*)(A->dred.p + 16 + 2 * kMaxPartials);
+  int32_t* bad = (int32_t*)A->dred.p;
+  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
+  GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
+  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, A->dinv.p, bad);
+  GD_CUDA_TRY(cudaGetLastError());
+  const int gs = grid_for(n, kRowsPerSpmvBlock);
+  const int gv = grid_for(n, kVecThreads);
+  // r = b - A*0 = b ; bb
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, dr, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);   // rz <- bb (temp), rr <- rr
+  GD_CUDA_TRY(cudaGetLastError());
+  Scalars h{};
+  int32_t hbad = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hbad) return fail(GD_ERR_NUMERIC, "gd_solve: non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
+  const double bnorm = std::sqrt(h.rz);
+  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, A->dinv.p, dr, dz, dp, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
+  GD_CUDA_TRY(cudaGetLastError());
+  int it = 0;
+  bool conv = bnorm == 0.0;
+  const int check_every = 8;
+  while (!conv && it < maxit) {
+    int nstep = std::min(check_every, maxit - it);
+    for (int s = 0; s < nstep; ++s) {
+      k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
+      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
+      k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, A->dinv.p, pa, pb);
+      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
+      k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
+    }
+    GD_CUDA_TRY(cudaGetLastError());
+    it += nstep;
+    GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!std::isfinite(h.rr)) break;
+    if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
+  }
+  // true FP64 residual
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, nullptr, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(x, dx, sizeof(double) * n,
+                              where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  const double rel = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
+  if (stats) {
+    stats->iterations = it;
+    stats->converged = rel <= rtol;
+    stats->rel_residual = rel;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, "gd_solve: residual is not finite");
+  if (rel > rtol) return fail(GD_ERR_NOTCONVERGED, "gd_solve: tolerance not reached in " + std::to_string(it) + " iterations");
+  return GD_OK;
+}
+
+extern "C" int gd_fe_function_local(const gd_space* S, int part, const double* x_global, int where, double* x_local) {
+  if (!S || part < 0 || part >= S->geom.nparts || !x_global || !x_local)
+    return fail(GD_ERR_ARG, "gd_fe_function_local: bad argument");
+  cudaStream_t st = S->model->ctx->stream;
+  const DevPart& P = S->parts[part];
+  const int64_t n = P.nfree;
+  DBuf<double> xg, xl;
+  const double* dxg = x_global;
+  if (where == GD_HOST) {
+    GD_TRY(dalloc(xg, std::max<int64_t>(S->ngdofs, 1)));
+    GD_CUDA_TRY(cudaMemcpyAsync(xg.p, x_global, sizeof(double) * S->ngdofs, cudaMemcpyHostToDevice, st));
+    dxg = xg.p;
+    GD_TRY(dalloc(xl, std::max<int64_t>(n, 1)));
+  }
+  double* dxl = where == GD_HOST ? xl.p : x_local;
+  if (n > 0) {
+    k_gather_local<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, S->lid_gid.p + P.lid_off, dxg, dxl);
+    GD_CUDA_TRY(cudaGetLastError());
+  }
+  if (where == GD_HOST && n > 0)
+    GD_CUDA_TRY(cudaMemcpyAsync(x_local, dxl, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  dfreeb(xg);
+  dfreeb(xl);
+  return GD_OK;
+}

@@ -1,0 +1,14 @@
+"""GB300 assembly-and-solve backend for GridapDistributed-style Cartesian problems.
+
+``distributed`` mirrors the reference's Julia API over the C ABI in
+``include/gdgpu.h``; ``_lib`` is the ctypes binding of ``libgdgpu.so``.
+"""
+from . import _lib
+from .distributed import (AffineFEOperator, CartesianDiscreteModel, FEFunction, FESpace,
+                          FullyAssembledRows, GB300Backend, Measure, PSparseMatrix, PVector,
+                          ReferenceFE, SparseMatrixAssembler, SubAssembledRows, TestFESpace,
+                          Triangulation, TrialFESpace, assemble_matrix_and_vector,
+                          collect_cell_matrix_and_vector, integral_grad_grad, integral_source,
+                          lagrangian, solve, with_gb300)
+
+__all__ = [n for n in dir() if not n.startswith("_")]

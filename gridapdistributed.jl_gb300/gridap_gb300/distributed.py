@@ -1,0 +1,527 @@
+"""Python mirror of GridapDistributed's assembly-and-solve API over libgdgpu.so.
+
+The names, argument meanings and return types follow the Julia API so that a
+script reads like the reference's tests (``test/FESpacesTests.jl``,
+``test/PoissonTests.jl``)::
+
+    with_gb300(lambda distribute: ...)                  # with_debug(f)
+    ranks = distribute(range(4))                         # distribute(LinearIndices((4,)))
+    model = CartesianDiscreteModel(ranks, (2, 2), (0, 1, 0, 1), (16, 16))
+    V = TestFESpace(model, ReferenceFE(lagrangian, float, 2), dirichlet_tags="boundary")
+    U = TrialFESpace(lambda x, y: (x + y) ** 2, V)
+    dΩ = Measure(Triangulation(model), 4)
+    a = integral_grad_grad(kappa=None, measure=dΩ)      # a(u,v) = ∫(κ ∇v⋅∇u)dΩ
+    l = integral_source(f=-4.0, measure=dΩ)             # l(v)   = ∫(v f)dΩ
+    op = AffineFEOperator(a, l, U, V)                    # A = op.matrix, b = op.vector
+    uh = solve(op)
+
+Weak forms are limited to what the device kernels implement: cell-constant
+diffusion ``∫(κ ∇v⋅∇u)`` and sources ``∫(v f)`` with constant or nodal f (the
+latter assembled as M f).  Every compute call goes to the C ABI; nothing here
+falls back to the CPU.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import _lib as L
+
+lagrangian = "lagrangian"
+
+
+class SubAssembledRows:
+    code = L.GD_SUB_ASSEMBLED_ROWS
+
+
+class FullyAssembledRows:
+    code = L.GD_FULLY_ASSEMBLED_ROWS
+
+
+# --------------------------------------------------------------------------------------
+# backend / ranks (with_debug + distribute)
+# --------------------------------------------------------------------------------------
+class GB300Backend:
+    """One CUDA context; every part of a partition lives on this device."""
+
+    def __init__(self, device: int = 0):
+        L.load()
+        h = C.c_void_p()
+        L.call("gd_ctx_create", device, C.byref(h))
+        self.handle = h
+        self.device = device
+
+    def distribute(self, ids):
+        return Ranks(list(ids), self)
+
+    def set_stream(self, stream_handle: int | None):
+        L.call("gd_ctx_set_stream", self.handle, C.c_void_p(stream_handle or 0))
+
+    def close(self):
+        if self.handle:
+            L.load().gd_ctx_destroy(self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def with_gb300(f, device: int = 0):
+    """``with_debug(f)`` counterpart: runs ``f(distribute)`` with all parts on one GPU."""
+    be = GB300Backend(device)
+    try:
+        return f(be.distribute)
+    finally:
+        be.close()
+
+
+@dataclass
+class Ranks:
+    ids: list
+    backend: GB300Backend
+
+    def __len__(self):
+        return len(self.ids)
+
+
+# --------------------------------------------------------------------------------------
+# model (Geometry.jl:378-411)
+# --------------------------------------------------------------------------------------
+class DistributedDiscreteModel:
+    def __init__(self, ranks: Ranks, parts, domain, cells):
+        if int(np.prod(parts)) != len(ranks):
+            raise ValueError("prod(parts) must equal the number of ranks")
+        if len(domain) != 2 * len(cells) or len(parts) != len(cells):
+            raise ValueError("domain/cells/parts dimensions disagree")
+        self.ranks = ranks
+        self.backend = ranks.backend
+        self.dim = len(cells)
+        self.parts = tuple(int(p) for p in parts)
+        self.cells = tuple(int(c) for c in cells)
+        self.domain = tuple(float(x) for x in domain)
+        h = C.c_void_p()
+        cells_a = np.array(self.cells, dtype=np.int64)
+        parts_a = np.array(self.parts, dtype=np.int32)
+        dom_a = np.array(self.domain, dtype=np.float64)
+        L.call("gd_model_cartesian", self.backend.handle, self.dim, L.ptr(cells_a, C.c_int64),
+               L.ptr(parts_a, C.c_int32), L.ptr(dom_a, C.c_double), C.byref(h))
+        self.handle = h
+
+    @property
+    def num_parts(self):
+        return int(np.prod(self.parts))
+
+    def part_boxes(self, p):
+        a = [np.zeros(self.dim, dtype=np.int64) for _ in range(4)]
+        L.call("gd_model_part_boxes", self.handle, p, *[L.ptr(x, C.c_int64) for x in a])
+        return tuple(tuple(int(v) for v in x) for x in a)   # own_lo, own_hi, loc_lo, loc_hi
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.load().gd_model_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def CartesianDiscreteModel(ranks, parts, domain, cells):
+    return DistributedDiscreteModel(ranks, parts, domain, cells)
+
+
+@dataclass
+class Triangulation:
+    model: DistributedDiscreteModel
+    portion: object = None
+
+
+@dataclass
+class Measure:
+    trian: Triangulation
+    degree: int
+
+
+def ReferenceFE(name, T, order):
+    if name != lagrangian or T not in (float, np.float64):
+        raise NotImplementedError("only scalar Lagrangian Float64 reference FEs")
+    return ("lagrangian", float, int(order))
+
+
+# --------------------------------------------------------------------------------------
+# FE spaces and gids (FESpaces.jl:139-261, 570-614)
+# --------------------------------------------------------------------------------------
+@dataclass
+class LocalIndices:
+    """``LocalIndices(ngdofs, me, ldof_to_gdof, ldof_to_owner)`` (0-based)."""
+
+    n_global: int
+    part: int
+    local_to_global: np.ndarray
+    local_to_owner: np.ndarray
+
+    @property
+    def own_mask(self):
+        return self.local_to_owner == self.part
+
+    def own_length(self):
+        return int(self.own_mask.sum())
+
+    def local_length(self):
+        return len(self.local_to_global)
+
+
+@dataclass
+class OwnAndGhostIndices:
+    n_global: int
+    part: int
+    own_to_global: np.ndarray
+    ghost_to_global: np.ndarray
+    ghost_to_owner: np.ndarray
+
+    def local_length(self):
+        return len(self.own_to_global) + len(self.ghost_to_global)
+
+    def own_length(self):
+        return len(self.own_to_global)
+
+    @property
+    def local_to_global(self):
+        return np.concatenate([self.own_to_global, self.ghost_to_global])
+
+
+class PRange:
+    def __init__(self, partition):
+        self._partition = partition
+
+    def partition(self):
+        return self._partition
+
+    def __len__(self):
+        return self._partition[0].n_global if self._partition else 0
+
+
+def _sides_from_tags(dim, dirichlet_tags):
+    if dirichlet_tags is None or dirichlet_tags == [] or dirichlet_tags == ():
+        return np.zeros(2 * dim, dtype=np.int32)
+    if isinstance(dirichlet_tags, str):
+        dirichlet_tags = [dirichlet_tags]
+    names = ["left", "right", "bottom", "top", "back", "front"]   # x0 x1 y0 y1 z0 z1
+    s = np.zeros(2 * dim, dtype=np.int32)
+    for t in dirichlet_tags:
+        if t == "boundary":
+            s[:] = 1
+        elif t in names[: 2 * dim]:
+            s[names.index(t)] = 1
+        else:
+            raise NotImplementedError(f"dirichlet tag {t!r}: use 'boundary' or one of {names[:2*dim]}")
+    return s
+
+
+class DistributedSingleFieldFESpace:
+    def __init__(self, model: DistributedDiscreteModel, reffe, dirichlet_tags="boundary"):
+        self.model = model
+        self.order = reffe[2]
+        self.sides = _sides_from_tags(model.dim, dirichlet_tags)
+        h = C.c_void_p()
+        L.call("gd_space_create", model.handle, self.order, 1, L.ptr(self.sides, C.c_int32), C.byref(h))
+        self.handle = h
+        self._gids = None
+        self.dirichlet_values = None
+
+    def num_free_dofs(self):
+        n = C.c_int64()
+        L.call("gd_space_num_free_dofs", self.handle, C.byref(n))
+        return n.value
+
+    def local_sizes(self, p):
+        a, b, c = C.c_int64(), C.c_int64(), C.c_int64()
+        L.call("gd_space_local_sizes", self.handle, p, C.byref(a), C.byref(b), C.byref(c))
+        return a.value, b.value, c.value
+
+    @property
+    def gids(self) -> PRange:
+        """``get_free_dof_ids(V)``: the DOF PRange built by generate_gids."""
+        if self._gids is None:
+            n = self.num_free_dofs()
+            parts = []
+            for p in range(self.model.num_parts):
+                nl, _, _ = self.local_sizes(p)
+                g = np.zeros(nl, dtype=np.int64)
+                o = np.zeros(nl, dtype=np.int32)
+                L.call("gd_space_get_gids", self.handle, p, L.ptr(g, C.c_int64), L.ptr(o, C.c_int32))
+                parts.append(LocalIndices(n, p, g, o))
+            self._gids = PRange(parts)
+        return self._gids
+
+    def dof_nodes(self, p):
+        nl, _, _ = self.local_sizes(p)
+        out = np.zeros(nl, dtype=np.int64)
+        L.call("gd_space_dof_nodes", self.handle, p, L.ptr(out, C.c_int64))
+        return out
+
+    # lattice helpers ------------------------------------------------------------------
+    @property
+    def lattice(self):
+        return tuple(self.order * c + 1 for c in self.model.cells)
+
+    def lattice_xyz(self):
+        """Coordinates of every global lattice node, (N, dim), x fastest."""
+        N = self.lattice
+        idx = np.indices(tuple(reversed(N))).reshape(self.model.dim, -1)[::-1]
+        h = [(self.model.domain[2 * d + 1] - self.model.domain[2 * d]) / (self.order * self.model.cells[d])
+             for d in range(self.model.dim)]
+        return np.stack([self.model.domain[2 * d] + idx[d] * h[d] for d in range(self.model.dim)], axis=1)
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.load().gd_space_destroy(self.handle)
+        except Exception:
+            pass
+
+
+def TestFESpace(model, reffe, dirichlet_tags="boundary", conformity=None):
+    if conformity not in (None, "H1", ":H1"):
+        raise NotImplementedError("only conforming (H1) spaces")
+    return DistributedSingleFieldFESpace(model, reffe, dirichlet_tags)
+
+
+FESpace = TestFESpace
+
+
+def TrialFESpace(u, V: DistributedSingleFieldFESpace):
+    """``TrialFESpace(u, V)``: nodal interpolation of ``u`` on the Dirichlet nodes.
+
+    ``u`` is a number, a vectorised callable of the coordinates, or a dense
+    array over the global node lattice."""
+    if u is None or (np.isscalar(u) and u == 0):
+        L.call("gd_space_set_dirichlet", V.handle, None, L.GD_HOST)
+        V.dirichlet_values = None
+        return V
+    if callable(u):
+        xyz = V.lattice_xyz()
+        vals = np.asarray(u(*[xyz[:, d] for d in range(V.model.dim)]), dtype=np.float64)
+        vals = np.broadcast_to(vals, (xyz.shape[0],)).copy()
+    elif np.isscalar(u):
+        vals = np.full(int(np.prod(V.lattice)), float(u))
+    else:
+        vals = np.ascontiguousarray(u, dtype=np.float64)
+    L.call("gd_space_set_dirichlet", V.handle, L.ptr(vals, C.c_double), L.GD_HOST)
+    V.dirichlet_values = vals
+    return V
+
+
+# --------------------------------------------------------------------------------------
+# weak forms (restricted vocabulary) and assembly (FESpaces.jl:746-862, Algebra.jl)
+# --------------------------------------------------------------------------------------
+@dataclass
+class GradGradForm:
+    """a(u,v) = ∫( κ ∇(v)⋅∇(u) )dΩ with κ per global cell (None = 1)."""
+
+    kappa: np.ndarray | None
+    measure: Measure
+
+
+@dataclass
+class SourceForm:
+    """l(v) = ∫( v f )dΩ with f constant or nodal (dense over the lattice)."""
+
+    f: object
+    measure: Measure
+
+
+def integral_grad_grad(kappa=None, measure: Measure = None):
+    return GradGradForm(None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64), measure)
+
+
+def integral_source(f=0.0, measure: Measure = None):
+    return SourceForm(f, measure)
+
+
+def SparseMatrixAssembler(U, V, strategy=None):
+    return DistributedSparseMatrixAssembler(U, V, strategy or SubAssembledRows())
+
+
+class DistributedSparseMatrixAssembler:
+    def __init__(self, U, V, strategy):
+        self.U, self.V, self.strategy = U, V, strategy
+        h = C.c_void_p()
+        L.call("gd_assembler_create", U.handle, V.handle, strategy.code, C.byref(h))
+        self.handle = h
+        self._symbolic = False
+
+    def symbolic(self):
+        if not self._symbolic:
+            L.call("gd_assemble_symbolic", self.handle)
+            self._symbolic = True
+
+    def numeric(self, a: GradGradForm, l: SourceForm):
+        self.symbolic()
+        keep = []
+        c = L.gd_coeffs()
+        c.kappa = None if a.kappa is None else a.kappa.ctypes.data
+        if a.kappa is not None:
+            keep.append(a.kappa)
+        f = l.f if l is not None else 0.0
+        if np.isscalar(f):
+            c.f_nodal = None
+            c.f_const = float(f)
+        else:
+            fa = np.ascontiguousarray(f, dtype=np.float64)
+            keep.append(fa)
+            c.f_nodal = fa.ctypes.data
+            c.f_const = 0.0
+        c.degree = int(a.measure.degree if a.measure is not None else 2 * self.V.order)
+        c.where = L.GD_HOST
+        L.call("gd_assemble_numeric", self.handle, C.byref(c))
+
+    def __del__(self):
+        try:
+            if self.handle:
+                L.load().gd_assembler_destroy(self.handle)
+        except Exception:
+            pass
+
+
+class PSparseMatrix:
+    """A PSparseMatrix whose parts live on the device; host copies on request."""
+
+    def __init__(self, assem: DistributedSparseMatrixAssembler):
+        self.assem = assem
+        self._parts = None
+
+    @property
+    def n_global(self):
+        return self.assem.V.num_free_dofs()
+
+    def _export(self):
+        if self._parts is not None:
+            return self._parts
+        import scipy.sparse as sps
+        V = self.assem.V
+        out = []
+        for p in range(V.model.num_parts):
+            nr, nc, nnz, ngr, ngc = (C.c_int64() for _ in range(5))
+            L.call("gd_matrix_sizes", self.assem.handle, p, *[C.byref(x) for x in (nr, nc, nnz, ngr, ngc)])
+            rp = np.zeros(nr.value + 1, dtype=np.int64)
+            ci = np.zeros(nnz.value, dtype=np.int32)
+            vv = np.zeros(nnz.value, dtype=np.float64)
+            grg = np.zeros(ngr.value, dtype=np.int64)
+            gro = np.zeros(ngr.value, dtype=np.int32)
+            gcg = np.zeros(ngc.value, dtype=np.int64)
+            gco = np.zeros(ngc.value, dtype=np.int32)
+            L.call("gd_matrix_export", self.assem.handle, p, L.ptr(rp, C.c_int64), L.ptr(ci, C.c_int32),
+                   L.ptr(vv, C.c_double), L.ptr(grg, C.c_int64), L.ptr(gro, C.c_int32), L.ptr(gcg, C.c_int64),
+                   L.ptr(gco, C.c_int32))
+            _, nown, first = V.local_sizes(p)
+            own = np.arange(first, first + nown, dtype=np.int64)
+            rows = OwnAndGhostIndices(self.n_global, p, own, grg, gro)
+            cols = OwnAndGhostIndices(self.n_global, p, own, gcg, gco)
+            mat = sps.csr_matrix((vv, ci, rp), shape=(nr.value, nc.value))
+            out.append((mat, rows, cols, (rp, ci, vv)))
+        self._parts = out
+        return out
+
+    @property
+    def matrix_partition(self):
+        return [m for m, _, _, _ in self._export()]
+
+    @property
+    def row_partition(self):
+        return [r for _, r, _, _ in self._export()]
+
+    @property
+    def col_partition(self):
+        return [c for _, _, c, _ in self._export()]
+
+    def csr_parts(self):
+        return [raw for _, _, _, raw in self._export()]
+
+    def __matmul__(self, x):
+        return self.mul(x)
+
+    def mul(self, x: np.ndarray) -> np.ndarray:
+        """``A*x`` for a global vector (PVector over the owned rows)."""
+        x = np.ascontiguousarray(x, dtype=np.float64)
+        y = np.zeros(self.n_global)
+        L.call("gd_spmv", self.assem.handle, L.vptr(x), L.vptr(y), L.GD_HOST)
+        return y
+
+    def solve(self, rtol=1e-12, maxit=100000):
+        """``A \\ b`` for the assembled right-hand side: Jacobi-PCG in FP64."""
+        x = np.zeros(self.n_global)
+        st = L.gd_solve_stats()
+        L.call("gd_solve", self.assem.handle, L.GD_SOLVE_JACOBI_PCG, float(rtol), int(maxit), L.vptr(x), L.GD_HOST,
+               C.byref(st))
+        self.last_stats = st
+        return x
+
+
+class PVector:
+    def __init__(self, assem: DistributedSparseMatrixAssembler, matrix: PSparseMatrix):
+        self.assem = assem
+        self.matrix = matrix
+
+    @property
+    def partition(self):
+        out = []
+        for p, (mat, rows, _, _) in enumerate(self.matrix._export()):
+            b = np.zeros(mat.shape[0])
+            L.call("gd_vector_export", self.assem.handle, p, L.ptr(b, C.c_double))
+            out.append(b)
+        return out
+
+    def global_values(self):
+        b = np.zeros(self.matrix.n_global)
+        L.call("gd_system_download", self.assem.handle, L.ptr(b, C.c_double), None)
+        return b
+
+
+def collect_cell_matrix_and_vector(U, V, a, l, uhd=None):
+    return (a, l)
+
+
+def assemble_matrix_and_vector(assem: DistributedSparseMatrixAssembler, data):
+    a, l = data
+    assem.numeric(a, l)
+    A = PSparseMatrix(assem)
+    return A, PVector(assem, A)
+
+
+class AffineFEOperator:
+    def __init__(self, a, l, U, V, assem=None):
+        self.U, self.V = U, V
+        self.assem = assem if assem is not None else SparseMatrixAssembler(U, V)
+        self.matrix, self.vector = assemble_matrix_and_vector(self.assem, (a, l))
+
+
+class FEFunction:
+    """``FEFunction(U, x)``: free values made consistent on every part."""
+
+    def __init__(self, U: DistributedSingleFieldFESpace, x: np.ndarray):
+        self.U = U
+        self.free_values = np.ascontiguousarray(x, dtype=np.float64)
+
+    def local_values(self, p):
+        nl, _, _ = self.U.local_sizes(p)
+        out = np.zeros(nl)
+        L.call("gd_fe_function_local", self.U.handle, p, L.vptr(self.free_values), L.GD_HOST,
+               L.ptr(out, C.c_double))
+        return out
+
+    def nodal_values(self):
+        """Dense lattice array of nodal values (Dirichlet values from the trial space)."""
+        N = int(np.prod(self.U.lattice))
+        u = np.zeros(N) if self.U.dirichlet_values is None else self.U.dirichlet_values.copy()
+        for p in range(self.U.model.num_parts):
+            u[self.U.dof_nodes(p)] = self.local_values(p)
+        return u
+
+
+def solve(op: AffineFEOperator, rtol=1e-12, maxit=100000):
+    x = op.matrix.solve(rtol=rtol, maxit=maxit)
+    return FEFunction(op.U, x)

@@ -1,0 +1,191 @@
+/*
+ * gdgpu.h -- C ABI of the GB300 assembly-and-solve library (libgdgpu.so).
+ *
+ * The library replaces, for Cartesian meshes, the path
+ *   CartesianDiscreteModel(ranks, parts, domain, cells)
+ *   -> TestFESpace / TrialFESpace
+ *   -> SparseMatrixAssembler(U, V, strategy)
+ *   -> assemble_matrix_and_vector (-> PSparseMatrix / PVector)
+ *   -> A \ b
+ * of GridapDistributed.jl.  Every part of the mesh partition lives on one GPU as a
+ * slab of device memory; the PartitionedArrays exchanges become device
+ * gather/scatter kernels.
+ *
+ * Conventions
+ *  - Every function returns an int status (GD_OK = 0).  On failure a message is
+ *    kept per host thread and returned by gd_last_error().  No exception crosses
+ *    the ABI, nothing calls exit/abort.
+ *  - Indices are 0-based.  Global DOF ids are int64, part ids and local ids int32.
+ *    (The Julia side adds 1 to obtain PartitionedArrays' 1-based ids.)
+ *  - Parts are numbered x-fastest (Julia's CartesianIndices(parts) order).
+ *    Cells and lattice nodes are numbered lexicographically, x fastest.  The
+ *    "node lattice" of an order-k space has k*cells[d]+1 nodes along d.
+ *  - Device memory belongs to the object that allocated it and is freed by the
+ *    matching *_destroy.  Host buffers are owned by the caller and are only
+ *    read or written during the call.  Export functions accept NULL for any
+ *    output they should skip; query sizes first with gd_matrix_sizes.
+ *  - All device work is ordered on the context's stream.  Calls return after
+ *    the stream has been synchronised unless their comment says otherwise.
+ */
+#ifndef GDGPU_H
+#define GDGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ---------------------------------------------------------- */
+enum {
+  GD_OK = 0,
+  GD_ERR_ARG = 1,          /* invalid argument (sizes, pointers, ranges)              */
+  GD_ERR_OOM = 2,          /* device or host allocation failed                        */
+  GD_ERR_CUDA = 3,         /* a CUDA runtime call failed                              */
+  GD_ERR_TIMEOUT = 4,      /* a bounded device wait ran out                           */
+  GD_ERR_STALL = 5,        /* iterative solve stalled (the fallback result is kept)   */
+  GD_ERR_STATE = 6,        /* call out of order (e.g. numeric before symbolic)        */
+  GD_ERR_UNSUPPORTED = 7,  /* configuration not built                                 */
+  GD_ERR_NUMERIC = 8,      /* NaN / Inf / non-positive coefficient in the input       */
+  GD_ERR_NOTCONVERGED = 9  /* maximum iterations reached before the tolerance         */
+};
+
+/* Assembly strategies (src/Algebra.jl:397-398). */
+enum { GD_SUB_ASSEMBLED_ROWS = 0, GD_FULLY_ASSEMBLED_ROWS = 1 };
+
+/* Solver methods behind `\` (the reference's own is a gathered sparse LU). */
+enum { GD_SOLVE_JACOBI_PCG = 1 };
+
+/* Where a coefficient/input pointer lives. */
+enum { GD_HOST = 0, GD_DEVICE = 1 };
+
+typedef struct gd_ctx gd_ctx;
+typedef struct gd_model gd_model;
+typedef struct gd_space gd_space;
+typedef struct gd_asm gd_asm;
+
+/* Thread-local message of the last failed call on this host thread ("" if none). */
+const char* gd_last_error(void);
+
+/* Library version string. */
+const char* gd_version(void);
+
+/* ---- context --------------------------------------------------------------- */
+/* A context owns one CUDA device and one stream.  No reference counterpart: it
+ * stands in for the `ranks` array handed to every constructor (with_debug's
+ * DebugArray), since all parts of the partition live on this device. */
+int gd_ctx_create(int device, gd_ctx** out);
+int gd_ctx_destroy(gd_ctx* ctx);
+/* Order all subsequent work of `ctx` on an externally owned cudaStream_t
+ * (NULL restores the context's own stream). */
+int gd_ctx_set_stream(gd_ctx* ctx, void* cuda_stream);
+int gd_ctx_synchronize(gd_ctx* ctx);
+
+/* ---- A1: CartesianDiscreteModel(ranks, parts, domain, cells) ---------------
+ * Replaces Geometry.jl:378-411 and _uniform_partition / _block_with_constant_size
+ * / _local_range (PArraysExtras.jl:5-84): block partition of `cells` into
+ * `parts` with a one-cell ghost layer.  Non-periodic only.
+ * domain = (x0,x1,y0,y1[,z0,z1]); dim = 2 or 3.                                  */
+int gd_model_cartesian(gd_ctx* ctx, int dim, const int64_t* cells, const int32_t* parts,
+                       const double* domain, gd_model** out);
+int gd_model_destroy(gd_model* model);
+int gd_model_num_parts(const gd_model* model, int32_t* nparts);
+/* Owned and local (owned+ghost) cell boxes of `part`, 0-based half-open
+ * [lo, hi) per direction (each array has `dim` entries). */
+int gd_model_part_boxes(const gd_model* model, int part, int64_t* own_lo, int64_t* own_hi,
+                        int64_t* loc_lo, int64_t* loc_hi);
+
+/* ---- A3-A5: TestFESpace / TrialFESpace ---------------------------------------
+ * Replaces FESpaces.jl:570-614 (per-part Lagrangian Q_k space on owned+ghost
+ * cells, Gridap's conforming numbering) and generate_gids (FESpaces.jl:139-261).
+ * dirichlet_sides[2*d] / [2*d+1] flag the planes x_d = min / max; a node on a
+ * flagged plane is a Dirichlet node ("boundary" = all flags set).
+ * Scalar spaces (ncomp = 1), order 1..3.                                          */
+int gd_space_create(gd_model* model, int order, int ncomp, const int32_t* dirichlet_sides,
+                    gd_space** out);
+int gd_space_destroy(gd_space* space);
+/* num_free_dofs(V) (global). */
+int gd_space_num_free_dofs(const gd_space* space, int64_t* n);
+/* Local sizes of one part: local free DOFs, owned DOFs, first owned gid. */
+int gd_space_local_sizes(const gd_space* space, int part, int64_t* nldofs, int64_t* nown,
+                         int64_t* first_gdof);
+/* LocalIndices of one part: ldof -> gid and ldof -> owner (FESpaces.jl:248-258). */
+int gd_space_get_gids(const gd_space* space, int part, int64_t* ldof_to_gdof,
+                      int32_t* ldof_to_owner);
+/* Global lattice node index of every local free DOF of one part. */
+int gd_space_dof_nodes(const gd_space* space, int part, int64_t* ldof_to_node);
+/* TrialFESpace(u, V) (FESpaces.jl:396-401): Dirichlet values as a dense array
+ * over the global node lattice (only Dirichlet nodes are read); NULL = zero. */
+int gd_space_set_dirichlet(gd_space* space, const double* u_lattice, int where);
+
+/* ---- A9-A13: SparseMatrixAssembler + assemble_matrix_and_vector --------------
+ * Replaces DistributedSparseMatrixAssembler (FESpaces.jl:746-862) and the
+ * PSparseMatrixBuilderCOO / PVectorBuilder protocol with create_from_nz
+ * (Algebra.jl:405-907): SubAssembledRows (ghost rows kept with explicit zeros,
+ * ghost columns in first-appearance order) or FullyAssembledRows (no ghost rows,
+ * ghost columns sorted by local DOF id).                                          */
+int gd_assembler_create(gd_space* trial, gd_space* test, int strategy, gd_asm** out);
+int gd_assembler_destroy(gd_asm* a);
+/* allocate_matrix_and_vector: builds row/col index sets and the local CSR
+ * patterns of every part (Algebra.jl:593-646 without the values). */
+int gd_assemble_symbolic(gd_asm* a);
+
+/* Coefficients of a(u,v) = int(kappa grad(v).grad(u)) and l(v) = int(v f). */
+typedef struct gd_coeffs {
+  const double* kappa;   /* per global cell (lexicographic); NULL = 1        */
+  const double* f_nodal; /* per global lattice node (load M*f); NULL = const */
+  double f_const;        /* constant source when f_nodal is NULL             */
+  int degree;            /* quadrature degree (tensor Gauss, (degree+2)/2 pts/dir) */
+  int where;             /* GD_HOST or GD_DEVICE for the pointers above      */
+} gd_coeffs;
+
+/* assemble_matrix_and_vector! into the symbolic pattern: matrix values and the
+ * right-hand side of every part.  Deterministic (no floating-point atomics). */
+int gd_assemble_numeric(gd_asm* a, const gd_coeffs* c);
+/* Same, without the final stream synchronisation (for timing loops). */
+int gd_assemble_numeric_async(gd_asm* a, const gd_coeffs* c);
+
+/* Sizes of one part's local matrix: rows (owned + ghost), columns (owned + ghost),
+ * stored entries, ghost rows, ghost columns. */
+int gd_matrix_sizes(const gd_asm* a, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
+                    int64_t* n_ghost_rows, int64_t* n_ghost_cols);
+/* One part of the PSparseMatrix: local CSR (rowptr[nrows+1], colidx[nnz],
+ * vals[nnz], columns sorted within a row) plus the ghost parts of its row and
+ * column OwnAndGhostIndices (owned gids are first_gdof .. first_gdof+nown-1). */
+int gd_matrix_export(const gd_asm* a, int part, int64_t* rowptr, int32_t* colidx, double* vals,
+                     int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
+                     int32_t* ghost_col_owners);
+/* One part of the PVector over the matrix rows (ghost entries are zero after
+ * assemble!, Algebra.jl:786-789). */
+int gd_vector_export(const gd_asm* a, int part, double* b);
+/* Device pointers of the assembled system seen as one global CSR over the
+ * owned rows (gid order): rowptr (int64, ngdofs+1), global column ids (int32),
+ * values (double), rhs (double, ngdofs).  Valid until the assembler is destroyed. */
+int gd_system_device_ptrs(const gd_asm* a, const int64_t** rowptr, const int32_t** colidx,
+                          const double** vals, const double** rhs, int64_t* ngdofs);
+/* Copy the global rhs (ngdofs) and optionally all owned-row values to host. */
+int gd_system_download(const gd_asm* a, double* rhs, double* owned_vals);
+
+/* ---- A14-A16: mul!, `\`, FEFunction ------------------------------------------ */
+/* y = A*x over global vectors (ngdofs), PSparseMatrix mul! semantics. */
+int gd_spmv(gd_asm* a, const double* x, double* y, int where);
+
+typedef struct gd_solve_stats {
+  int32_t iterations;
+  int32_t converged;
+  double rel_residual;   /* ||b - A x|| / ||b|| recomputed in FP64 at exit */
+  double seconds;
+} gd_solve_stats;
+/* x = A \ b for the assembled rhs, Jacobi-preconditioned CG in FP64 to the
+ * relative residual rtol.  x: global vector (ngdofs). */
+int gd_solve(gd_asm* a, int method, double rtol, int maxit, double* x, int where,
+             gd_solve_stats* stats);
+/* FEFunction(U, x) / consistent!: the local (owned+ghost) free values of one part
+ * from a global vector (FESpaces.jl:354-371, Algebra.jl:270-293). */
+int gd_fe_function_local(const gd_space* space, int part, const double* x_global, int where,
+                         double* x_local);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* GDGPU_H */

@@ -1,0 +1,905 @@
+"""CPU oracle for the GridapDistributed assembly-and-solve path.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the shipped library imports this module:
+it is the checker that the CUDA path is compared against, and (through
+``oracle_core.c``) the timed CPU baseline.  Only ``tests/``, ``__graft_entry__.smoke``
+and ``bench.py``'s CPU-baseline leg may use it.
+
+It restates, in plain numpy/Python, what the reference computes on its
+``with_debug`` path for a non-periodic ``CartesianDiscreteModel``:
+
+* cell partition with a one-cell ghost layer
+  (``src/PArraysExtras.jl:5-84``, ``src/Geometry.jl:378-411``);
+* per-part Lagrangian Q_k DOF numbering on the owned+ghost box.  This part is
+  Gridap.jl 0.20 (third party, not in the reference tree): vertices, then edges,
+  then faces, then cells, each face numbered at its first appearance when the
+  cells are visited in order, free DOFs positive and Dirichlet DOFs negative.
+  It is restated from that published algorithm; the reference's own tests pin
+  only its consequences (DOF counts, exact solutions), not the order;
+* ``generate_gids`` (``src/FESpaces.jl:139-261``): owner = max owner rank of the
+  cells around a DOF, owned DOFs numbered part-contiguously in local order,
+  ghost ids fetched from the owners through cell-wise exchanges;
+* element matrices/vectors by tensor Gauss quadrature (Gridap ``integrate``,
+  called from ``src/CellData.jl:234-259``) with Dirichlet lifting;
+* the COO builders and ``create_from_nz`` for both strategies
+  (``src/Algebra.jl:537-646, 720-793, 919-962, 1048-1257``):
+  SubAssembledRows (ghost-row triplets zeroed but kept, sent to the row owner and
+  appended there; ghost columns in first-appearance order) and FullyAssembledRows
+  (no ghost rows, ghost columns sorted by local DOF id);
+* the gathered sparse LU behind ``\\`` (PartitionedArrays 0.3, third party) via
+  scipy's SuperLU, a Jacobi-PCG in FP64, and ``consistent!`` for ``FEFunction``
+  (``src/FESpaces.jl:354-371``, ``src/Algebra.jl:270-293``).
+
+Conventions: every index here is 0-based (the reference is 1-based).  Parts are
+numbered x-fastest (``CartesianIndices(np)``), cells and lattice nodes
+lexicographically x-fastest.  The "node lattice" of an order-k space is the
+k-refined vertex grid: global node coordinates ``X_d`` in ``[0, k*n_d]``.
+"""
+from __future__ import annotations
+
+import itertools
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# --------------------------------------------------------------------------------------
+# A1. Cartesian cell partition (src/PArraysExtras.jl:21-84)
+# --------------------------------------------------------------------------------------
+
+
+def local_range(p1: int, np_: int, n: int, ghost: bool = False):
+    """0-based half-open cell range of 1-based part ``p1`` along one direction.
+
+    Restates ``_local_range`` (src/PArraysExtras.jl:72-84): ``divrem(n,np)``, the
+    last ``rem`` parts get one extra cell, the ghost layer extends one cell each
+    way, clamped to the mesh (non-periodic)."""
+    l, rem = divmod(n, np_)
+    offset = l * (p1 - 1)
+    if rem >= (np_ - p1 + 1):
+        l += 1
+        offset += p1 - (np_ - rem) - 1
+    g = 1 if ghost else 0
+    start = 1 + offset - g
+    stop = l + offset + g
+    start = max(1, start)
+    stop = min(n, stop)
+    return start - 1, stop  # 0-based [lo, hi)
+
+
+@dataclass
+class Partition:
+    """Cell partition of ``n`` cells into ``np`` parts (src/PArraysExtras.jl:21-70)."""
+
+    np: tuple
+    n: tuple
+    own_lo: list = field(default_factory=list)   # per part, per dim
+    own_hi: list = field(default_factory=list)
+    loc_lo: list = field(default_factory=list)
+    loc_hi: list = field(default_factory=list)
+
+    @property
+    def dim(self):
+        return len(self.n)
+
+    @property
+    def nparts(self):
+        return int(np.prod(self.np))
+
+    def part_coords(self, p):
+        c = []
+        for d in range(self.dim):
+            c.append(p % self.np[d])
+            p //= self.np[d]
+        return tuple(c)
+
+    def part_id(self, coords):
+        p = 0
+        for d in reversed(range(self.dim)):
+            p = p * self.np[d] + coords[d]
+        return p
+
+    def cell_part_coord(self, d, cidx):
+        """Part coordinate along ``d`` owning cell index ``cidx`` (src/PArraysExtras.jl:26-36)."""
+        for pc in range(self.np[d]):
+            lo, hi = local_range(pc + 1, self.np[d], self.n[d])
+            if lo <= cidx < hi:
+                return pc
+        raise ValueError("cell index out of range")
+
+    def local_cells(self, p):
+        """Global lexicographic ids of the local (owned+ghost) cells of part ``p``,
+        in the local model's cell order (box lexicographic, x fastest)."""
+        ranges = [range(self.loc_lo[p][d], self.loc_hi[p][d]) for d in range(self.dim)]
+        out = []
+        for ci in itertools.product(*reversed(ranges)):
+            ci = tuple(reversed(ci))
+            out.append(self.cell_gid(ci))
+        return np.array(out, dtype=np.int64)
+
+    def cell_gid(self, ci):
+        g = 0
+        for d in reversed(range(self.dim)):
+            g = g * self.n[d] + ci[d]
+        return g
+
+    def cell_coords(self, gid):
+        c = []
+        for d in range(self.dim):
+            c.append(gid % self.n[d])
+            gid //= self.n[d]
+        return tuple(c)
+
+    def cell_owner(self, ci):
+        return self.part_id(tuple(self.cell_part_coord(d, ci[d]) for d in range(self.dim)))
+
+    def ghost_maps(self, p):
+        """``ghost_to_global``, ``ghost_to_owner`` and ``perm`` of part ``p`` in the
+        order produced by ``_block_with_constant_size`` (src/PArraysExtras.jl:40-69)."""
+        lcells = self.local_cells(p)
+        n_own = int(np.prod([self.own_hi[p][d] - self.own_lo[p][d] for d in range(self.dim)]))
+        g2g, g2o, perm = [], [], np.zeros(len(lcells), dtype=np.int64)
+        i_own = 0
+        i_gh = 0
+        for i, g in enumerate(lcells):
+            ci = self.cell_coords(int(g))
+            owned = all(self.own_lo[p][d] <= ci[d] < self.own_hi[p][d] for d in range(self.dim))
+            if owned:
+                perm[i] = i_own
+                i_own += 1
+            else:
+                g2g.append(int(g))
+                g2o.append(self.cell_owner(ci))
+                perm[i] = n_own + i_gh
+                i_gh += 1
+        return np.array(g2g, dtype=np.int64), np.array(g2o, dtype=np.int32), perm
+
+
+def make_partition(np_, n):
+    """``_uniform_partition(ranks, np, n, ghost=true)`` (src/PArraysExtras.jl:5-19)."""
+    P = Partition(tuple(np_), tuple(n))
+    for p in range(P.nparts):
+        pc = P.part_coords(p)
+        ol, oh, ll, lh = [], [], [], []
+        for d in range(P.dim):
+            a, b = local_range(pc[d] + 1, P.np[d], P.n[d])
+            c, e = local_range(pc[d] + 1, P.np[d], P.n[d], ghost=True)
+            ol.append(a); oh.append(b); ll.append(c); lh.append(e)
+        P.own_lo.append(ol); P.own_hi.append(oh); P.loc_lo.append(ll); P.loc_hi.append(lh)
+    return P
+
+
+# --------------------------------------------------------------------------------------
+# A3. Reference element, local Q_k numbering (Gridap 0.20 conforming FE space)
+# --------------------------------------------------------------------------------------
+
+# Gridap polytope orderings (vertex ids lexicographic, x fastest).
+QUAD_EDGES = [(0, 1), (2, 3), (0, 2), (1, 3)]
+HEX_EDGES = [(0, 1), (2, 3), (4, 5), (6, 7), (0, 2), (1, 3), (4, 6), (5, 7),
+             (0, 4), (1, 5), (2, 6), (3, 7)]
+HEX_FACES = [(0, 1, 2, 3), (4, 5, 6, 7), (0, 1, 4, 5), (2, 3, 6, 7), (0, 2, 4, 6), (1, 3, 5, 7)]
+
+
+def vertex_offsets(dim):
+    return [tuple((v >> d) & 1 for d in range(dim)) for v in range(1 << dim)]
+
+
+def cell_local_nodes(dim, k):
+    """Cell-local node offsets (in k-refined lattice units, each in [0,k]) in Gridap's
+    Lagrangian node order: vertices, then own nodes of each edge (in edge order,
+    increasing along the edge), then own nodes of each face (lexicographic in the
+    face's first/second axes), then the interior nodes (lexicographic)."""
+    verts = vertex_offsets(dim)
+    nodes = [tuple(k * c for c in v) for v in verts]
+    edges = QUAD_EDGES if dim == 2 else HEX_EDGES
+    for (a, b) in edges:
+        va, vb = np.array(verts[a]), np.array(verts[b])
+        for t in range(1, k):
+            nodes.append(tuple(int(x) for x in k * va + t * (vb - va)))
+    if dim == 3:
+        for (a, b, c, _) in HEX_FACES:
+            va, vb, vc = np.array(verts[a]), np.array(verts[b]), np.array(verts[c])
+            for t in range(1, k):
+                for s in range(1, k):
+                    nodes.append(tuple(int(x) for x in k * va + s * (vb - va) + t * (vc - va)))
+    rng = [range(1, k)] * dim
+    for ci in itertools.product(*rng):
+        nodes.append(tuple(reversed(ci)))
+    assert len(nodes) == (k + 1) ** dim
+    return nodes
+
+
+@dataclass
+class LocalSpace:
+    """One part's local FE space on its owned+ghost box."""
+
+    part: int
+    box_lo: tuple            # cell range of the local box
+    box_hi: tuple
+    cells: np.ndarray        # global cell ids in local order
+    cell_dofs: np.ndarray    # (ncells, ndofs_cell): free lid >= 0, Dirichlet -(d+1)
+    dof_node: np.ndarray     # (nfree, dim) global lattice coords of each free dof
+    dof_comp: np.ndarray     # (nfree,)
+    dir_node: np.ndarray     # (ndir, dim)
+    dir_comp: np.ndarray
+    nfree: int
+    ndir: int
+
+
+def dirichlet_node(X, N, dirichlet_sides):
+    """A lattice node is Dirichlet iff it lies on a flagged boundary plane.
+    ``dirichlet_sides[2d]`` flags the plane x_d = 0, ``[2d+1]`` x_d = max."""
+    for d in range(len(N)):
+        if dirichlet_sides[2 * d] and X[d] == 0:
+            return True
+        if dirichlet_sides[2 * d + 1] and X[d] == N[d] - 1:
+            return True
+    return False
+
+
+def build_local_space(P: Partition, p: int, k: int, ncomp: int, dirichlet_sides):
+    """Gridap-order conforming numbering on the local box of part ``p``.
+
+    Faces are numbered by dimension (vertices, edges, faces, cells); vertices in
+    lexicographic order, higher faces at first appearance while visiting the
+    cells in local order and their local faces in polytope order.  DOFs are
+    numbered face by face (own nodes component-major), then split into free
+    (0,1,2,...) and Dirichlet (-1,-2,...) in that same order."""
+    dim = P.dim
+    lo = tuple(P.loc_lo[p]); hi = tuple(P.loc_hi[p])
+    m = tuple(hi[d] - lo[d] for d in range(dim))
+    N = tuple(k * P.n[d] + 1 for d in range(dim))
+    verts = vertex_offsets(dim)
+    edges = QUAD_EDGES if dim == 2 else HEX_EDGES
+    faces2 = [] if dim == 2 else HEX_FACES
+    lnodes = cell_local_nodes(dim, k)
+
+    cell_list = []
+    for ci in itertools.product(*[range(m[d]) for d in reversed(range(dim))]):
+        cell_list.append(tuple(reversed(ci)))
+
+    def vid(vc):
+        g = 0
+        for d in reversed(range(dim)):
+            g = g * (m[d] + 1) + vc[d]
+        return g
+
+    nverts = int(np.prod([mm + 1 for mm in m]))
+    # face own nodes (global lattice coordinates), by face id within each dimension
+    face_nodes = []   # list over faces (all dims, in dimension order) of list of lattice coords
+    # vertices
+    vert_nodes = [None] * nverts
+    for vc in itertools.product(*[range(mm + 1) for mm in reversed(m)]):
+        vc = tuple(reversed(vc))
+        vert_nodes[vid(vc)] = [tuple(k * (lo[d] + vc[d]) for d in range(dim))]
+    face_nodes.extend(vert_nodes)
+
+    def first_appearance(local_faces, nown_fn):
+        seen = {}
+        out = []
+        for ci in cell_list:
+            for lf in local_faces:
+                key = tuple(sorted(vid(tuple(ci[d] + verts[v][d] for d in range(dim))) for v in lf))
+                if key in seen:
+                    continue
+                seen[key] = len(out)
+                out.append(nown_fn(ci, lf))
+        return out
+
+    def edge_own(ci, e):
+        a, b = e
+        va, vb = np.array(verts[a]), np.array(verts[b])
+        base = np.array([k * (lo[d] + ci[d]) for d in range(dim)])
+        return [tuple(int(x) for x in base + k * va + t * (vb - va)) for t in range(1, k)]
+
+    def face_own(ci, f):
+        a, b, c, _ = f
+        va, vb, vc = np.array(verts[a]), np.array(verts[b]), np.array(verts[c])
+        base = np.array([k * (lo[d] + ci[d]) for d in range(dim)])
+        return [tuple(int(x) for x in base + k * va + s * (vb - va) + t * (vc - va))
+                for t in range(1, k) for s in range(1, k)]
+
+    if k > 1:
+        face_nodes.extend(first_appearance(edges, edge_own))
+        if dim == 3:
+            face_nodes.extend(first_appearance(faces2, face_own))
+        for ci in cell_list:
+            base = [k * (lo[d] + ci[d]) for d in range(dim)]
+            own = []
+            for off in itertools.product(*[range(1, k)] * dim):
+                off = tuple(reversed(off))
+                own.append(tuple(base[d] + off[d] for d in range(dim)))
+            face_nodes.append(own)
+
+    # DOFs face by face, component-major within a face, then the free/Dirichlet split
+    node_comp_to_lid = {}
+    dof_node, dof_comp, dir_node, dir_comp = [], [], [], []
+    for fn in face_nodes:
+        for c in range(ncomp):
+            for X in fn:
+                if dirichlet_node(X, N, dirichlet_sides):
+                    dir_node.append(X); dir_comp.append(c)
+                    node_comp_to_lid[(X, c)] = -len(dir_node)
+                else:
+                    dof_node.append(X); dof_comp.append(c)
+                    node_comp_to_lid[(X, c)] = len(dof_node) - 1
+
+    nnode = len(lnodes)
+    cell_dofs = np.zeros((len(cell_list), nnode * ncomp), dtype=np.int64)
+    cells = np.zeros(len(cell_list), dtype=np.int64)
+    for ic, ci in enumerate(cell_list):
+        gci = tuple(lo[d] + ci[d] for d in range(dim))
+        cells[ic] = P.cell_gid(gci)
+        for c in range(ncomp):
+            for a, off in enumerate(lnodes):
+                X = tuple(k * gci[d] + off[d] for d in range(dim))
+                cell_dofs[ic, c * nnode + a] = node_comp_to_lid[(X, c)]
+    return LocalSpace(part=p, box_lo=lo, box_hi=hi, cells=cells, cell_dofs=cell_dofs,
+                      dof_node=np.array(dof_node, dtype=np.int64).reshape(-1, dim),
+                      dof_comp=np.array(dof_comp, dtype=np.int64),
+                      dir_node=np.array(dir_node, dtype=np.int64).reshape(-1, dim),
+                      dir_comp=np.array(dir_comp, dtype=np.int64),
+                      nfree=len(dof_node), ndir=len(dir_node))
+
+
+# --------------------------------------------------------------------------------------
+# A4. generate_gids (src/FESpaces.jl:139-261)
+# --------------------------------------------------------------------------------------
+
+
+@dataclass
+class DofIndices:
+    """``LocalIndices(ngdofs, me, ldof_to_gdof, ldof_to_owner)`` of one part (0-based)."""
+
+    part: int
+    ngdofs: int
+    ldof_to_gdof: np.ndarray
+    ldof_to_owner: np.ndarray
+
+    @property
+    def own_mask(self):
+        return self.ldof_to_owner == self.part
+
+    @property
+    def n_own(self):
+        return int(self.own_mask.sum())
+
+    @property
+    def own_to_global(self):
+        return self.ldof_to_gdof[self.own_mask]
+
+    @property
+    def ghost_lids(self):
+        return np.nonzero(~self.own_mask)[0]
+
+
+def generate_gids(P: Partition, spaces):
+    """Restates ``generate_gids`` step by step, including the three cell-wise
+    owner->ghost exchanges (src/FESpaces.jl:139-261)."""
+    nparts = P.nparts
+    cell_owner = []
+    cell_is_own = []
+    gid_to_lcell = []
+    for p in range(nparts):
+        owners = np.array([P.cell_owner(P.cell_coords(int(g))) for g in spaces[p].cells], dtype=np.int32)
+        cell_owner.append(owners)
+        cell_is_own.append(owners == p)
+        gid_to_lcell.append({int(g): i for i, g in enumerate(spaces[p].cells)})
+
+    # FESpaces.jl:145-163 local max owner
+    ldof_to_owner = []
+    for p in range(nparts):
+        s = spaces[p]
+        o = np.full(s.nfree, -1, dtype=np.int32)
+        for c in range(len(s.cells)):
+            for ld in s.cell_dofs[c]:
+                if ld >= 0:
+                    o[ld] = max(o[ld], cell_owner[p][c])
+        ldof_to_owner.append(o)
+
+    def dof_to_cell(vals):
+        # dof_wise_to_cell_wise! over owned cells (FESpaces.jl:70-90); -1 elsewhere
+        out = []
+        for p in range(nparts):
+            s = spaces[p]
+            cw = np.full(s.cell_dofs.shape, -1, dtype=np.int64)
+            for c in np.nonzero(cell_is_own[p])[0]:
+                for i, ld in enumerate(s.cell_dofs[c]):
+                    if ld >= 0:
+                        cw[c, i] = vals[p][ld]
+            out.append(cw)
+        return out
+
+    def fetch_ghost(cw):
+        # owner -> ghost copy of cell-wise data (FESpaces.jl:130-137)
+        new = [a.copy() for a in cw]
+        for p in range(nparts):
+            for c in np.nonzero(~cell_is_own[p])[0]:
+                q = int(cell_owner[p][c])
+                cq = gid_to_lcell[q][int(spaces[p].cells[c])]
+                new[p][c] = cw[q][cq]
+        return new
+
+    def cell_to_dof(vals, cw):
+        # cell_wise_to_dof_wise! over ghost cells (FESpaces.jl:92-109)
+        for p in range(nparts):
+            s = spaces[p]
+            for c in np.nonzero(~cell_is_own[p])[0]:
+                for i, ld in enumerate(s.cell_dofs[c]):
+                    if ld >= 0:
+                        vals[p][ld] = cw[p][c, i]
+
+    cw = fetch_ghost(dof_to_cell(ldof_to_owner))
+    cell_to_dof(ldof_to_owner, cw)
+    nodofs = [int((ldof_to_owner[p] == p).sum()) for p in range(nparts)]
+    first_gdof = np.concatenate([[0], np.cumsum(nodofs)[:-1]]).astype(np.int64)
+    ldof_to_gdof = []
+    for p in range(nparts):
+        g = np.full(spaces[p].nfree, -1, dtype=np.int64)
+        own = ldof_to_owner[p] == p
+        g[own] = first_gdof[p] + np.arange(int(own.sum()))
+        ldof_to_gdof.append(g)
+    cw = fetch_ghost(dof_to_cell(ldof_to_gdof))
+    for p in range(nparts):   # FESpaces.jl:215-233
+        s = spaces[p]
+        for c in np.nonzero(~cell_is_own[p])[0]:
+            for i, ld in enumerate(s.cell_dofs[c]):
+                if ld >= 0 and ldof_to_owner[p][ld] == cell_owner[p][c]:
+                    ldof_to_gdof[p][ld] = cw[p][c, i]
+    cw = fetch_ghost(dof_to_cell(ldof_to_gdof))
+    cell_to_dof(ldof_to_gdof, cw)
+    ngdofs = int(sum(nodofs))
+    out = [DofIndices(p, ngdofs, ldof_to_gdof[p], ldof_to_owner[p]) for p in range(nparts)]
+    for d in out:
+        assert (d.ldof_to_gdof >= 0).all()
+    return out, first_gdof
+
+
+# --------------------------------------------------------------------------------------
+# A7. Reference element integrals (Gridap integrate with tensor Gauss quadrature)
+# --------------------------------------------------------------------------------------
+
+
+def gauss_legendre(npts):
+    x, w = np.polynomial.legendre.leggauss(npts)
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def lagrange_1d(k, x):
+    """Values and derivatives of the k+1 equispaced Lagrange polynomials on [0,1]."""
+    nodes = np.linspace(0.0, 1.0, k + 1)
+    x = np.atleast_1d(x)
+    V = np.ones((len(x), k + 1))
+    D = np.zeros((len(x), k + 1))
+    for a in range(k + 1):
+        others = [b for b in range(k + 1) if b != a]
+        den = np.prod([nodes[a] - nodes[b] for b in others])
+        val = np.ones(len(x))
+        for b in others:
+            val = val * (x - nodes[b])
+        V[:, a] = val / den
+        der = np.zeros(len(x))
+        for b in others:
+            t = np.ones(len(x))
+            for c in others:
+                if c != b:
+                    t = t * (x - nodes[c])
+            der += t
+        D[:, a] = der / den
+    return V, D
+
+
+def quad_points_per_dir(degree):
+    """Tensor Gauss rule with ceil((degree+1)/2) points per direction."""
+    return (degree + 2) // 2
+
+
+def reference_matrices(dim, k, h, degree):
+    """Element stiffness ``Kh[i,j] = sum_q w_q |J| grad(phi_i).grad(phi_j)``, mass
+    ``Mh`` and load ``Fh[i] = sum_q w_q |J| phi_i`` for an axis-aligned cell of
+    sizes ``h``, in Gridap's cell-local node order."""
+    nq = quad_points_per_dir(degree)
+    xq, wq = gauss_legendre(nq)
+    V, D = lagrange_1d(k, xq)
+    lnodes = cell_local_nodes(dim, k)
+    nn = len(lnodes)
+    detJ = float(np.prod(h))
+    qidx = list(itertools.product(*[range(nq)] * dim))
+    nqt = len(qidx)
+    phi = np.zeros((nqt, nn))
+    grad = np.zeros((nqt, nn, dim))
+    W = np.zeros(nqt)
+    for iq, qi in enumerate(qidx):
+        qi = tuple(reversed(qi))
+        W[iq] = np.prod([wq[qi[d]] for d in range(dim)]) * detJ
+        for a, off in enumerate(lnodes):
+            vals = [V[qi[d], off[d]] for d in range(dim)]
+            phi[iq, a] = np.prod(vals)
+            for d in range(dim):
+                g = D[qi[d], off[d]] / h[d]
+                for e in range(dim):
+                    if e != d:
+                        g *= vals[e]
+                grad[iq, a, d] = g
+    K = np.einsum("q,qid,qjd->ij", W, grad, grad)
+    M = np.einsum("q,qi,qj->ij", W, phi, phi)
+    F = np.einsum("q,qi->i", W, phi)
+    return K, M, F
+
+
+# --------------------------------------------------------------------------------------
+# Problem description
+# --------------------------------------------------------------------------------------
+
+
+@dataclass
+class Problem:
+    """A scalar diffusion problem ``-div(kappa grad u) = f`` on a Cartesian box."""
+
+    np: tuple
+    n: tuple
+    domain: tuple
+    order: int = 1
+    degree: int = 2
+    dirichlet_sides: tuple = None   # 2*dim flags; default: whole boundary
+    kappa: np.ndarray = None        # per global cell (lexicographic); default 1
+    f_const: float = 0.0            # constant source
+    f_nodal: np.ndarray = None      # or nodal source values on the global lattice (b = M f)
+    u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0
+
+    def __post_init__(self):
+        dim = len(self.n)
+        if self.dirichlet_sides is None:
+            self.dirichlet_sides = (1,) * (2 * dim)
+        if self.kappa is None:
+            self.kappa = np.ones(int(np.prod(self.n)))
+        self.kappa = np.asarray(self.kappa, dtype=np.float64)
+
+    @property
+    def dim(self):
+        return len(self.n)
+
+    @property
+    def h(self):
+        return tuple((self.domain[2 * d + 1] - self.domain[2 * d]) / self.n[d] for d in range(self.dim))
+
+    @property
+    def lattice(self):
+        return tuple(self.order * self.n[d] + 1 for d in range(self.dim))
+
+    def node_lin(self, X):
+        N = self.lattice
+        X = np.asarray(X)
+        g = np.zeros(X.shape[:-1], dtype=np.int64)
+        for d in reversed(range(self.dim)):
+            g = g * N[d] + X[..., d]
+        return g
+
+    def node_xyz(self, X):
+        X = np.asarray(X, dtype=np.float64)
+        out = np.empty_like(X)
+        for d in range(self.dim):
+            out[..., d] = self.domain[2 * d] + X[..., d] * self.h[d] / self.order
+        return out
+
+
+@dataclass
+class FESpaceData:
+    P: Partition
+    spaces: list
+    dofs: list
+    first_gdof: np.ndarray
+
+
+def build_fespace(pb: Problem) -> FESpaceData:
+    P = make_partition(pb.np, pb.n)
+    spaces = [build_local_space(P, p, pb.order, 1, pb.dirichlet_sides) for p in range(P.nparts)]
+    dofs, first = generate_gids(P, spaces)
+    return FESpaceData(P, spaces, dofs, first)
+
+
+# --------------------------------------------------------------------------------------
+# A8/A10. Cell matrices/vectors and the COO numeric loop
+# --------------------------------------------------------------------------------------
+
+
+def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
+    """Per local cell: element matrix ``kappa_c*Kh`` and element vector
+    ``f-term - K_e[:,D] u_D`` (Dirichlet lifting with the trial space's values)."""
+    dim = pb.dim
+    lnodes = np.array(cell_local_nodes(dim, pb.order))
+    mats, vecs = [], []
+    for ic, g in enumerate(sp.cells):
+        kap = pb.kappa[g]
+        Ke = kap * Kh
+        ci = np.array(P_cell_coords(pb.n, int(g)))
+        X = pb.order * ci[None, :] + lnodes
+        if pb.f_nodal is not None:
+            be = Mh @ pb.f_nodal[pb.node_lin(X)]
+        else:
+            be = pb.f_const * Fh
+        dofs = sp.cell_dofs[ic]
+        if pb.u_dir is not None:
+            ud = np.where(dofs < 0, pb.u_dir[pb.node_lin(X)], 0.0)
+            be = be - Ke @ ud
+        mats.append(Ke)
+        vecs.append(be)
+    return mats, vecs
+
+
+def P_cell_coords(n, gid):
+    c = []
+    for d in range(len(n)):
+        c.append(gid % n[d])
+        gid //= n[d]
+    return c
+
+
+@dataclass
+class LocalMatrix:
+    """One part of a ``PSparseMatrix``: local CSR (sorted columns, duplicates summed,
+    explicit zeros kept) and its row/col ``OwnAndGhostIndices``."""
+
+    part: int
+    nrows: int
+    ncols: int
+    rowptr: np.ndarray
+    colidx: np.ndarray
+    vals: np.ndarray
+    row_own_gids: np.ndarray
+    row_ghost_gids: np.ndarray
+    row_ghost_owner: np.ndarray
+    col_own_gids: np.ndarray
+    col_ghost_gids: np.ndarray
+    col_ghost_owner: np.ndarray
+    b: np.ndarray      # RHS over the rows (ghost entries zero after assemble!)
+
+
+def _compress(nrows, I, J, V, ncols):
+    """Local ``sparse(I,J,V,m,n)``: duplicates summed in COO order, columns sorted
+    within each row (CSR view of the same matrix)."""
+    order = np.lexsort((np.arange(len(I)), J, I))
+    I, J, V = I[order], J[order], V[order]
+    if len(I):
+        new = np.ones(len(I), dtype=bool)
+        new[1:] = (I[1:] != I[:-1]) | (J[1:] != J[:-1])
+        starts = np.nonzero(new)[0]
+        vals = np.add.reduceat(V, starts)
+        rows, cols = I[starts], J[starts]
+    else:
+        vals = np.zeros(0); rows = np.zeros(0, dtype=np.int64); cols = np.zeros(0, dtype=np.int64)
+    rowptr = np.zeros(nrows + 1, dtype=np.int64)
+    np.add.at(rowptr, rows + 1, 1)
+    rowptr = np.cumsum(rowptr)
+    return rowptr, cols.astype(np.int64), vals
+
+
+def assemble(pb: Problem, fe: FESpaceData, strategy: str = "sub"):
+    """``assemble_matrix_and_vector`` with a DistributedSparseMatrixAssembler.
+
+    ``strategy`` is ``"sub"`` (SubAssembledRows, the default, Algebra.jl:593-646) or
+    ``"full"`` (FullyAssembledRows, Algebra.jl:549-579)."""
+    P, spaces, dofs = fe.P, fe.spaces, fe.dofs
+    nparts = P.nparts
+    Kh, Mh, Fh = reference_matrices(pb.dim, pb.order, pb.h, pb.degree)
+    coo = []
+    bloc = []
+    for p in range(nparts):
+        sp, di = spaces[p], dofs[p]
+        owners = np.array([P.cell_owner(P.cell_coords(int(g))) for g in sp.cells])
+        mats, vecs = cell_contributions(pb, sp, Kh, Mh, Fh)
+        own_dof = di.ldof_to_owner == p
+        I, J, V = [], [], []
+        b = np.zeros(sp.nfree)
+        touched = np.zeros(sp.nfree, dtype=bool)
+        for ic in range(len(sp.cells)):
+            if strategy == "sub" and owners[ic] != p:
+                continue   # Triangulation(no_ghost) (Geometry.jl:802-847)
+            cd = sp.cell_dofs[ic]
+            Ke, be = mats[ic], vecs[ic]
+            nd = len(cd)
+            for j in range(nd):          # Gridap add_entries!: column-major loop
+                gj = cd[j]
+                if gj < 0:
+                    continue
+                for i in range(nd):
+                    gi = cd[i]
+                    if gi < 0:
+                        continue
+                    if strategy == "full" and not own_dof[gi]:
+                        continue   # FESpaces.jl:808-816
+                    I.append(gi); J.append(gj); V.append(Ke[i, j])
+            for i in range(nd):
+                gi = cd[i]
+                if gi < 0:
+                    continue
+                if strategy == "full" and not own_dof[gi]:
+                    continue
+                b[gi] += be[i]
+                touched[gi] = True
+        coo.append([np.array(I, dtype=np.int64), np.array(J, dtype=np.int64), np.array(V, dtype=np.float64)])
+        bloc.append((b, touched))
+
+    # to_global_indices! (Algebra.jl:600-601)
+    gI, gJ, gV = [], [], []
+    for p in range(nparts):
+        I, J, V = coo[p]
+        gI.append(dofs[p].ldof_to_gdof[I]); gJ.append(dofs[p].ldof_to_gdof[J]); gV.append(V.copy())
+
+    gid_owner = np.zeros(dofs[0].ngdofs, dtype=np.int32)
+    for p in range(nparts):
+        gid_owner[dofs[p].ldof_to_gdof] = dofs[p].ldof_to_owner
+
+    mats_out = []
+    if strategy == "sub":
+        # rows: owned + ghost rows touched by I, sorted by FE-space lid (Algebra.jl:931-962, 919-928)
+        row_ghost = []
+        for p in range(nparts):
+            di = dofs[p]
+            lids = coo[p][0]
+            gmask = ~di.own_mask[lids]
+            gl = np.unique(lids[gmask])        # sorted by local dof id
+            row_ghost.append(gl)
+        # Jo and triplet routing (Algebra.jl:1048-1131)
+        gJo = [gid_owner[gJ[p]] for p in range(nparts)]
+        send = {}
+        for p in range(nparts):
+            rown = gid_owner[gI[p]]
+            for q in sorted(set(rown.tolist()) - {p}):
+                sel = np.nonzero(rown == q)[0]    # COO order preserved
+                send[(p, q)] = (gI[p][sel].copy(), gJ[p][sel].copy(), gJo[p][sel].copy(), gV[p][sel].copy())
+                gV[p][sel] = 0.0                  # zeroed, not removed (Algebra.jl:1084)
+        for q in range(nparts):
+            for p in range(nparts):               # received data appended in ascending sender order
+                if (p, q) in send:
+                    a, b_, c, v = send[(p, q)]
+                    gI[q] = np.concatenate([gI[q], a]); gJ[q] = np.concatenate([gJ[q], b_])
+                    gJo[q] = np.concatenate([gJo[q], c]); gV[q] = np.concatenate([gV[q], v])
+        for p in range(nparts):
+            di = dofs[p]
+            own_g = di.own_to_global
+            n_own = len(own_g)
+            rg_l = row_ghost[p]
+            rg_g = di.ldof_to_gdof[rg_l]
+            rg_o = di.ldof_to_owner[rg_l]
+            # cols: ghost cols in first-appearance order among non-owned J (Algebra.jl:1210-1238)
+            seen = {}
+            cg_g, cg_o = [], []
+            for j, jo in zip(gJ[p].tolist(), gJo[p].tolist()):
+                if jo != p and j not in seen:
+                    seen[j] = len(cg_g); cg_g.append(j); cg_o.append(jo)
+            cg_g = np.array(cg_g, dtype=np.int64); cg_o = np.array(cg_o, dtype=np.int32)
+            row_map = {int(g): i for i, g in enumerate(own_g)}
+            for i, g in enumerate(rg_g):
+                row_map[int(g)] = n_own + i
+            col_map = {int(g): i for i, g in enumerate(own_g)}
+            for i, g in enumerate(cg_g):
+                col_map[int(g)] = n_own + i
+            I = np.array([row_map[int(g)] for g in gI[p]], dtype=np.int64)
+            J = np.array([col_map[int(g)] for g in gJ[p]], dtype=np.int64)
+            nrows = n_own + len(rg_g); ncols = n_own + len(cg_g)
+            rowptr, colidx, vals = _compress(nrows, I, J, gV[p], ncols)
+            mats_out.append(LocalMatrix(p, nrows, ncols, rowptr, colidx, vals, own_g, rg_g, rg_o,
+                                        own_g, cg_g, cg_o, None))
+        # RHS: _rhs_callback + assemble! (Algebra.jl:720-753, 786-789)
+        bfull = np.zeros(dofs[0].ngdofs)
+        for p in range(nparts):
+            b, touched = bloc[p]
+            np.add.at(bfull, dofs[p].ldof_to_gdof, np.where(touched, b, 0.0))
+        for p in range(nparts):
+            M = mats_out[p]
+            M.b = np.concatenate([bfull[M.row_own_gids], np.zeros(len(M.row_ghost_gids))])
+    else:
+        for p in range(nparts):
+            di = dofs[p]
+            own_g = di.own_to_global
+            n_own = len(own_g)
+            J_l = coo[p][1]
+            # cols: touched ghost lids sorted by FE-space lid (Algebra.jl:1245-1257, 919-928)
+            gl = np.unique(J_l[~di.own_mask[J_l]])
+            cg_g = di.ldof_to_gdof[gl]; cg_o = di.ldof_to_owner[gl]
+            row_map = {int(g): i for i, g in enumerate(own_g)}
+            col_map = dict(row_map)
+            for i, g in enumerate(cg_g):
+                col_map[int(g)] = n_own + i
+            I = np.array([row_map[int(g)] for g in gI[p]], dtype=np.int64)
+            J = np.array([col_map[int(g)] for g in gJ[p]], dtype=np.int64)
+            rowptr, colidx, vals = _compress(n_own, I, J, gV[p], n_own + len(cg_g))
+            b, _ = bloc[p]
+            M = LocalMatrix(p, n_own, n_own + len(cg_g), rowptr, colidx, vals, own_g,
+                            np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32),
+                            own_g, cg_g, cg_o.astype(np.int32), b[di.own_mask])
+            mats_out.append(M)
+    return mats_out
+
+
+# --------------------------------------------------------------------------------------
+# A14-A16. Gathered operator, solve, consistent!
+# --------------------------------------------------------------------------------------
+
+
+def gather_global(mats, ngdofs):
+    """Owned rows of every part in part order = the global matrix in gid order."""
+    import scipy.sparse as sps
+    rows, cols, vals = [], [], []
+    b = np.zeros(ngdofs)
+    for M in mats:
+        n_own = len(M.row_own_gids)
+        colg = np.concatenate([M.col_own_gids, M.col_ghost_gids])
+        for r in range(n_own):
+            s, e = M.rowptr[r], M.rowptr[r + 1]
+            rows.append(np.full(e - s, M.row_own_gids[r]))
+            cols.append(colg[M.colidx[s:e]])
+            vals.append(M.vals[s:e])
+        b[M.row_own_gids] = M.b[:n_own]
+    A = sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))),
+                       shape=(ngdofs, ngdofs))
+    return A, b
+
+
+def solve_lu(mats, ngdofs):
+    """``A \\ b`` on a PSparseMatrix: gather to one part, sparse LU, scatter."""
+    import scipy.sparse.linalg as spla
+    A, b = gather_global(mats, ngdofs)
+    return spla.splu(A.tocsc()).solve(b)
+
+
+def pcg_jacobi(A, b, rtol=1e-8, maxit=100000, x0=None):
+    """Jacobi-preconditioned CG in FP64; stops at ||b-Ax|| <= rtol*||b||."""
+    x = np.zeros_like(b) if x0 is None else x0.copy()
+    dinv = 1.0 / A.diagonal()
+    r = b - A @ x
+    z = dinv * r
+    p = z.copy()
+    rz = r @ z
+    nb = np.linalg.norm(b)
+    it = 0
+    while np.linalg.norm(r) > rtol * nb and it < maxit:
+        Ap = A @ p
+        alpha = rz / (p @ Ap)
+        x += alpha * p
+        r -= alpha * Ap
+        z = dinv * r
+        rz_new = r @ z
+        p = z + (rz_new / rz) * p
+        rz = rz_new
+        it += 1
+    return x, it
+
+
+def consistent_local(x_global, dofs):
+    """``change_ghost(..., make_consistent=true)`` onto the FE-space gids: every
+    local DOF (owned and ghost) gets the owner's value."""
+    return [x_global[d.ldof_to_gdof] for d in dofs]
+
+
+def nodal_solution(pb: Problem, fe: FESpaceData, x_global):
+    """Dense lattice array of the FE solution's nodal values (free from x, Dirichlet
+    from u_dir)."""
+    N = pb.lattice
+    u = np.zeros(int(np.prod(N))) if pb.u_dir is None else pb.u_dir.copy()
+    for sp, d in zip(fe.spaces, fe.dofs):
+        u[pb.node_lin(sp.dof_node)] = x_global[d.ldof_to_gdof]
+    return u
+
+
+def l2_error(pb: Problem, u_nodal, u_exact):
+    """``sqrt(sum(integrate(abs2(u - uh))))`` with the problem's quadrature degree."""
+    dim, k = pb.dim, pb.order
+    nq = quad_points_per_dir(pb.degree)
+    xq, wq = gauss_legendre(nq)
+    V, _ = lagrange_1d(k, xq)
+    h = pb.h
+    err = 0.0
+    lnodes = np.array(cell_local_nodes(dim, k))
+    qidx = [tuple(reversed(q)) for q in itertools.product(*[range(nq)] * dim)]
+    for g in range(int(np.prod(pb.n))):
+        ci = np.array(P_cell_coords(pb.n, g))
+        X = k * ci[None, :] + lnodes
+        ue = u_nodal[pb.node_lin(X)]
+        for qi in qidx:
+            phi = np.array([np.prod([V[qi[d], off[d]] for d in range(dim)]) for off in lnodes])
+            xyz = [pb.domain[2 * d] + (ci[d] + xq[qi[d]]) * h[d] for d in range(dim)]
+            w = np.prod([wq[qi[d]] for d in range(dim)]) * np.prod(h)
+            err += w * (u_exact(*xyz) - phi @ ue) ** 2
+    return math.sqrt(err)

@@ -1,0 +1,160 @@
+"""GPU parity: the CUDA path against the CPU oracle, through the C ABI.
+
+Bit-exact: DOF numbering, gids and owners, row/column index sets, local CSR
+patterns.  FP64 values: |gpu - oracle| <= 1e-12 * (max |oracle| in the row).
+Solutions: relative difference to the oracle's gathered sparse LU <= 1e-8.
+"""
+import numpy as np
+import pytest
+
+import gridap_oracle as go
+from helpers import make_problem, row_scaled_error
+
+pytestmark = pytest.mark.gpu
+
+VAL_TOL = 1e-12     # FP64 matrix/vector entries, relative to the row scale
+SOL_TOL = 1e-8      # solution vs gathered sparse LU
+
+
+@pytest.fixture(scope="module")
+def backend():
+    import gridap_gb300 as G
+    be = G.GB300Backend(0)
+    yield be
+    be.close()
+
+
+def gpu_system(backend, pb, strategy):
+    import gridap_gb300 as G
+    ranks = backend.distribute(range(int(np.prod(pb.np))))
+    model = G.CartesianDiscreteModel(ranks, pb.np, pb.domain, pb.n)
+    tags = ["left", "right", "bottom", "top", "back", "front"]
+    sides = [t for t, s in zip(tags, pb.dirichlet_sides) if s]
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, pb.order), dirichlet_tags=sides)
+    U = G.TrialFESpace(pb.u_dir, V) if pb.u_dir is not None else G.TrialFESpace(0.0, V)
+    dO = G.Measure(G.Triangulation(model), pb.degree)
+    a = G.integral_grad_grad(pb.kappa, dO)
+    l = G.integral_source(pb.f_nodal if pb.f_nodal is not None else pb.f_const, dO)
+    strat = G.SubAssembledRows() if strategy == "sub" else G.FullyAssembledRows()
+    assem = G.SparseMatrixAssembler(U, V, strat)
+    op = G.AffineFEOperator(a, l, U, V, assem)
+    return model, V, U, op
+
+
+CASES = [
+    dict(dim=2, n=(4, 4), parts=(2, 2), order=1),
+    dict(dim=2, n=(5, 4), parts=(2, 2), order=2, seed=1),
+    dict(dim=2, n=(6, 5), parts=(2, 1), order=3, sides=(1, 0, 1, 0), seed=2),
+    dict(dim=2, n=(7, 3), parts=(3, 1), order=2, seed=3),
+    dict(dim=2, n=(4, 4), parts=(1, 1), order=1),
+    dict(dim=3, n=(5, 4, 3), parts=(2, 2, 1), order=1, seed=4),
+    dict(dim=3, n=(6, 6, 6), parts=(2, 2, 2), order=1, seed=5),
+    dict(dim=3, n=(4, 3, 5), parts=(2, 1, 2), order=2, seed=6),
+    dict(dim=3, n=(3, 4, 3), parts=(1, 2, 2), order=3, sides=(1, 0, 1, 0, 1, 0), seed=7),
+    dict(dim=3, n=(4, 4, 4), parts=(2, 2, 2), order=1, sides=(0, 0, 0, 0, 0, 0), seed=8),
+    dict(dim=3, n=(5, 5, 5), parts=(2, 2, 2), order=2, sides=(1, 0, 0, 0, 0, 0), seed=9, f_nodal=True),
+]
+
+
+def case_id(c):
+    return f"{c['dim']}d_n{'x'.join(map(str, c['n']))}_p{''.join(map(str, c['parts']))}_q{c['order']}"
+
+
+@pytest.mark.parametrize("strategy", ["sub", "full"])
+@pytest.mark.parametrize("case", CASES, ids=case_id)
+def test_parity_against_oracle(backend, case, strategy):
+    pb = make_problem(**case)
+    fe = go.build_fespace(pb)
+    ref = go.assemble(pb, fe, strategy)
+    model, V, U, op = gpu_system(backend, pb, strategy)
+    # A4: gids and owners, bit-exact; local DOF order via the lattice node of each DOF
+    assert V.num_free_dofs() == fe.dofs[0].ngdofs
+    for p, (d, sp) in enumerate(zip(fe.dofs, fe.spaces)):
+        li = V.gids.partition()[p]
+        assert np.array_equal(li.local_to_global, d.ldof_to_gdof), f"gids part {p}"
+        assert np.array_equal(li.local_to_owner, d.ldof_to_owner), f"owners part {p}"
+        assert np.array_equal(V.dof_nodes(p), pb.node_lin(sp.dof_node)), f"local numbering part {p}"
+    # A11: local matrices, index sets bit-exact, values to VAL_TOL
+    A = op.matrix
+    b_parts = op.vector.partition
+    for p, M in enumerate(ref):
+        rp, ci, vv = A.csr_parts()[p]
+        rows, cols = A.row_partition[p], A.col_partition[p]
+        assert np.array_equal(rows.own_to_global, M.row_own_gids)
+        assert np.array_equal(rows.ghost_to_global, M.row_ghost_gids), f"ghost rows part {p}"
+        assert np.array_equal(rows.ghost_to_owner, M.row_ghost_owner)
+        assert np.array_equal(cols.ghost_to_global, M.col_ghost_gids), f"ghost cols part {p}"
+        assert np.array_equal(cols.ghost_to_owner, M.col_ghost_owner)
+        assert np.array_equal(rp, M.rowptr), f"rowptr part {p}"
+        assert np.array_equal(ci, M.colidx), f"colidx part {p}"
+        assert row_scaled_error(vv, M.vals, M.rowptr) <= VAL_TOL
+        scale = max(np.abs(M.b).max(), 1e-300)
+        assert np.abs(b_parts[p] - M.b).max() <= VAL_TOL * scale
+
+
+@pytest.mark.parametrize("case", [CASES[1], CASES[6], CASES[7]], ids=case_id)
+def test_solve_matches_gathered_lu(backend, case):
+    pb = make_problem(**case)
+    fe = go.build_fespace(pb)
+    x_ref = go.solve_lu(go.assemble(pb, fe, "sub"), fe.dofs[0].ngdofs)
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    x = op.matrix.solve(rtol=1e-13)
+    assert op.matrix.last_stats.converged
+    assert np.abs(x - x_ref).max() / np.abs(x_ref).max() <= SOL_TOL
+
+
+@pytest.mark.parametrize("strategy", ["sub", "full"])
+@pytest.mark.parametrize("parts", [(2, 2), (1, 1), (2, 1), (1, 2)])
+def test_fespaces_kat_on_gpu(backend, parts, strategy):
+    """test/FESpacesTests.jl:10-59 on the GPU path: Q1, u = x+y, L2 error < 1e-9."""
+    import gridap_gb300 as G
+    pb = make_problem(2, (4, 4), parts, 1, f=0.0, u=lambda x, y: x + y, domain=(0, 4, 0, 4))
+    pb.degree = 3
+    _, V, U, op = gpu_system(backend, pb, strategy)
+    uh = G.solve(op, rtol=1e-14)
+    assert go.l2_error(pb, uh.nodal_values(), lambda x, y: x + y) < 1e-9
+    r = op.matrix.mul(uh.free_values) - op.vector.global_values()
+    assert np.abs(r).max() < 1e-10
+
+
+def test_poisson_q2_kat_on_gpu(backend):
+    """test/PoissonTests.jl:14-45 (all-Dirichlet): Q2 reproduces (x+y)^2."""
+    import gridap_gb300 as G
+    pb = make_problem(2, (4, 4), (2, 2), 2, f=-4.0, u=lambda x, y: (x + y) ** 2, domain=(0, 4, 0, 4))
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    uh = G.solve(op, rtol=1e-14)
+    assert go.l2_error(pb, uh.nodal_values(), lambda x, y: (x + y) ** 2) < 1e-9
+
+
+def test_vector_kat_on_gpu(backend):
+    """test/FESpacesTests.jl:61-70: sum(b) == length(b) for ∫(1*v)."""
+    pb = go.Problem(np=(2, 2), n=(4, 4), domain=(0, 4, 0, 4), order=1, degree=3, f_const=1.0)
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    b = op.vector.global_values()
+    assert abs(b.sum() - len(b)) < 1e-12
+
+
+@pytest.mark.parametrize("fixture_case", ["fespaces_q1_2x2", "poisson_q2_2x2", "diffusion_q1_3d"])
+@pytest.mark.parametrize("strategy", ["sub", "full"])
+def test_gpu_against_golden_fixtures(backend, fixture_case, strategy):
+    from pathlib import Path
+    import make_golden as mg
+    g = np.load(Path(__file__).resolve().parent / "golden" / f"{fixture_case}_{strategy}.npz")
+    pb = make_problem(**mg.CASES[fixture_case])
+    _, V, U, op = gpu_system(backend, pb, strategy)
+    for p in range(int(np.prod(pb.np))):
+        rp, ci, vv = op.matrix.csr_parts()[p]
+        assert np.array_equal(V.gids.partition()[p].local_to_global, g[f"p{p}_gid"])
+        assert np.array_equal(rp, g[f"p{p}_rowptr"]) and np.array_equal(ci, g[f"p{p}_colidx"])
+        assert row_scaled_error(vv, g[f"p{p}_vals"], g[f"p{p}_rowptr"]) <= VAL_TOL
+    x = op.matrix.solve(rtol=1e-14)
+    assert np.abs(x - g["x"]).max() / max(np.abs(g["x"]).max(), 1e-300) <= SOL_TOL
+
+
+def test_nonpositive_kappa_is_rejected(backend):
+    import gridap_gb300 as G
+    pb = make_problem(2, (4, 4), (2, 2), 1, seed=1)
+    pb.kappa[3] = -1.0
+    with pytest.raises(G._lib.GdError) as e:
+        gpu_system(backend, pb, "sub")
+    assert e.value.status == 8
