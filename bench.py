@@ -1,0 +1,394 @@
+"""Benchmark of the assembly hot path on the 3D variable-coefficient Poisson workload.
+
+Workload: unit cube, 128^3 Q1 hex cells, parts (2,2,2) as 8 slabs on one GPU,
+kappa = exp(g) with g a seeded Gaussian random field (sigma 1, squared-exponential
+correlation length 0.1) at the cell centres, f = 1, homogeneous Dirichlet,
+quadrature degree 2.  A "step" is one numeric assembly of matrix values and
+right-hand side into the cached symbolic pattern (assemble_matrix_and_vector!),
+SubAssembledRows.
+
+Metric: assembled matrix entries per second (the global matrix's nnz divided by the
+step time), whole job.  `e2e` is the same metric through the C-ABI call with host
+buffers: kappa copied host->device and the assembled values + rhs copied
+device->host inside every timed step.  `roofline` uses the algorithmic bytes
+8*nnz + 8*n_free + 8*n_cells per assembly against the measured HBM copy bandwidth.
+`solve` reports Jacobi-PCG to 1e-8 relative residual on the assembled system.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+Under torchrun with N>1 every rank runs its own replica of the workload on its own
+GPU (weak scaling, no data-path collective); the max time over ranks is reported.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "gridapdistributed.jl_gb300"
+sys.path.insert(0, str(PKG))
+
+METRIC = "assembly nnz/s (HBM % of peak); solve s to 1e-8 rel. res., learned vs Jacobi"
+UNIT = "nnz/s"
+L2_FLUSH_BYTES = 512 << 20   # > 129 MB L2
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--cells", type=int, default=128, help="cells per direction (default: the 128^3 workload)")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def reduce_max(value: float, world: int, device=None) -> float:
+    """Max of a float over all ranks (identity for one rank)."""
+    if world <= 1:
+        return value
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([value], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def workload(cells):
+    from gridap_gb300.synthetic import POISSON3D_128, lognormal_kappa
+    w = dict(POISSON3D_128)
+    if cells != 128:
+        w["cells"] = (cells,) * 3
+        w["name"] = f"poisson3d_q1_{cells}^3_parts2x2x2"
+    kappa = lognormal_kappa(w["cells"], w["sigma"], w["corr_len"], w["seed"])
+    return w, kappa
+
+
+# ------------------------------------------------------------------------------------
+# clocks during the timed region
+# ------------------------------------------------------------------------------------
+class ClockSampler:
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = Path(os.environ.get("TMPDIR", "/tmp")) / f"gd_clocks_{os.getpid()}.csv"
+
+    def start(self):
+        try:
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=self.fh, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        self.fh.close()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.path.read_text().splitlines():
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax.append(float(parts[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        try:
+            self.path.unlink()
+        except OSError:
+            pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic(workload_name):
+    """Per-launch DRAM bytes of the numeric kernels from the committed ncu summary."""
+    p = ROOT / "profiles" / "ncu_traffic.json"
+    if not p.exists():
+        return None
+    try:
+        d = json.loads(p.read_text())
+        return d.get(workload_name)
+    except Exception:
+        return None
+
+
+# ------------------------------------------------------------------------------------
+# CPU baseline: the oracle's C restatement of the reference's assembly
+# ------------------------------------------------------------------------------------
+def cpu_assembly(w, kappa, threads):
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle_c
+    _, _, ta = oracle_c.assemble(3, w["cells"], w["parts"], w["domain"], (1,) * 6, kappa, w["f"], w["degree"],
+                                 "sub", threads, keep=False)
+    return ta
+
+
+def global_nnz(cells):
+    m = cells - 1   # free nodes per direction (homogeneous Dirichlet on the whole boundary)
+    # 27-point stencil count of an m^3 grid: (3m-2)^3
+    return (3 * m - 2) ** 3, m ** 3
+
+
+def run_reference(args, rank, world):
+    """Reference arm: the reference's assembly algorithm (COO + ghost-row exchange +
+    compression, restated in C) on the host cores, same workload and metric."""
+    if rank != 0:
+        return
+    w, kappa = workload(args.cells)
+    threads = int(np.prod(w["parts"]))
+    nnz, _ = global_nnz(w["cells"][0])
+    # a CPU assembly has no device state to warm: one warm-up run is enough, so the
+    # whole run stays within a few minutes (about 10 s per full assembly)
+    for _ in range(min(args.warmup, 1)):
+        cpu_assembly(w, kappa, threads)
+    times = [cpu_assembly(w, kappa, threads) for _ in range(args.steps)]
+    t = float(np.mean(times))
+    v = nnz / t
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "cells": list(w["cells"]), "parts": list(w["parts"]), "order": 1,
+                       "strategy": "SubAssembledRows", "nnz": nnz, "l2": "inputs and outputs > L2"},
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"full workload, {args.steps} assemblies (integrate+COO+exchange+compress)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------------------------
+# GB300 arm
+# ------------------------------------------------------------------------------------
+def run_gb300(args, rank, world, local):
+    import torch
+    import gridap_gb300 as G
+    from gridap_gb300 import _lib as L
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    w, kappa = workload(args.cells)
+    be = G.GB300Backend(local)
+    # a dedicated (non-default) stream: the library launches on it and the CUDA
+    # events below are recorded on it
+    stream = torch.cuda.Stream(dev)
+    torch.cuda.set_stream(stream)
+    be.set_stream(stream.cuda_stream)
+    ranks = be.distribute(range(int(np.prod(w["parts"]))))
+    model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], w["cells"])
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 1), dirichlet_tags="boundary")
+    U = G.TrialFESpace(0.0, V)
+    assem = G.SparseMatrixAssembler(U, V, G.SubAssembledRows())
+    t_sym0 = time.perf_counter()
+    assem.symbolic()
+    t_sym = time.perf_counter() - t_sym0
+    ng, nnz_own, nnz_tot, kpn = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
+    L.call("gd_assembler_counts", assem.handle, C.byref(ng), C.byref(nnz_own), C.byref(nnz_tot), C.byref(kpn))
+    ngdofs, nnz, nnz_total, kernels_per_step = ng.value, nnz_own.value, nnz_tot.value, kpn.value
+    ncells = int(np.prod(w["cells"]))
+
+    kappa_d = torch.from_numpy(kappa).to(dev)
+    coeffs = L.gd_coeffs()
+    coeffs.kappa = kappa_d.data_ptr()
+    coeffs.f_nodal = None
+    coeffs.f_const = w["f"]
+    coeffs.degree = w["degree"]
+    coeffs.where = L.GD_DEVICE
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+
+    def step():
+        L.call("gd_assemble_numeric_async", assem.handle, C.byref(coeffs))
+
+    # correctness gate on the device result before timing (also validates kappa)
+    L.call("gd_assemble_numeric", assem.handle, C.byref(coeffs))
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- device-resident timing: per-step CUDA events, L2 flushed between steps ----
+    L.call("gd_assembler_set_profiling", assem.handle, 1)
+    clocks = ClockSampler(local)
+    barrier(world)
+    torch.cuda.synchronize()
+    clocks.start()
+    time.sleep(0.3)
+    t_wall0 = time.perf_counter()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    phase = []
+    for i in range(args.steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        step()
+        ev[i][1].record(stream)
+        m0, m1, m2 = C.c_double(), C.c_double(), C.c_double()
+        L.call("gd_assembler_phase_times", assem.handle, C.byref(m0), C.byref(m1), C.byref(m2))
+        phase.append((m0.value, m1.value, m2.value))
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall0
+    barrier(world)
+    clk = clocks.stop()
+    L.call("gd_assembler_set_profiling", assem.handle, 0)
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    ms = float(np.mean(step_ms))
+    ms_max = reduce_max(ms, world, dev)
+    value = world * nnz / (ms_max * 1e-3)
+
+    peak, peak_kind = measured_peaks()
+    alg_bytes = 8 * nnz + 8 * ngdofs + 8 * ncells
+    ph = np.array(phase)
+    ms_matrix = float(ph[:, 1].mean())
+    ms_rhs = float(ph[:, 2].mean())
+    ms_zero = float(ph[:, 0].mean())
+    step_gbs = alg_bytes / (ms * 1e-3) / 1e9
+    mat_bytes = 8 * nnz + 8 * ncells
+    mat_gbs = mat_bytes / (ms_matrix * 1e-3) / 1e9
+    traffic = profiled_traffic(w["name"])
+
+    # ---- end to end through the C-ABI with host buffers (pinned) ----
+    kappa_h = torch.from_numpy(kappa).pin_memory()
+    vals_h = torch.empty(nnz, dtype=torch.float64).pin_memory()
+    rhs_h = torch.empty(ngdofs, dtype=torch.float64).pin_memory()
+    hc = L.gd_coeffs()
+    hc.kappa = kappa_h.data_ptr()
+    hc.f_nodal = None
+    hc.f_const = w["f"]
+    hc.degree = w["degree"]
+    hc.where = L.GD_HOST
+    e2e_steps = max(3, min(args.steps, 10))
+    for _ in range(2):
+        L.call("gd_assemble_numeric", assem.handle, C.byref(hc))
+        L.call("gd_system_download", assem.handle, C.cast(C.c_void_p(rhs_h.data_ptr()), L.DP), C.cast(C.c_void_p(vals_h.data_ptr()), L.DP))
+    barrier(world)
+    e2e_t = []
+    for _ in range(e2e_steps):
+        t0 = time.perf_counter()
+        L.call("gd_assemble_numeric", assem.handle, C.byref(hc))
+        L.call("gd_system_download", assem.handle, C.cast(C.c_void_p(rhs_h.data_ptr()), L.DP), C.cast(C.c_void_p(vals_h.data_ptr()), L.DP))
+        e2e_t.append(time.perf_counter() - t0)
+    e2e_s = reduce_max(float(np.mean(e2e_t)), world, dev)
+    e2e_value = world * nnz / e2e_s
+    checksum = float(rhs_h.numpy().sum())
+
+    # ---- solve: Jacobi-PCG to 1e-8 on the assembled system ----
+    solve = None
+    if not args.no_solve:
+        x = torch.empty(ngdofs, dtype=torch.float64, device=dev)
+        st = L.gd_solve_stats()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        rc = L.load().gd_solve(assem.handle, L.GD_SOLVE_JACOBI_PCG, 1e-8, 20000, C.c_void_p(x.data_ptr()),
+                               L.GD_DEVICE, C.byref(st))
+        t_solve = time.perf_counter() - t0
+        solve = {"method": "jacobi_pcg_fp64", "rtol": 1e-8, "seconds": t_solve, "iterations": st.iterations,
+                 "rel_residual": st.rel_residual, "converged": bool(st.converged and rc == 0),
+                 "ms_per_iteration": 1e3 * t_solve / max(st.iterations, 1)}
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = int(np.prod(w["parts"]))
+        ta = cpu_assembly(w, kappa, threads)
+        cpu = {"value": nnz / ta, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": "one full assembly of the same workload by the oracle's C restatement of the reference "
+                         "(per-cell quadrature, COO, ghost-row exchange, sparse compression), one thread per part"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": w["name"], "cells": list(w["cells"]), "parts": list(w["parts"]), "order": 1,
+                       "quadrature_degree": w["degree"], "strategy": "SubAssembledRows", "nnz": nnz,
+                       "nnz_stored_with_ghost_rows": nnz_total, "free_dofs": ngdofs, "cells_total": ncells,
+                       "l2": f"flushed between steps ({L2_FLUSH_BYTES >> 20} MiB write); outputs > L2",
+                       "parallelism": f"replicas x{world}" if world > 1 else "1 GPU, 8 parts as slabs"},
+            "cells_per_s": world * ncells / (ms_max * 1e-3),
+            "roofline": {"bound": "hbm", "achieved": step_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": step_gbs / peak, "traffic": traffic,
+                         "peak_kind": peak_kind, "algorithmic_bytes": alg_bytes,
+                         "scope": "whole numeric assembly (ghost-row zeroing + matrix kernel + rhs kernel)",
+                         "matrix_kernel": {"ms": ms_matrix, "bytes": mat_bytes, "achieved": mat_gbs,
+                                           "frac": mat_gbs / peak},
+                         "rhs_kernel_ms": ms_rhs, "ghost_zero_ms": ms_zero},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * ncells,
+                    "d2h_bytes_per_step": 8 * nnz + 8 * ngdofs, "ms_per_step": 1e3 * e2e_s, "rhs_checksum": checksum},
+            "gpu_launches": kernels_per_step * args.steps,
+            "clocks": clk,
+            "symbolic_s": t_sym,
+            "wall_s_timed_region": t_wall,
+            "solve": solve,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    be.close()
+
+
+def main():
+    args = parse()
+    rank, world, local = dist_env()
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world)
+        else:
+            run_gb300(args, rank, world, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -228,10 +228,20 @@ struct gd_asm {
   gd::DBuf<int32_t> gcol_lid;
   // per concatenated local node: local column id or -1
   gd::DBuf<int32_t> node_col;
+  // Q1 row patterns: per owned row a pattern id; per pattern 32 bytes = the CSR
+  // position of each canonical stencil neighbour (0xFF = absent), byte 31 = length
+  bool fast_q1 = false;
+  int npat = 0;
+  gd::DBuf<uint16_t> row_pat;
+  gd::DBuf<uint8_t> pat;
+  int q1_grid = 0;
   // reference element tables (device)
   gd::DBuf<double> Khat, Mhat, Fhat;
   int ref_degree = -1;
   gd::DBuf<double> kappa_dev, f_dev;   // staging for host inputs
+  // profiling events: start, after ghost zeroing, after matrix, after rhs
+  bool profiling = false;
+  cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
   // solver workspace
   gd::DBuf<double> w;              // vectors
   gd::DBuf<double> dred;           // reduction partials

@@ -317,6 +317,235 @@ __global__ void k_numeric_rhs(Geom g, int64_t nrows_own, const int32_t* __restri
   if (nbad) atomicAdd(bad, nbad);
 }
 
+
+// ---- Q1 fast path: one thread per owned row, values staged in shared memory ----------------
+// Each thread loads the kappa of the 2^DIM cells around its node once and forms the
+// whole 3^DIM stencil in registers (64 FMAs in 3D, unrolled at compile time); the row's
+// pattern id gives the CSR position of every neighbour.  A 128-row chunk of values
+// is contiguous in the CSR value array; it is written into a shared-memory buffer and
+// streamed to global memory with one TMA bulk store (cp.async.bulk), double-buffered
+// so the store of one chunk overlaps the computation of the next.  The right-hand side
+// (source term and Dirichlet lifting) is fused.  Per row the kernel reads 4 bytes of
+// node id and 2 bytes of pattern id; per entry it only writes the value.
+constexpr int kQ1Rows = 128;
+
+__device__ __forceinline__ void bulk_store_s2g(void* gdst, const void* ssrc, uint32_t bytes) {
+  const uint32_t saddr = (uint32_t)__cvta_generic_to_shared(ssrc);
+  asm volatile("cp.async.bulk.global.shared::cta.bulk_group [%0], [%1], %2;" ::"l"(gdst), "r"(saddr), "r"(bytes)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+template <int N>
+__device__ __forceinline__ void bulk_wait_all() {
+  asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+template <int DIM>
+struct Q1 {
+  static constexpr int S = DIM == 3 ? 27 : 9;   // stencil neighbours
+  static constexpr int NC = 1 << DIM;           // cells around a node = nodes of a cell
+  static constexpr int BUF = kQ1Rows * S + 2;   // doubles per staging buffer (even)
+  static constexpr int TAB = 2 * NC * NC + NC + (NC & 1) + 4;   // Khat, Mhat, Fhat, warp sums
+  static constexpr size_t SMEM = sizeof(double) * (TAB + 2 * BUF);
+};
+
+template <int DIM, bool FN, bool UD>
+__global__ void __launch_bounds__(kQ1Rows)
+k_numeric_q1(Geom g, int64_t nrows, int64_t nchunks, const int64_t* __restrict__ rowptr,
+             const int32_t* __restrict__ row_node, const uint16_t* __restrict__ row_pat,
+             const uint8_t* __restrict__ pat, const double* __restrict__ kappa, const double* __restrict__ Khat,
+             const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
+             const double* __restrict__ f_nodal, const double* __restrict__ u_dir, double* __restrict__ vals,
+             double* __restrict__ rhs, int32_t* __restrict__ bad) {
+  using Q = Q1<DIM>;
+  constexpr int S = Q::S, NC = Q::NC;
+  extern __shared__ __align__(128) double smem[];
+  double* sK = smem;
+  double* sM = sK + NC * NC;
+  double* sF = sM + NC * NC;
+  int* s_wsum = (int*)(sF + NC + (NC & 1));
+  double* buf0 = smem + Q::TAB;
+  double* buf1 = buf0 + Q::BUF;
+  const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+  for (int i = tid; i < NC * NC; i += blockDim.x) {
+    sK[i] = Khat[i];
+    sM[i] = Mhat[i];
+  }
+  if (tid < NC) sF[tid] = Fhat[tid];
+  __syncthreads();
+  const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
+  const int64_t n0 = g.n[0], n1 = g.n[1], n2 = DIM == 3 ? g.n[2] : 1;
+  int nbad = 0;
+  int b = 0;
+  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
+    const int64_t r0 = c * kQ1Rows;
+    const int64_t r = r0 + tid;
+    const bool valid = r < nrows;
+    double v[S];
+    uint32_t pw[8];
+    int len = 0;
+    if (valid) {
+      const uint32_t lin = (uint32_t)row_node[r];
+      int64_t X[3];
+      X[0] = lin % N0;
+      if (DIM == 3) {
+        const uint32_t t = lin / N0;
+        X[1] = t % N1;
+        X[2] = t / N1;
+      } else {
+        X[1] = lin / N0;
+        X[2] = 0;
+      }
+      const uint4* pp = reinterpret_cast<const uint4*>(pat + (int64_t)row_pat[r] * 32);
+      const uint4 p0 = __ldg(pp), p1 = __ldg(pp + 1);
+      pw[0] = p0.x; pw[1] = p0.y; pw[2] = p0.z; pw[3] = p0.w;
+      pw[4] = p1.x; pw[5] = p1.y; pw[6] = p1.z; pw[7] = p1.w;
+      len = (int)(pw[7] >> 24);
+      // kappa of the cells around X; slot a: cell X - 1 + bit_d(a) per direction
+      double kap[NC];
+      bool cin[NC];
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        const int64_t cx = X[0] - 1 + (a & 1), cy = X[1] - 1 + ((a >> 1) & 1);
+        const int64_t cz = DIM == 3 ? X[2] - 1 + ((a >> 2) & 1) : 0;
+        cin[a] = cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && (DIM == 2 || (cz >= 0 && cz < n2));
+        kap[a] = cin[a] ? __ldg(kappa + cx + n0 * (cy + n1 * cz)) : 0.0;
+        if (cin[a] && !(kap[a] > 0.0 && kap[a] < INFINITY)) ++nbad;
+      }
+      double bval = 0.0;
+#pragma unroll
+      for (int a = 0; a < NC; ++a)
+        if (cin[a]) bval += f_const * sF[(NC - 1) - a];   // local index of X in slot a is (1-bit_d(a))
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const int o0 = s % 3 - 1, o1 = (s / 3) % 3 - 1, o2 = DIM == 3 ? s / 9 - 1 : 0;
+        double acc = 0.0, macc = 0.0;
+#pragma unroll
+        for (int a = 0; a < NC; ++a) {
+          const int a0 = a & 1, a1 = (a >> 1) & 1, a2 = DIM == 3 ? (a >> 2) & 1 : 0;
+          const bool ok = (o0 == 0 || (o0 < 0) == (a0 == 0)) && (o1 == 0 || (o1 < 0) == (a1 == 0)) &&
+                          (DIM == 2 || o2 == 0 || (o2 < 0) == (a2 == 0));
+          if (ok) {
+            const int lx = (1 - a0) + 2 * (1 - a1) + (DIM == 3 ? 4 * (1 - a2) : 0);
+            const int ly = (1 - a0 + o0) + 2 * (1 - a1 + o1) + (DIM == 3 ? 4 * (1 - a2 + o2) : 0);
+            acc += kap[a] * sK[lx * NC + ly];
+            if (FN && cin[a]) macc += sM[lx * NC + ly];
+          }
+        }
+        v[s] = acc;
+        if (FN || UD) {
+          const int64_t Y0 = X[0] + o0, Y1 = X[1] + o1, Y2 = X[2] + o2;
+          const bool in = Y0 >= 0 && Y0 < g.N[0] && Y1 >= 0 && Y1 < g.N[1] && (DIM == 2 || (Y2 >= 0 && Y2 < g.N[2]));
+          if (in) {
+            const int64_t ylin = Y0 + g.N[0] * (Y1 + g.N[1] * Y2);
+            if (FN) bval += macc * __ldg(f_nodal + ylin);
+            if (UD) {
+              const int64_t Yv[3] = {Y0, Y1, Y2};
+              if (node_is_dirichlet(g, Yv)) bval -= acc * __ldg(u_dir + ylin);
+            }
+          }
+        }
+      }
+      rhs[r] = bval;
+    }
+    // block-wide exclusive scan of the row lengths
+    int incl = len;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += y;
+    }
+    if (tid == 0) bulk_wait_read<1>();   // the store that last read this buffer is done
+    __syncthreads();
+    if (lane == 31) s_wsum[wid] = incl;
+    __syncthreads();
+    int woff = 0, total = 0;
+#pragma unroll
+    for (int w = 0; w < kQ1Rows / 32; ++w) {
+      const int t = s_wsum[w];
+      woff += w < wid ? t : 0;
+      total += t;
+    }
+    const int off = woff + incl - len;
+    const int64_t e0 = rowptr[r0];
+    const int ofs = (int)(e0 & 1);   // keeps shared and global addresses congruent mod 16 bytes
+    double* buf = b ? buf1 : buf0;
+    if (valid) {
+#pragma unroll
+      for (int s = 0; s < S; ++s) {
+        const uint32_t pos = (pw[s >> 2] >> (8 * (s & 3))) & 0xFFu;
+        if (pos != 0xFFu) buf[ofs + off + (int)pos] = v[s];
+      }
+    }
+    fence_proxy_async_smem();
+    __syncthreads();
+    if (tid == 0 && total > 0) {
+      const int64_t e1 = e0 + total;
+      if (ofs) vals[e0] = buf[1];                                   // unaligned head
+      const int64_t ja = e0 + ofs, jb = e1 - (e1 & 1);
+      if ((e1 & 1) && e1 - 1 >= ja) vals[e1 - 1] = buf[ofs + total - 1];   // unaligned tail
+      if (jb > ja) bulk_store_s2g(vals + ja, buf + ofs + (ja - e0), (uint32_t)((jb - ja) * sizeof(double)));
+    }
+    if (tid == 0) bulk_commit();
+    b ^= 1;
+  }
+  if (tid == 0) bulk_wait_all<0>();
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+template <int DIM, bool FN, bool UD>
+static int launch_q1_inst(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, const double* udir,
+                          int32_t* bad, cudaStream_t st) {
+  using Q = Q1<DIM>;
+  static int blocks_per_sm = -1;
+  static int num_sms = 0;
+  auto kern = k_numeric_q1<DIM, FN, UD>;
+  if (blocks_per_sm < 0) {
+    GD_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::SMEM));
+    GD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kQ1Rows, Q::SMEM));
+    int dev = 0;
+    GD_CUDA_TRY(cudaGetDevice(&dev));
+    GD_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
+    if (blocks_per_sm < 1) blocks_per_sm = 1;
+  }
+  const int64_t n = A->ngdofs;
+  const int64_t nchunks = (n + kQ1Rows - 1) / kQ1Rows;
+  int64_t grid = (int64_t)blocks_per_sm * num_sms;
+  if (grid > nchunks) grid = nchunks;
+  A->q1_grid = (int)grid;
+  kern<<<(unsigned)grid, kQ1Rows, Q::SMEM, st>>>(A->test->geom, n, nchunks, A->rowptr.p, A->row_node.p,
+                                                  A->row_pat.p, A->pat.p, kappa, A->Khat.p, A->Mhat.p, A->Fhat.p,
+                                                  f_const, f_nodal, udir, A->vals.p, A->rhs.p, bad);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+template <int DIM>
+static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, int32_t* bad,
+                     cudaStream_t st) {
+  const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
+  if (A->ngdofs == 0) return GD_OK;
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
+  int s;
+  if (f_nodal && udir) s = launch_q1_inst<DIM, true, true>(A, kappa, f_nodal, 0.0, udir, bad, st);
+  else if (f_nodal) s = launch_q1_inst<DIM, true, false>(A, kappa, f_nodal, 0.0, nullptr, bad, st);
+  else if (udir) s = launch_q1_inst<DIM, false, true>(A, kappa, nullptr, f_const, udir, bad, st);
+  else s = launch_q1_inst<DIM, false, false>(A, kappa, nullptr, f_const, nullptr, bad, st);
+  if (s != GD_OK) return s;
+  if (A->profiling) {   // one fused kernel: the rhs phase is empty
+    GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
+    GD_CUDA_TRY(cudaEventRecord(A->ev[3], st));
+  }
+  return GD_OK;
+}
+
 template <int DIM, int K>
 static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal, double f_const,
                           int32_t* bad, cudaStream_t st) {
@@ -324,6 +553,7 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   const int64_t R = A->ngdofs;
   if (R == 0) return GD_OK;
   const unsigned nb = (unsigned)((R + kRowsPerBlock - 1) / kRowsPerBlock);
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
   if (A->code_bytes == 1)
     k_numeric_matrix<DIM, K, uint8_t><<<nb, kNumericThreads, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, A->code.p,
                                                                        kappa, A->Khat.p, A->vals.p);
@@ -332,11 +562,13 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
                                                                         (const uint16_t*)A->code.p, kappa,
                                                                         A->Khat.p, A->vals.p);
   GD_CUDA_TRY(cudaGetLastError());
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
   k_numeric_rhs<DIM, K><<<(unsigned)((R + 127) / 128), 128, 0, st>>>(g, R, A->row_node.p, kappa, A->Khat.p,
                                                                      A->Mhat.p, A->Fhat.p, f_const, f_nodal, udir,
                                                                      A->rhs.p, bad);
   GD_CUDA_TRY(cudaGetLastError());
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[3], st));
   return GD_OK;
 }
 
@@ -376,11 +608,13 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   if (!A->dred.p) GD_TRY(dalloc(A->dred, 4096));
   int32_t* bad = (int32_t*)A->dred.p;
   GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
-  // ghost rows: explicit zeros
-  if (A->nnz_total > A->nnz_own)
-    GD_CUDA_TRY(cudaMemsetAsync(A->vals.p + A->nnz_own, 0, sizeof(double) * (A->nnz_total - A->nnz_own), st));
+  // Ghost rows (SubAssembledRows) hold explicit zeros: they were cleared by the symbolic
+  // phase and no numeric kernel writes them.
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[0], st));
   int s = GD_ERR_UNSUPPORTED;
-  if (g.dim == 2 && g.k == 1) s = launch_numeric<2, 1>(A, kappa, fn, c->f_const, bad, st);
+  if (A->fast_q1 && g.dim == 3) s = launch_q1<3>(A, kappa, fn, c->f_const, bad, st);
+  else if (A->fast_q1 && g.dim == 2) s = launch_q1<2>(A, kappa, fn, c->f_const, bad, st);
+  else if (g.dim == 2 && g.k == 1) s = launch_numeric<2, 1>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 2 && g.k == 2) s = launch_numeric<2, 2>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 2 && g.k == 3) s = launch_numeric<2, 3>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 3 && g.k == 1) s = launch_numeric<3, 1>(A, kappa, fn, c->f_const, bad, st);
@@ -399,6 +633,35 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
 }
 
 }  // namespace gd
+
+extern "C" int gd_assembler_set_profiling(gd_asm* A, int on) {
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_set_profiling: null assembler");
+  if (on && !A->ev[0])
+    for (int i = 0; i < 4; ++i) GD_CUDA_TRY(cudaEventCreate(&A->ev[i]));
+  A->profiling = on != 0;
+  return GD_OK;
+}
+
+extern "C" int gd_assembler_phase_times(const gd_asm* A, double* ms0, double* ms1, double* ms2) {
+  if (!A || !A->ev[0]) return gd::fail(GD_ERR_STATE, "gd_assembler_phase_times: profiling was not enabled");
+  GD_CUDA_TRY(cudaEventSynchronize(A->ev[3]));
+  float t[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i) GD_CUDA_TRY(cudaEventElapsedTime(&t[i], A->ev[i], A->ev[i + 1]));
+  if (ms0) *ms0 = t[0];
+  if (ms1) *ms1 = t[1];
+  if (ms2) *ms2 = t[2];
+  return GD_OK;
+}
+
+extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nnz_owned, int64_t* nnz_total,
+                                   int32_t* kernels) {
+  if (!A || !A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_counts: run gd_assemble_symbolic first");
+  if (ngdofs) *ngdofs = A->ngdofs;
+  if (nnz_owned) *nnz_owned = A->nnz_own;
+  if (nnz_total) *nnz_total = A->nnz_total;
+  if (kernels) *kernels = A->fast_q1 ? 1 : 2;   // fused Q1 kernel, or k_numeric_matrix + k_numeric_rhs
+  return GD_OK;
+}
 
 extern "C" int gd_assemble_numeric(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, true); }
 extern "C" int gd_assemble_numeric_async(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, false); }

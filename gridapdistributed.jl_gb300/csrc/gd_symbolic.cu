@@ -398,9 +398,174 @@ __global__ void k_row_fill(Geom g, const DevPart* __restrict__ parts, int64_t ng
   }
 }
 
+
+// ---- Q1 row patterns ---------------------------------------------------------------------
+// For an owned Q1 row every lattice neighbour within +-1 that is free shares a cell with
+// it.  perm[s] = CSR position of canonical neighbour s (offsets lexicographic, x
+// fastest), 0xFF if absent.  Rows with equal perm share a pattern id, so the numeric
+// kernel reads 2 bytes per row instead of a code per entry.
+template <int DIM>
+__global__ void k_row_perm_q1(Geom g, const DevPart* __restrict__ parts, int64_t nrows_own,
+                              const int32_t* __restrict__ row_node, const int32_t* __restrict__ row_part,
+                              const int32_t* __restrict__ node_lid, const int32_t* __restrict__ lid_col,
+                              const int64_t* __restrict__ rowptr, uint8_t* __restrict__ rec,
+                              unsigned long long* __restrict__ hash, int32_t* __restrict__ err) {
+  constexpr int S = DIM == 3 ? 27 : 9;
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows_own) return;
+  const DevPart& P = parts[row_part[r]];
+  int64_t X[kMaxDim] = {0, 0, 0};
+  lattice_coords(g, row_node[r], X);
+  int32_t col[S];
+  int n = 0;
+#pragma unroll
+  for (int s = 0; s < S; ++s) {
+    int64_t Y[kMaxDim] = {X[0] + (s % 3) - 1, X[1] + (s / 3) % 3 - 1, DIM == 3 ? X[2] + s / 9 - 1 : 0};
+    bool in = true;
+    for (int d = 0; d < DIM; ++d) in = in && Y[d] >= 0 && Y[d] < g.N[d];
+    col[s] = -1;
+    if (in && !node_is_dirichlet(g, Y)) {
+      int64_t bi = box_index(g, P, Y);
+      int32_t lid = bi >= 0 ? node_lid[P.node_off + bi] : -1;
+      col[s] = lid >= 0 ? lid_col[P.lid_off + lid] : -2;
+      if (col[s] < 0) atomicExch(err, 3);
+      ++n;
+    }
+  }
+  uint8_t* out = rec + r * 32;
+  unsigned long long h = 1469598103934665603ull;   // FNV-1a over the 32-byte record
+  for (int s = 0; s < 32; ++s) {
+    uint8_t v = 0xFF;
+    if (s < S && col[s] >= 0) {
+      int rank = 0;
+      for (int t = 0; t < S; ++t) rank += (col[t] >= 0 && col[t] < col[s]);
+      v = (uint8_t)rank;
+    }
+    if (s == 31) v = (uint8_t)n;
+    out[s] = v;
+    h = (h ^ v) * 1099511628211ull;
+  }
+  if (h == ~0ull) h = 0;
+  hash[r] = h;
+  if (rowptr[r + 1] - rowptr[r] != n) atomicExch(err, 4);
+}
+
+__global__ void k_pat_insert(int64_t n, const unsigned long long* __restrict__ hash, unsigned long long* keys,
+                             int32_t* rep, int64_t mask) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const unsigned long long h = hash[r];
+  int64_t slot = (int64_t)(h & (unsigned long long)mask);
+  for (int64_t probe = 0; probe <= mask; ++probe) {
+    unsigned long long prev = atomicCAS(&keys[slot], ~0ull, h);
+    if (prev == ~0ull || prev == h) {
+      atomicMin(&rep[slot], (int32_t)r);
+      return;
+    }
+    slot = (slot + 1) & mask;
+  }
+}
+
+__global__ void k_pat_occupied(int64_t cap, const unsigned long long* __restrict__ keys, int32_t* __restrict__ occ) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < cap) occ[i] = keys[i] != ~0ull;
+}
+
+__global__ void k_pat_assign(int64_t n, const unsigned long long* __restrict__ hash,
+                             const unsigned long long* __restrict__ keys, const int32_t* __restrict__ rep,
+                             const int64_t* __restrict__ slot_id, const uint8_t* __restrict__ rec, int64_t mask,
+                             uint16_t* __restrict__ row_pat, int32_t* __restrict__ err) {
+  int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const unsigned long long h = hash[r];
+  int64_t slot = (int64_t)(h & (unsigned long long)mask);
+  for (int64_t probe = 0; probe <= mask && keys[slot] != h; ++probe) slot = (slot + 1) & mask;
+  if (keys[slot] != h) {
+    atomicExch(err, 5);
+    return;
+  }
+  const int64_t id = slot_id[slot];
+  const uint8_t* a = rec + (int64_t)r * 32;
+  const uint8_t* b = rec + (int64_t)rep[slot] * 32;
+  for (int s = 0; s < 32; ++s)
+    if (a[s] != b[s]) atomicExch(err, 6);   // hash collision: fall back to the generic kernel
+  row_pat[r] = id < 65536 ? (uint16_t)id : 0;
+}
+
+__global__ void k_pat_table(int64_t cap, const unsigned long long* __restrict__ keys, const int32_t* __restrict__ rep,
+                            const int64_t* __restrict__ slot_id, const uint8_t* __restrict__ rec, int64_t npat,
+                            uint8_t* __restrict__ pat) {
+  int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= cap || keys[i] == ~0ull) return;
+  const int64_t id = slot_id[i];
+  if (id >= npat) return;
+  for (int s = 0; s < 32; ++s) pat[id * 32 + s] = rec[(int64_t)rep[i] * 32 + s];
+}
+
 }  // namespace gd
 
 using namespace gd;
+
+// Builds the Q1 pattern table; leaves fast_q1 false (generic kernel) when the
+// patterns do not fit 16-bit ids or a hash collision is detected.
+static int build_q1_patterns(gd_asm* A, const int32_t* lid_col) {
+  gd_space* S = A->test;
+  const Geom& g = S->geom;
+  cudaStream_t st = S->model->ctx->stream;
+  A->fast_q1 = false;
+  const int64_t n = A->ngdofs;
+  if (g.k != 1 || n == 0) return GD_OK;
+  const int T = 256;
+  DBuf<uint8_t> rec;
+  DBuf<unsigned long long> hash, keys;
+  DBuf<int32_t> rep, occ, err;
+  DBuf<int64_t> slot_id;
+  int64_t cap = 1024;
+  while (cap < 2 * n) cap <<= 1;
+  GD_TRY(dalloc(rec, n * 32));
+  GD_TRY(dalloc(hash, n));
+  GD_TRY(dalloc(keys, cap));
+  GD_TRY(dalloc(rep, cap));
+  GD_TRY(dalloc(occ, cap));
+  GD_TRY(dalloc(slot_id, cap + 1));
+  GD_TRY(dalloc(err, 1));
+  GD_CUDA_TRY(cudaMemsetAsync(err.p, 0, sizeof(int32_t), st));
+  GD_CUDA_TRY(cudaMemsetAsync(keys.p, 0xFF, sizeof(unsigned long long) * cap, st));
+  GD_CUDA_TRY(cudaMemsetAsync(rep.p, 0x7F, sizeof(int32_t) * cap, st));
+  if (g.dim == 3)
+    k_row_perm_q1<3><<<nblk(n, T), T, 0, st>>>(g, A->d_parts.p, n, A->row_node.p, A->row_part.p, S->node_lid.p,
+                                               lid_col, A->rowptr.p, rec.p, hash.p, err.p);
+  else
+    k_row_perm_q1<2><<<nblk(n, T), T, 0, st>>>(g, A->d_parts.p, n, A->row_node.p, A->row_part.p, S->node_lid.p,
+                                               lid_col, A->rowptr.p, rec.p, hash.p, err.p);
+  GD_TRY(launch_ok("k_row_perm_q1"));
+  k_pat_insert<<<nblk(n, T), T, 0, st>>>(n, hash.p, keys.p, rep.p, cap - 1);
+  GD_TRY(launch_ok("k_pat_insert"));
+  k_pat_occupied<<<nblk(cap, T), T, 0, st>>>(cap, keys.p, occ.p);
+  GD_TRY(launch_ok("k_pat_occupied"));
+  GD_TRY(exclusive_scan_i32(occ.p, slot_id.p, cap, st));
+  int64_t npat = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&npat, slot_id.p + cap, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  GD_TRY(dalloc(A->row_pat, n));
+  k_pat_assign<<<nblk(n, T), T, 0, st>>>(n, hash.p, keys.p, rep.p, slot_id.p, rec.p, cap - 1, A->row_pat.p, err.p);
+  GD_TRY(launch_ok("k_pat_assign"));
+  GD_TRY(dalloc(A->pat, std::max<int64_t>(npat, 1) * 32));
+  k_pat_table<<<nblk(cap, T), T, 0, st>>>(cap, keys.p, rep.p, slot_id.p, rec.p, npat, A->pat.p);
+  GD_TRY(launch_ok("k_pat_table"));
+  int32_t herr = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&herr, err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (herr == 3 || herr == 4) return fail(GD_ERR_STATE, "symbolic: Q1 row pattern disagrees with the CSR pattern");
+  if (herr == 0 && npat < 65536) {
+    A->fast_q1 = true;
+    A->npat = (int)npat;
+  } else {
+    dfreeb(A->row_pat);
+    dfreeb(A->pat);
+  }
+  return GD_OK;
+}
 
 // ---------------------------------------------------------------------------------
 // C ABI
@@ -444,6 +609,10 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->w);
   dfreeb(A->dred);
   dfreeb(A->dinv);
+  dfreeb(A->row_pat);
+  dfreeb(A->pat);
+  for (int i = 0; i < 4; ++i)
+    if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;
   return GD_OK;
 }
@@ -595,6 +764,7 @@ static int symbolic_impl(gd_asm* A) {
   int32_t herr = 0;
   GD_CUDA_TRY(cudaMemcpyAsync(&herr, err.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (!herr) GD_TRY(build_q1_patterns(A, lid_col.p));
   dfreeb(err);
   dfreeb(own_lid);
   dfreeb(len);

@@ -1,0 +1,48 @@
+"""Seeded synthetic inputs for the benchmark configurations.
+
+The coefficient fields are lognormal, kappa = exp(g), with g a Gaussian random
+field of standard deviation sigma and squared-exponential correlation
+exp(-r^2 / (2 l^2)).  g is drawn by spectral synthesis on a periodically embedded
+grid twice the mesh size per direction (numpy PCG64, seed given by the caller),
+evaluated at the cell centres and normalised to mean 0 and the target sigma.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def gaussian_random_field(cells, sigma=1.0, corr_len=0.1, seed=0, domain_len=1.0):
+    """g at the cell centres of a uniform grid with ``cells`` cells per direction.
+
+    Returns a flat float64 array in lexicographic cell order (x fastest)."""
+    cells = tuple(int(c) for c in cells)
+    dim = len(cells)
+    rng = np.random.Generator(np.random.PCG64(seed))
+    M = tuple(2 * c for c in cells)
+    h = [domain_len / c for c in cells]
+    # wavenumbers of the embedded periodic grid (axis order z,y,x for C-order arrays)
+    ks = [2 * np.pi * np.fft.fftfreq(M[d], d=h[d]) for d in range(dim)]
+    grids = np.meshgrid(*[ks[d] for d in reversed(range(dim))], indexing="ij", sparse=True)
+    k2 = sum(g * g for g in grids)
+    amp = np.exp(-k2 * corr_len * corr_len / 4.0)   # sqrt of the squared-exponential spectrum
+    shape = tuple(reversed(M))
+    noise = rng.standard_normal(shape) + 1j * rng.standard_normal(shape)
+    field = np.fft.ifftn(amp * noise).real
+    field = field[tuple(slice(0, c) for c in reversed(cells))]
+    field = field - field.mean()
+    std = field.std()
+    if std > 0:
+        field = field * (sigma / std)
+    return np.ascontiguousarray(field.reshape(-1), dtype=np.float64)
+
+
+def lognormal_kappa(cells, sigma=1.0, corr_len=0.1, seed=0):
+    return np.exp(gaussian_random_field(cells, sigma, corr_len, seed))
+
+
+# The 3D variable-coefficient Poisson workload: 128^3 Q1 hex cells on the unit
+# cube, parts (2,2,2), kappa = exp(g) (sigma 1, correlation length 0.1), f = 1,
+# homogeneous Dirichlet on the whole boundary, quadrature degree 2.
+POISSON3D_128 = dict(name="poisson3d_q1_128^3_parts2x2x2", dim=3, cells=(128, 128, 128), parts=(2, 2, 2),
+                     domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=1, degree=2, sigma=1.0, corr_len=0.1,
+                     f=1.0, seed=1000)

@@ -145,6 +145,17 @@ int gd_assemble_numeric(gd_asm* a, const gd_coeffs* c);
 /* Same, without the final stream synchronisation (for timing loops). */
 int gd_assemble_numeric_async(gd_asm* a, const gd_coeffs* c);
 
+/* Record CUDA events around the phases of every numeric assembly (off by default). */
+int gd_assembler_set_profiling(gd_asm* a, int on);
+/* Event-timed durations (ms) of the last profiled numeric assembly: clearing the
+ * ghost-row values, the matrix-value kernel, the right-hand-side kernel. */
+int gd_assembler_phase_times(const gd_asm* a, double* ms_ghost_zero, double* ms_matrix, double* ms_rhs);
+/* Counts of the assembled system: global DOFs, stored entries of the owned rows,
+ * stored entries of all rows (owned + ghost), and the kernels one numeric
+ * assembly launches. */
+int gd_assembler_counts(const gd_asm* a, int64_t* ngdofs, int64_t* nnz_owned, int64_t* nnz_total,
+                        int32_t* kernels_per_numeric);
+
 /* Sizes of one part's local matrix: rows (owned + ghost), columns (owned + ghost),
  * stored entries, ghost rows, ghost columns. */
 int gd_matrix_sizes(const gd_asm* a, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,

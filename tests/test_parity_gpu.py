@@ -53,6 +53,12 @@ CASES = [
     dict(dim=3, n=(3, 4, 3), parts=(1, 2, 2), order=3, sides=(1, 0, 1, 0, 1, 0), seed=7),
     dict(dim=3, n=(4, 4, 4), parts=(2, 2, 2), order=1, sides=(0, 0, 0, 0, 0, 0), seed=8),
     dict(dim=3, n=(5, 5, 5), parts=(2, 2, 2), order=2, sides=(1, 0, 0, 0, 0, 0), seed=9, f_nodal=True),
+    # Q1 with free boundary nodes, a nodal source and non-zero Dirichlet values (lifting)
+    dict(dim=3, n=(6, 5, 4), parts=(2, 1, 2), order=1, sides=(1, 1, 0, 1, 1, 0), seed=10, f_nodal=True,
+         u=lambda x, y, z: x + 2 * y + z * z),
+    dict(dim=2, n=(6, 4), parts=(2, 2), order=1, sides=(0, 1, 1, 0), seed=11, f_nodal=True,
+         u=lambda x, y: 1.0 + x * y),
+    dict(dim=3, n=(7, 6, 5), parts=(3, 2, 1), order=1, seed=12, u=lambda x, y, z: 2.0 - x),
 ]
 
 
