@@ -230,7 +230,7 @@ def run_gb300(args, rank, world, local):
     t_sym = time.perf_counter() - t_sym0
     ng, nnz_own, nnz_tot, kpn = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
     L.call("gd_assembler_counts", assem.handle, C.byref(ng), C.byref(nnz_own), C.byref(nnz_tot), C.byref(kpn))
-    ngdofs, nnz, nnz_total, kernels_per_step = ng.value, nnz_own.value, nnz_tot.value, kpn.value
+    ngdofs, nnz, nnz_total = ng.value, nnz_own.value, nnz_tot.value
     ncells = int(np.prod(w["cells"]))
 
     kappa_d = torch.from_numpy(kappa).to(dev)
@@ -245,8 +245,16 @@ def run_gb300(args, rank, world, local):
     def step():
         L.call("gd_assemble_numeric_async", assem.handle, C.byref(coeffs))
 
-    # correctness gate on the device result before timing (also validates kappa)
+    # first numeric assembly: validates kappa and runs the launch-shape autotuner
     L.call("gd_assemble_numeric", assem.handle, C.byref(coeffs))
+    sh, rows_, nbuf_, nsh = C.c_int32(), C.c_int32(), C.c_int32(), C.c_int32()
+    shape_ms = (C.c_float * 8)()
+    L.call("gd_assembler_tuning", assem.handle, C.byref(sh), C.byref(rows_), C.byref(nbuf_), shape_ms,
+           C.byref(nsh))
+    tuning = {"shape": sh.value, "rows_per_chunk": rows_.value, "staging_buffers": nbuf_.value,
+              "ms_per_shape": [round(shape_ms[i], 4) for i in range(nsh.value)]}
+    L.call("gd_assembler_counts", assem.handle, None, None, None, C.byref(kpn))
+    kernels_per_step = kpn.value   # known once the first numeric assembly chose its kernels
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -358,6 +366,7 @@ def run_gb300(args, rank, world, local):
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * ncells,
                     "d2h_bytes_per_step": 8 * nnz + 8 * ngdofs, "ms_per_step": 1e3 * e2e_s, "rhs_checksum": checksum},
             "gpu_launches": kernels_per_step * args.steps,
+            "autotune": tuning,
             "clocks": clk,
             "symbolic_s": t_sym,
             "wall_s_timed_region": t_wall,

@@ -235,6 +235,13 @@ struct gd_asm {
   gd::DBuf<uint16_t> row_pat;
   gd::DBuf<uint8_t> pat;
   int q1_grid = 0;
+  int q1_shape = -1;            // autotuned launch shape (-1: not tuned yet)
+  float q1_shape_ms[8] = {0};
+  gd::DBuf<double> w_cells;   // prescaled coefficients (cube Q1 path)
+  std::string q1c_blob;        // cached Q1 class constants for the current reference element
+  double q1c_f0 = 0.0;
+  bool q1c_cube = false;
+  int q1c_degree = -1;
   // reference element tables (device)
   gd::DBuf<double> Khat, Mhat, Fhat;
   int ref_degree = -1;

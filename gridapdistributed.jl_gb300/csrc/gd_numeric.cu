@@ -14,6 +14,7 @@
 // coalesced, in CSR order.  Ghost rows (SubAssembledRows) hold explicit zeros
 // (Algebra.jl:1084): their range is cleared with a memset.
 #include <cmath>
+#include <cstring>
 #include <string>
 #include <vector>
 
@@ -347,114 +348,221 @@ __device__ __forceinline__ void fence_proxy_async_smem() {
   asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
 }
 
-template <int DIM>
+template <int DIM, int ROWS = kQ1Rows, int NBUF = 2>
 struct Q1 {
   static constexpr int S = DIM == 3 ? 27 : 9;   // stencil neighbours
   static constexpr int NC = 1 << DIM;           // cells around a node = nodes of a cell
-  static constexpr int BUF = kQ1Rows * S + 2;   // doubles per staging buffer (even)
-  static constexpr int TAB = 2 * NC * NC + NC + (NC & 1) + 4;   // Khat, Mhat, Fhat, warp sums
-  static constexpr size_t SMEM = sizeof(double) * (TAB + 2 * BUF);
+  static constexpr int BUF = ROWS * S + 2;      // doubles per staging buffer (even)
+  static constexpr int HEAD = 8 + 72;           // warp sums, mass table
+  static constexpr size_t SMEM = sizeof(double) * (HEAD + NBUF * BUF);
 };
 
-template <int DIM, bool FN, bool UD>
-__global__ void __launch_bounds__(kQ1Rows)
-k_numeric_q1(Geom g, int64_t nrows, int64_t nchunks, const int64_t* __restrict__ rowptr,
+// Launch shapes the autotuner chooses from: rows per chunk (= threads per CTA) and
+// staging buffers per CTA (2 overlaps a chunk's bulk store with the next chunk; 1
+// halves shared memory so twice as many CTAs fit on an SM).
+struct Q1Shape {
+  int rows, nbuf;
+};
+constexpr Q1Shape kQ1Shapes[] = {{128, 2}, {128, 1}, {64, 2}, {64, 1}, {256, 1}};
+constexpr int kNumQ1Shapes = 5;
+
+// Element-matrix classes of an axis-aligned Q1 cell.  With exact (degree >= 2)
+// quadrature, K_e[i][j] depends only on which coordinates of nodes i and j differ
+// (class bits x=1, y=2, z=4), and so does M_e; the load int(phi_i) is the same for
+// every node.  So the value of the entry (X, X+o) is K[class(o)] * (sum of kappa over
+// the valid cells that hold both nodes).
+struct Q1Const {
+  double Kc[8];        // stiffness per class
+  double Mtab[8][9];   // mass per class times the number of valid shared cells
+  double btab[9];      // f * load per node times the number of valid cells
+  double ratio;        // Kc[0] / Kc[3] (cube mode)
+  int kzero[8];        // class whose stiffness vanishes exactly in exact arithmetic
+};
+
+// The kappa of a cell is a finite positive double: checked on the bits (integer pipe).
+__device__ __forceinline__ bool bad_coefficient(double k) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(k);
+  return (b >> 63) != 0ull || ((b >> 52) & 0x7FFull) == 0x7FFull || b == 0ull;
+}
+
+// Cube cells: w_c = Kc[3] * kappa_c once per cell (validated here), so a 3D row needs
+// 12 adds for the face diagonals, 3 adds + 1 multiply for the diagonal, and nothing
+// for the corners (w itself) and the edge neighbours (exactly 0 on a cube).
+__global__ void k_prescale(int64_t ncells, const double* __restrict__ kappa, double scale, double* __restrict__ w,
+                           int32_t* __restrict__ bad) {
+  int nbad = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += (int64_t)gridDim.x * blockDim.x) {
+    const double k = kappa[i];
+    nbad += bad_coefficient(k);
+    w[i] = scale * k;
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+// values of one row in canonical neighbour order (offsets lexicographic, x fastest)
+template <int DIM, bool CUBE>
+__device__ __forceinline__ void q1_row_values(const double* kap, const Q1Const& q, double* v) {
+  if (CUBE) {   // DIM == 3; kap holds w = Kc[3] * kappa
+    double P[4];
+#pragma unroll
+    for (int a = 0; a < 4; ++a) P[a] = kap[a] + kap[a + 4];   // z pairs at (a0, a1)
+#pragma unroll
+    for (int s = 0; s < 27; ++s) {
+      const int o0 = s % 3 - 1, o1 = (s / 3) % 3 - 1, o2 = s / 9 - 1;
+      const int nz = (o0 != 0) + (o1 != 0) + (o2 != 0);
+      const int a0 = (o0 + 1) >> 1, a1 = (o1 + 1) >> 1, a2 = (o2 + 1) >> 1;
+      if (nz == 0) {
+        v[s] = q.ratio * ((P[0] + P[1]) + (P[2] + P[3]));
+      } else if (nz == 1) {
+        v[s] = 0.0;
+      } else if (nz == 3) {
+        v[s] = kap[a0 + 2 * a1 + 4 * a2];
+      } else if (o2 == 0) {
+        v[s] = P[a0 + 2 * a1];
+      } else if (o1 == 0) {
+        v[s] = kap[a0 + 4 * a2] + kap[a0 + 2 + 4 * a2];
+      } else {
+        v[s] = kap[2 * a1 + 4 * a2] + kap[1 + 2 * a1 + 4 * a2];
+      }
+    }
+    return;
+  }
+  // general axis-aligned box: subset sums by a separable tree (x, then y, then z)
+  // sx[ch][a1][a2]: ch 0 -> cell a0=0, 1 -> a0=1, 2 -> both
+  constexpr int NZ = DIM == 3 ? 2 : 1;
+  double sx[3][2][NZ];
+#pragma unroll
+  for (int a1 = 0; a1 < 2; ++a1)
+#pragma unroll
+    for (int a2 = 0; a2 < NZ; ++a2) {
+      const double k0 = kap[2 * a1 + 4 * a2], k1 = kap[1 + 2 * a1 + 4 * a2];
+      sx[0][a1][a2] = k0;
+      sx[1][a1][a2] = k1;
+      sx[2][a1][a2] = k0 + k1;
+    }
+  double sxy[3][3][NZ];
+#pragma unroll
+  for (int cx = 0; cx < 3; ++cx)
+#pragma unroll
+    for (int a2 = 0; a2 < NZ; ++a2) {
+      sxy[cx][0][a2] = sx[cx][0][a2];
+      sxy[cx][1][a2] = sx[cx][1][a2];
+      sxy[cx][2][a2] = sx[cx][0][a2] + sx[cx][1][a2];
+    }
+#pragma unroll
+  for (int s = 0; s < Q1<DIM>::S; ++s) {
+    const int o0 = s % 3 - 1, o1 = (s / 3) % 3 - 1, o2 = DIM == 3 ? s / 9 - 1 : 0;
+    const int c0 = o0 == 0 ? 2 : (o0 + 1) >> 1, c1 = o1 == 0 ? 2 : (o1 + 1) >> 1;
+    double S;
+    if (DIM == 2) {
+      S = sxy[c0][c1][0];
+    } else {
+      const int c2 = o2 == 0 ? 2 : (o2 + 1) >> 1;
+      S = c2 == 2 ? sxy[c0][c1][0] + sxy[c0][c1][NZ - 1] : sxy[c0][c1][c2 == 2 ? 0 : c2];
+    }
+    const int cls = (o0 != 0) | ((o1 != 0) << 1) | ((o2 != 0) << 2);
+    v[s] = q.kzero[cls] ? 0.0 : q.Kc[cls] * S;
+  }
+}
+
+// Per-row inputs of one chunk, loaded one chunk ahead (software pipeline): the
+// row ids are fetched two chunks ahead, the coefficients and pattern one chunk ahead,
+// so their latency overlaps the staging and bulk store of the current chunk.
+template <int DIM>
+struct Q1Row {
+  int64_t X[3];
+  uint32_t pw[8];
+  double kap[1 << DIM];
+  int ncell;
+  uint32_t cmask;   // cells inside the mesh
+  bool valid;
+};
+
+template <int DIM, bool CUBE>
+__device__ __forceinline__ void q1_load_row(const Geom& g, int64_t r, int64_t nrows, uint32_t lin, uint32_t pid,
+                                            const uint8_t* __restrict__ pat, const double* __restrict__ kappa,
+                                            Q1Row<DIM>& R) {
+  constexpr int NC = 1 << DIM;
+  R.valid = r < nrows;
+  R.ncell = 0;
+  R.cmask = 0;
+  if (!R.valid) {
+    for (int i = 0; i < 8; ++i) R.pw[i] = 0xFFFFFFFFu;
+    R.pw[7] = 0x00FFFFFFu;   // length 0
+    return;
+  }
+  const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
+  R.X[0] = lin % N0;
+  if (DIM == 3) {
+    const uint32_t t = lin / N0;
+    R.X[1] = t % N1;
+    R.X[2] = t / N1;
+  } else {
+    R.X[1] = lin / N0;
+    R.X[2] = 0;
+  }
+  const uint4* pp = reinterpret_cast<const uint4*>(pat + (int64_t)pid * 32);
+  const uint4 p0 = __ldg(pp), p1 = __ldg(pp + 1);
+  R.pw[0] = p0.x; R.pw[1] = p0.y; R.pw[2] = p0.z; R.pw[3] = p0.w;
+  R.pw[4] = p1.x; R.pw[5] = p1.y; R.pw[6] = p1.z; R.pw[7] = p1.w;
+  const int64_t n0 = g.n[0], n1 = g.n[1], n2 = DIM == 3 ? g.n[2] : 1;
+#pragma unroll
+  for (int a = 0; a < NC; ++a) {
+    const int64_t cx = R.X[0] - 1 + (a & 1), cy = R.X[1] - 1 + ((a >> 1) & 1);
+    const int64_t cz = DIM == 3 ? R.X[2] - 1 + ((a >> 2) & 1) : 0;
+    const bool cin = cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && (DIM == 2 || (cz >= 0 && cz < n2));
+    R.kap[a] = cin ? __ldg(kappa + cx + n0 * (cy + n1 * cz)) : 0.0;
+    R.ncell += cin;
+    R.cmask |= (uint32_t)cin << a;
+  }
+}
+
+template <int DIM, bool CUBE, bool FN, bool UD, int ROWS, int NBUF>
+__global__ void __launch_bounds__(ROWS)
+k_numeric_q1(Geom g, Q1Const q, int64_t nrows, int64_t nchunks, const int64_t* __restrict__ rowptr,
              const int32_t* __restrict__ row_node, const uint16_t* __restrict__ row_pat,
-             const uint8_t* __restrict__ pat, const double* __restrict__ kappa, const double* __restrict__ Khat,
-             const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
-             const double* __restrict__ f_nodal, const double* __restrict__ u_dir, double* __restrict__ vals,
-             double* __restrict__ rhs, int32_t* __restrict__ bad) {
-  using Q = Q1<DIM>;
+             const uint8_t* __restrict__ pat, const double* __restrict__ kappa, const double* __restrict__ f_nodal,
+             const double* __restrict__ u_dir, double* __restrict__ vals, double* __restrict__ rhs,
+             int32_t* __restrict__ bad) {
+  using Q = Q1<DIM, ROWS, NBUF>;
   constexpr int S = Q::S, NC = Q::NC;
   extern __shared__ __align__(128) double smem[];
-  double* sK = smem;
-  double* sM = sK + NC * NC;
-  double* sF = sM + NC * NC;
-  int* s_wsum = (int*)(sF + NC + (NC & 1));
-  double* buf0 = smem + Q::TAB;
-  double* buf1 = buf0 + Q::BUF;
+  int* s_wsum = (int*)smem;
+  double* s_mtab = smem + 8;   // mass per class and shared-cell count (kernel parameters
+                               // are not indexed dynamically: that would go to local memory)
+  double* buf0 = smem + Q::HEAD;
+  double* buf1 = NBUF == 2 ? buf0 + Q::BUF : buf0;
   const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-  for (int i = tid; i < NC * NC; i += blockDim.x) {
-    sK[i] = Khat[i];
-    sM[i] = Mhat[i];
-  }
-  if (tid < NC) sF[tid] = Fhat[tid];
-  __syncthreads();
-  const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
-  const int64_t n0 = g.n[0], n1 = g.n[1], n2 = DIM == 3 ? g.n[2] : 1;
+  if (FN)
+    for (int i = tid; i < 72; i += blockDim.x) s_mtab[i] = q.Mtab[i / 9][i % 9];
+  if (FN) __syncthreads();
+  const int64_t G = gridDim.x;
   int nbad = 0;
   int b = 0;
-  for (int64_t c = blockIdx.x; c < nchunks; c += gridDim.x) {
-    const int64_t r0 = c * kQ1Rows;
-    const int64_t r = r0 + tid;
-    const bool valid = r < nrows;
-    double v[S];
-    uint32_t pw[8];
-    int len = 0;
-    if (valid) {
-      const uint32_t lin = (uint32_t)row_node[r];
-      int64_t X[3];
-      X[0] = lin % N0;
-      if (DIM == 3) {
-        const uint32_t t = lin / N0;
-        X[1] = t % N1;
-        X[2] = t / N1;
-      } else {
-        X[1] = lin / N0;
-        X[2] = 0;
-      }
-      const uint4* pp = reinterpret_cast<const uint4*>(pat + (int64_t)row_pat[r] * 32);
-      const uint4 p0 = __ldg(pp), p1 = __ldg(pp + 1);
-      pw[0] = p0.x; pw[1] = p0.y; pw[2] = p0.z; pw[3] = p0.w;
-      pw[4] = p1.x; pw[5] = p1.y; pw[6] = p1.z; pw[7] = p1.w;
-      len = (int)(pw[7] >> 24);
-      // kappa of the cells around X; slot a: cell X - 1 + bit_d(a) per direction
-      double kap[NC];
-      bool cin[NC];
-#pragma unroll
-      for (int a = 0; a < NC; ++a) {
-        const int64_t cx = X[0] - 1 + (a & 1), cy = X[1] - 1 + ((a >> 1) & 1);
-        const int64_t cz = DIM == 3 ? X[2] - 1 + ((a >> 2) & 1) : 0;
-        cin[a] = cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && (DIM == 2 || (cz >= 0 && cz < n2));
-        kap[a] = cin[a] ? __ldg(kappa + cx + n0 * (cy + n1 * cz)) : 0.0;
-        if (cin[a] && !(kap[a] > 0.0 && kap[a] < INFINITY)) ++nbad;
-      }
-      double bval = 0.0;
-#pragma unroll
-      for (int a = 0; a < NC; ++a)
-        if (cin[a]) bval += f_const * sF[(NC - 1) - a];   // local index of X in slot a is (1-bit_d(a))
-#pragma unroll
-      for (int s = 0; s < S; ++s) {
-        const int o0 = s % 3 - 1, o1 = (s / 3) % 3 - 1, o2 = DIM == 3 ? s / 9 - 1 : 0;
-        double acc = 0.0, macc = 0.0;
-#pragma unroll
-        for (int a = 0; a < NC; ++a) {
-          const int a0 = a & 1, a1 = (a >> 1) & 1, a2 = DIM == 3 ? (a >> 2) & 1 : 0;
-          const bool ok = (o0 == 0 || (o0 < 0) == (a0 == 0)) && (o1 == 0 || (o1 < 0) == (a1 == 0)) &&
-                          (DIM == 2 || o2 == 0 || (o2 < 0) == (a2 == 0));
-          if (ok) {
-            const int lx = (1 - a0) + 2 * (1 - a1) + (DIM == 3 ? 4 * (1 - a2) : 0);
-            const int ly = (1 - a0 + o0) + 2 * (1 - a1 + o1) + (DIM == 3 ? 4 * (1 - a2 + o2) : 0);
-            acc += kap[a] * sK[lx * NC + ly];
-            if (FN && cin[a]) macc += sM[lx * NC + ly];
-          }
-        }
-        v[s] = acc;
-        if (FN || UD) {
-          const int64_t Y0 = X[0] + o0, Y1 = X[1] + o1, Y2 = X[2] + o2;
-          const bool in = Y0 >= 0 && Y0 < g.N[0] && Y1 >= 0 && Y1 < g.N[1] && (DIM == 2 || (Y2 >= 0 && Y2 < g.N[2]));
-          if (in) {
-            const int64_t ylin = Y0 + g.N[0] * (Y1 + g.N[1] * Y2);
-            if (FN) bval += macc * __ldg(f_nodal + ylin);
-            if (UD) {
-              const int64_t Yv[3] = {Y0, Y1, Y2};
-              if (node_is_dirichlet(g, Yv)) bval -= acc * __ldg(u_dir + ylin);
-            }
-          }
-        }
-      }
-      rhs[r] = bval;
+  // pipeline prologue: data of the first chunk, ids of the second
+  int64_t c = blockIdx.x;
+  Q1Row<DIM> cur;
+  int64_t e0_cur = c < nchunks ? rowptr[c * ROWS] : 0;
+  {
+    const int64_t r = c * ROWS + tid;
+    const bool ok = c < nchunks && r < nrows;
+    const uint32_t lin = ok ? (uint32_t)row_node[r] : 0u;
+    const uint32_t pid = ok ? (uint32_t)row_pat[r] : 0u;
+    q1_load_row<DIM, CUBE>(g, ok ? r : nrows, nrows, lin, pid, pat, kappa, cur);
+  }
+  uint32_t nlin = 0, npid = 0;
+  int64_t e0_next = c + G < nchunks ? rowptr[(c + G) * ROWS] : 0;
+  {
+    const int64_t r = (c + G) * ROWS + tid;
+    if (c + G < nchunks && r < nrows) {
+      nlin = (uint32_t)row_node[r];
+      npid = (uint32_t)row_pat[r];
     }
+  }
+  for (; c < nchunks; c += G) {
+    const int64_t r0 = c * ROWS;
+    const int64_t r = r0 + tid;
+    const int len = (int)(cur.pw[7] >> 24);
     // block-wide exclusive scan of the row lengths
     int incl = len;
 #pragma unroll
@@ -462,69 +570,196 @@ k_numeric_q1(Geom g, int64_t nrows, int64_t nchunks, const int64_t* __restrict__
       const int y = __shfl_up_sync(0xffffffffu, incl, o);
       if (lane >= o) incl += y;
     }
-    if (tid == 0) bulk_wait_read<1>();   // the store that last read this buffer is done
+    if (tid == 0) bulk_wait_read<NBUF - 1>();   // the store that last read this buffer is done
     __syncthreads();
     if (lane == 31) s_wsum[wid] = incl;
     __syncthreads();
     int woff = 0, total = 0;
 #pragma unroll
-    for (int w = 0; w < kQ1Rows / 32; ++w) {
+    for (int w = 0; w < ROWS / 32; ++w) {
       const int t = s_wsum[w];
       woff += w < wid ? t : 0;
       total += t;
     }
     const int off = woff + incl - len;
-    const int64_t e0 = rowptr[r0];
+    const int64_t e0 = e0_cur;
     const int ofs = (int)(e0 & 1);   // keeps shared and global addresses congruent mod 16 bytes
     double* buf = b ? buf1 : buf0;
-    if (valid) {
+    if (cur.valid) {
+      if (!CUBE)
+#pragma unroll
+        for (int a = 0; a < NC; ++a) nbad += ((cur.cmask >> a) & 1u) && bad_coefficient(cur.kap[a]);
+      double v[S];
+      q1_row_values<DIM, CUBE>(cur.kap, q, v);
+      double* dst = buf + ofs + off;
 #pragma unroll
       for (int s = 0; s < S; ++s) {
-        const uint32_t pos = (pw[s >> 2] >> (8 * (s & 3))) & 0xFFu;
-        if (pos != 0xFFu) buf[ofs + off + (int)pos] = v[s];
+        const uint32_t pos = (cur.pw[s >> 2] >> (8 * (s & 3))) & 0xFFu;
+        if (pos != 0xFFu) dst[pos] = v[s];
+      }
+      double bval = 0.0;
+      if (!FN) {
+#pragma unroll
+        for (int n = 0; n <= NC; ++n) bval = cur.ncell == n ? q.btab[n] : bval;
+      }
+      if (FN || UD) {
+        const int64_t n0 = g.n[0], n1 = g.n[1], n2 = DIM == 3 ? g.n[2] : 1;
+#pragma unroll
+        for (int s = 0; s < S; ++s) {
+          const int o0 = s % 3 - 1, o1 = (s / 3) % 3 - 1, o2 = DIM == 3 ? s / 9 - 1 : 0;
+          const int64_t Y0 = cur.X[0] + o0, Y1 = cur.X[1] + o1, Y2 = cur.X[2] + o2;
+          const bool in = Y0 >= 0 && Y0 < g.N[0] && Y1 >= 0 && Y1 < g.N[1] && (DIM == 2 || (Y2 >= 0 && Y2 < g.N[2]));
+          if (!in) continue;
+          const int64_t ylin = Y0 + g.N[0] * (Y1 + g.N[1] * Y2);
+          if (FN) {   // number of valid cells shared by X and Y
+            int cnt = 0;
+#pragma unroll
+            for (int a = 0; a < NC; ++a) {
+              const int a0 = a & 1, a1 = (a >> 1) & 1, a2 = (a >> 2) & 1;
+              const bool sh = (o0 == 0 || (o0 < 0) == (a0 == 0)) && (o1 == 0 || (o1 < 0) == (a1 == 0)) &&
+                              (DIM == 2 || o2 == 0 || (o2 < 0) == (a2 == 0));
+              const int64_t cx = cur.X[0] - 1 + a0, cy = cur.X[1] - 1 + a1, cz = DIM == 3 ? cur.X[2] - 1 + a2 : 0;
+              cnt += sh && cx >= 0 && cx < n0 && cy >= 0 && cy < n1 && (DIM == 2 || (cz >= 0 && cz < n2));
+            }
+            const int cls = (o0 != 0) | ((o1 != 0) << 1) | ((o2 != 0) << 2);
+            bval += s_mtab[cls * 9 + cnt] * __ldg(f_nodal + ylin);
+          }
+          if (UD && Y0 >= 0) {
+            const bool dir = (g.dsides[0] && Y0 == 0) || (g.dsides[1] && Y0 == g.N[0] - 1) ||
+                             (g.dsides[2] && Y1 == 0) || (g.dsides[3] && Y1 == g.N[1] - 1) ||
+                             (DIM == 3 && ((g.dsides[4] && Y2 == 0) || (g.dsides[5] && Y2 == g.N[2] - 1)));
+            if (dir) bval -= v[s] * __ldg(u_dir + ylin);
+          }
+        }
+      }
+      rhs[r] = bval;
+    }
+    // prefetch: data of the next chunk (its ids arrived one iteration ago), ids of the one after
+    {
+      const int64_t cn = c + G;
+      const int64_t rn = cn * ROWS + tid;
+      const bool okn = cn < nchunks && rn < nrows;
+      q1_load_row<DIM, CUBE>(g, okn ? rn : nrows, nrows, nlin, npid, pat, kappa, cur);
+      e0_cur = e0_next;
+      e0_next = c + 2 * G < nchunks ? rowptr[(c + 2 * G) * ROWS] : 0;
+      const int64_t r2 = (c + 2 * G) * ROWS + tid;
+      nlin = 0;
+      npid = 0;
+      if (c + 2 * G < nchunks && r2 < nrows) {
+        nlin = (uint32_t)row_node[r2];
+        npid = (uint32_t)row_pat[r2];
       }
     }
     fence_proxy_async_smem();
     __syncthreads();
     if (tid == 0 && total > 0) {
       const int64_t e1 = e0 + total;
-      if (ofs) vals[e0] = buf[1];                                   // unaligned head
+      if (ofs) vals[e0] = buf[1];                                          // unaligned head
       const int64_t ja = e0 + ofs, jb = e1 - (e1 & 1);
       if ((e1 & 1) && e1 - 1 >= ja) vals[e1 - 1] = buf[ofs + total - 1];   // unaligned tail
       if (jb > ja) bulk_store_s2g(vals + ja, buf + ofs + (ja - e0), (uint32_t)((jb - ja) * sizeof(double)));
     }
     if (tid == 0) bulk_commit();
-    b ^= 1;
+    if (NBUF == 2) b ^= 1;
   }
   if (tid == 0) bulk_wait_all<0>();
   if (nbad) atomicAdd(bad, nbad);
 }
 
-template <int DIM, bool FN, bool UD>
-static int launch_q1_inst(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, const double* udir,
-                          int32_t* bad, cudaStream_t st) {
-  using Q = Q1<DIM>;
+// Class constants from the device reference element (lexicographic local nodes).
+static int q1_constants(gd_asm* A, double f_const, Q1Const& q, bool& cube) {
+  const Geom& g = A->test->geom;
+  cudaStream_t st = A->test->model->ctx->stream;
+  const int NC = 1 << g.dim;
+  if (A->q1c_degree == A->ref_degree) {   // cached for this reference element
+    q = *reinterpret_cast<const Q1Const*>(A->q1c_blob.data());
+    for (int n = 0; n <= 8; ++n) q.btab[n] = f_const * A->q1c_f0 * n;
+    cube = A->q1c_cube;
+    return GD_OK;
+  }
+  std::vector<double> K(NC * NC), M(NC * NC), F(NC);
+  GD_CUDA_TRY(cudaMemcpyAsync(K.data(), A->Khat.p, sizeof(double) * NC * NC, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(M.data(), A->Mhat.p, sizeof(double) * NC * NC, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(F.data(), A->Fhat.p, sizeof(double) * NC, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  memset(&q, 0, sizeof(q));
+  // node 0 is (0,0,0); node cls has the coordinate bits of the class
+  for (int cls = 0; cls < 8; ++cls) {
+    if (cls >= NC) continue;
+    q.Kc[cls] = K[0 * NC + cls];
+    for (int n = 0; n <= 8; ++n) q.Mtab[cls][n] = M[0 * NC + cls] * n;
+  }
+  for (int n = 0; n <= 8; ++n) q.btab[n] = f_const * F[0] * n;
+  const double k0 = std::fabs(q.Kc[0]);
+  // the class rule holds only if every entry equals its class representative
+  bool classes_ok = true;
+  for (int i = 0; i < NC; ++i)
+    for (int j = 0; j < NC; ++j) {
+      const int cls = (i ^ j);
+      if (std::fabs(K[i * NC + j] - q.Kc[cls]) > 1e-14 * k0 || std::fabs(M[i * NC + j] - M[cls]) > 1e-14 * std::fabs(M[0]))
+        classes_ok = false;
+    }
+  for (int i = 0; i < NC; ++i)
+    if (std::fabs(F[i] - F[0]) > 1e-14 * std::fabs(F[0])) classes_ok = false;
+  if (!classes_ok) return fail(GD_ERR_UNSUPPORTED, "Q1 element matrix does not have the box-cell class structure");
+  for (int cls = 0; cls < NC; ++cls) q.kzero[cls] = std::fabs(q.Kc[cls]) <= 1e-14 * k0;
+  cube = g.dim == 3 && q.kzero[1] && q.kzero[2] && q.kzero[4] &&
+         std::fabs(q.Kc[3] - q.Kc[7]) <= 1e-14 * k0 && std::fabs(q.Kc[5] - q.Kc[7]) <= 1e-14 * k0 &&
+         std::fabs(q.Kc[6] - q.Kc[7]) <= 1e-14 * k0 && q.Kc[3] != 0.0;
+  q.ratio = cube ? q.Kc[0] / q.Kc[3] : 0.0;
+  A->q1c_blob.assign(reinterpret_cast<const char*>(&q), reinterpret_cast<const char*>(&q) + sizeof(q));
+  A->q1c_f0 = F[0];
+  A->q1c_cube = cube;
+  A->q1c_degree = A->ref_degree;
+  return GD_OK;
+}
+
+template <int DIM, bool CUBE, bool FN, bool UD, int ROWS, int NBUF>
+static int launch_q1_inst(gd_asm* A, const Q1Const& q, const double* kappa, const double* f_nodal,
+                          const double* udir, int32_t* bad, cudaStream_t st) {
+  using Q = Q1<DIM, ROWS, NBUF>;
   static int blocks_per_sm = -1;
   static int num_sms = 0;
-  auto kern = k_numeric_q1<DIM, FN, UD>;
+  auto kern = k_numeric_q1<DIM, CUBE, FN, UD, ROWS, NBUF>;
   if (blocks_per_sm < 0) {
     GD_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Q::SMEM));
-    GD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, kQ1Rows, Q::SMEM));
+    GD_CUDA_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&blocks_per_sm, kern, ROWS, Q::SMEM));
     int dev = 0;
     GD_CUDA_TRY(cudaGetDevice(&dev));
     GD_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
   const int64_t n = A->ngdofs;
-  const int64_t nchunks = (n + kQ1Rows - 1) / kQ1Rows;
-  int64_t grid = (int64_t)blocks_per_sm * num_sms;
+  const int64_t nchunks = (n + ROWS - 1) / ROWS;
+  int64_t grid = (int64_t)blocks_per_sm * num_sms;   // persistent: one wave of resident CTAs
   if (grid > nchunks) grid = nchunks;
   A->q1_grid = (int)grid;
-  kern<<<(unsigned)grid, kQ1Rows, Q::SMEM, st>>>(A->test->geom, n, nchunks, A->rowptr.p, A->row_node.p,
-                                                  A->row_pat.p, A->pat.p, kappa, A->Khat.p, A->Mhat.p, A->Fhat.p,
-                                                  f_const, f_nodal, udir, A->vals.p, A->rhs.p, bad);
+  kern<<<(unsigned)grid, ROWS, Q::SMEM, st>>>(A->test->geom, q, n, nchunks, A->rowptr.p, A->row_node.p,
+                                               A->row_pat.p, A->pat.p, kappa, f_nodal, udir, A->vals.p, A->rhs.p,
+                                               bad);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
+}
+
+template <int DIM, bool CUBE, bool FN, bool UD>
+static int launch_q1_shape(gd_asm* A, int shape, const Q1Const& q, const double* kappa, const double* f_nodal,
+                           const double* udir, int32_t* bad, cudaStream_t st) {
+  switch (shape) {
+    case 1: return launch_q1_inst<DIM, CUBE, FN, UD, 128, 1>(A, q, kappa, f_nodal, udir, bad, st);
+    case 2: return launch_q1_inst<DIM, CUBE, FN, UD, 64, 2>(A, q, kappa, f_nodal, udir, bad, st);
+    case 3: return launch_q1_inst<DIM, CUBE, FN, UD, 64, 1>(A, q, kappa, f_nodal, udir, bad, st);
+    case 4: return launch_q1_inst<DIM, CUBE, FN, UD, 256, 1>(A, q, kappa, f_nodal, udir, bad, st);
+    default: return launch_q1_inst<DIM, CUBE, FN, UD, 128, 2>(A, q, kappa, f_nodal, udir, bad, st);
+  }
+}
+
+template <int DIM, bool CUBE>
+static int launch_q1_mode(gd_asm* A, int shape, const Q1Const& q, const double* kappa, const double* f_nodal,
+                          const double* udir, int32_t* bad, cudaStream_t st) {
+  if (f_nodal && udir) return launch_q1_shape<DIM, CUBE, true, true>(A, shape, q, kappa, f_nodal, udir, bad, st);
+  if (f_nodal) return launch_q1_shape<DIM, CUBE, true, false>(A, shape, q, kappa, f_nodal, nullptr, bad, st);
+  if (udir) return launch_q1_shape<DIM, CUBE, false, true>(A, shape, q, kappa, nullptr, udir, bad, st);
+  return launch_q1_shape<DIM, CUBE, false, false>(A, shape, q, kappa, nullptr, nullptr, bad, st);
 }
 
 template <int DIM>
@@ -532,12 +767,53 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
                      cudaStream_t st) {
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
   if (A->ngdofs == 0) return GD_OK;
+  Q1Const q;
+  bool cube = false;
+  GD_TRY(q1_constants(A, f_nodal ? 0.0 : f_const, q, cube));
+  int64_t ncells = 1;
+  for (int d = 0; d < DIM; ++d) ncells *= A->test->geom.n[d];
+  const double* coef = kappa;
+  if (cube) {   // w = Kc[3] * kappa, validated on the way
+    if (A->w_cells.n != (size_t)ncells) GD_TRY(dalloc(A->w_cells, ncells));
+    int blocks = (int)std::min<int64_t>((ncells + 255) / 256, 4096);
+    k_prescale<<<blocks, 256, 0, st>>>(ncells, kappa, q.Kc[3], A->w_cells.p, bad);
+    GD_CUDA_TRY(cudaGetLastError());
+    coef = A->w_cells.p;
+  }
+  // autotune the launch shape once per assembler: time every shape with CUDA events
+  // (each run writes the same values) and keep the fastest
+  if (A->q1_shape < 0) {
+    cudaEvent_t e0, e1;
+    GD_CUDA_TRY(cudaEventCreate(&e0));
+    GD_CUDA_TRY(cudaEventCreate(&e1));
+    float best = 1e30f;
+    int best_shape = 0;
+    for (int sh = 0; sh < kNumQ1Shapes; ++sh) {
+      float ms_sum = 0.f;
+      for (int rep = 0; rep < 3; ++rep) {
+        GD_CUDA_TRY(cudaEventRecord(e0, st));
+        int s2 = cube ? launch_q1_mode<DIM, true>(A, sh, q, coef, f_nodal, udir, bad, st)
+                      : launch_q1_mode<DIM, false>(A, sh, q, coef, f_nodal, udir, bad, st);
+        if (s2 != GD_OK) return s2;
+        GD_CUDA_TRY(cudaEventRecord(e1, st));
+        GD_CUDA_TRY(cudaEventSynchronize(e1));
+        float ms = 0.f;
+        GD_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
+        if (rep > 0) ms_sum += ms;
+      }
+      A->q1_shape_ms[sh] = ms_sum / 2;
+      if (ms_sum < best) {
+        best = ms_sum;
+        best_shape = sh;
+      }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    A->q1_shape = best_shape;
+  }
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
-  int s;
-  if (f_nodal && udir) s = launch_q1_inst<DIM, true, true>(A, kappa, f_nodal, 0.0, udir, bad, st);
-  else if (f_nodal) s = launch_q1_inst<DIM, true, false>(A, kappa, f_nodal, 0.0, nullptr, bad, st);
-  else if (udir) s = launch_q1_inst<DIM, false, true>(A, kappa, nullptr, f_const, udir, bad, st);
-  else s = launch_q1_inst<DIM, false, false>(A, kappa, nullptr, f_const, nullptr, bad, st);
+  int s = cube ? launch_q1_mode<DIM, true>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st)
+               : launch_q1_mode<DIM, false>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st);
   if (s != GD_OK) return s;
   if (A->profiling) {   // one fused kernel: the rhs phase is empty
     GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
@@ -653,13 +929,27 @@ extern "C" int gd_assembler_phase_times(const gd_asm* A, double* ms0, double* ms
   return GD_OK;
 }
 
+extern "C" int gd_assembler_tuning(const gd_asm* A, int32_t* shape, int32_t* rows, int32_t* nbuf, float* ms,
+                                   int32_t* nshapes) {
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_tuning: null assembler");
+  const int sh = A->fast_q1 ? A->q1_shape : -1;
+  if (shape) *shape = sh;
+  if (rows) *rows = sh >= 0 ? gd::kQ1Shapes[sh].rows : 0;
+  if (nbuf) *nbuf = sh >= 0 ? gd::kQ1Shapes[sh].nbuf : 0;
+  if (ms)
+    for (int i = 0; i < gd::kNumQ1Shapes; ++i) ms[i] = A->q1_shape_ms[i];
+  if (nshapes) *nshapes = gd::kNumQ1Shapes;
+  return GD_OK;
+}
+
 extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nnz_owned, int64_t* nnz_total,
                                    int32_t* kernels) {
   if (!A || !A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_counts: run gd_assemble_symbolic first");
   if (ngdofs) *ngdofs = A->ngdofs;
   if (nnz_owned) *nnz_owned = A->nnz_own;
   if (nnz_total) *nnz_total = A->nnz_total;
-  if (kernels) *kernels = A->fast_q1 ? 1 : 2;   // fused Q1 kernel, or k_numeric_matrix + k_numeric_rhs
+  // cube Q1: k_prescale + k_numeric_q1; other Q1: k_numeric_q1; Q_k: k_numeric_matrix + k_numeric_rhs
+  if (kernels) *kernels = A->fast_q1 ? (A->q1c_cube ? 2 : 1) : 2;
   return GD_OK;
 }
 

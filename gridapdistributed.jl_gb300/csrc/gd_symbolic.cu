@@ -611,6 +611,7 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->dinv);
   dfreeb(A->row_pat);
   dfreeb(A->pat);
+  dfreeb(A->w_cells);
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;

@@ -156,6 +156,12 @@ int gd_assembler_phase_times(const gd_asm* a, double* ms_ghost_zero, double* ms_
 int gd_assembler_counts(const gd_asm* a, int64_t* ngdofs, int64_t* nnz_owned, int64_t* nnz_total,
                         int32_t* kernels_per_numeric);
 
+/* Launch shape the autotuner chose for the Q1 numeric kernel on the first numeric
+ * assembly (-1 before it ran, or when the generic kernel is used): index, rows per
+ * chunk, staging buffers, and the measured ms of each of the `nshapes` candidates. */
+int gd_assembler_tuning(const gd_asm* a, int32_t* shape, int32_t* rows, int32_t* nbuf, float* ms_per_shape,
+                        int32_t* nshapes);
+
 /* Sizes of one part's local matrix: rows (owned + ghost), columns (owned + ghost),
  * stored entries, ghost rows, ghost columns. */
 int gd_matrix_sizes(const gd_asm* a, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
