@@ -49,6 +49,7 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-solve", action="store_true")
+    ap.add_argument("--solve-maxit", type=int, default=20000)
     ap.add_argument("--cells", type=int, default=128, help="cells per direction (default: the 128^3 workload)")
     return ap.parse_args()
 
@@ -330,7 +331,7 @@ def run_gb300(args, rank, world, local):
         st = L.gd_solve_stats()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        rc = L.load().gd_solve(assem.handle, L.GD_SOLVE_JACOBI_PCG, 1e-8, 20000, C.c_void_p(x.data_ptr()),
+        rc = L.load().gd_solve(assem.handle, L.GD_SOLVE_JACOBI_PCG, 1e-8, args.solve_maxit, C.c_void_p(x.data_ptr()),
                                L.GD_DEVICE, C.byref(st))
         t_solve = time.perf_counter() - t0
         solve = {"method": "jacobi_pcg_fp64", "rtol": 1e-8, "seconds": t_solve, "iterations": st.iterations,

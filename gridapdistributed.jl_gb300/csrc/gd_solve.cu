@@ -9,6 +9,7 @@
 // deterministic two-stage reductions.
 #include <chrono>
 #include <cmath>
+#include <mutex>
 #include <string>
 
 #include "gd_internal.h"
@@ -338,5 +339,138 @@ extern "C" int gd_fe_function_local(const gd_space* S, int part, const double* x
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   dfreeb(xg);
   dfreeb(xl);
+  return GD_OK;
+}
+
+// ---------------------------------------------------------------------------------
+// Allocation-free solve
+//
+// Some callers of this library cannot allocate device memory while they run: an
+// application whose device memory is owned by its own pool allocator (every byte
+// reserved up front, so a cudaMalloc behind its back fails or evicts), or a control
+// or time-stepping loop in which a cudaMalloc -- which may synchronise the whole
+// device, or fail part-way through a run -- is not acceptable.  gd_solve allocates
+// its Jacobi-PCG workspace on first use; gd_solve_noalloc runs the same iteration
+// with every scratch vector, partial sum and scalar in one file-scope device array
+// instead, so it calls no cudaMalloc/cudaFree at all.
+//
+// Limits and rules (also stated in gdgpu.h):
+//  * at most kNoAllocMaxDofs global DOFs; larger systems are rejected with GD_ERR_ARG;
+//  * the array (about 12.6 MB) is held by every device that loads the library, until
+//    the process exits;
+//  * the first call on a device looks the array's device address up
+//    (cudaGetSymbolAddress) with that device current; make that first call before
+//    any stream capture;
+//  * every call shares the one array and it keeps the last call's contents: each call
+//    clears what must start at zero, and calls that overlap on the GPU (other streams,
+//    other host threads) race on it.
+// ---------------------------------------------------------------------------------
+namespace gd {
+
+constexpr int64_t kNoAllocMaxDofs = (int64_t)1 << 18;   // 262,144 global DOFs
+constexpr int64_t kNoAllocDoubles = 6 * kNoAllocMaxDofs + 2 * kMaxPartials + 64;
+
+static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
+
+// Device address of the scratch array for the current device (looked up once per device).
+static int noalloc_scratch(double** out) {
+  int dev = 0;
+  GD_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(GD_ERR_UNSUPPORTED, "gd_solve_noalloc: device index too large");
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  if (!g_noalloc_ptr[dev]) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p)
+      return fail(GD_ERR_CUDA, std::string("gd_solve_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+    g_noalloc_ptr[dev] = static_cast<double*>(p);
+  }
+  *out = g_noalloc_ptr[dev];
+  return GD_OK;
+}
+
+}  // namespace gd
+
+extern "C" int gd_solve_noalloc(gd_asm* A, double rtol, int maxit, double* x, int where, gd_solve_stats* stats) {
+  GD_TRY(check_ready(A, "gd_solve_noalloc"));
+  if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve_noalloc: bad argument");
+  const int64_t n = A->ngdofs;
+  if (n > kNoAllocMaxDofs)
+    return fail(GD_ERR_ARG, "gd_solve_noalloc: " + std::to_string(n) + " DOFs exceed the static scratch limit of " +
+                                std::to_string(kNoAllocMaxDofs) + " (use gd_solve)");
+  GD_CUDA_TRY(cudaSetDevice(A->test->model->ctx->device));
+  double* base = nullptr;
+  GD_TRY(noalloc_scratch(&base));
+  cudaStream_t st = A->test->model->ctx->stream;
+  auto t0 = std::chrono::steady_clock::now();
+  double* dx = base;
+  double* dr = base + 1 * kNoAllocMaxDofs;
+  double* dz = base + 2 * kNoAllocMaxDofs;
+  double* dp = base + 3 * kNoAllocMaxDofs;
+  double* dq = base + 4 * kNoAllocMaxDofs;
+  double* dinv = base + 5 * kNoAllocMaxDofs;
+  double* pa = base + 6 * kNoAllocMaxDofs;
+  double* pb = pa + kMaxPartials;
+  Scalars* sc = reinterpret_cast<Scalars*>(pb + kMaxPartials);
+  int32_t* bad = reinterpret_cast<int32_t*>(pb + kMaxPartials + 16);
+  // the array keeps the previous call's contents: clear what must start at zero
+  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
+  GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
+  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dinv, bad);
+  GD_CUDA_TRY(cudaGetLastError());
+  const int gs = grid_for(n, kRowsPerSpmvBlock);
+  const int gv = grid_for(n, kVecThreads);
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, dr, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);
+  GD_CUDA_TRY(cudaGetLastError());
+  Scalars h{};
+  int32_t hbad = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hbad) return fail(GD_ERR_NUMERIC, "gd_solve_noalloc: non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
+  const double bnorm = std::sqrt(h.rz);
+  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
+  GD_CUDA_TRY(cudaGetLastError());
+  int it = 0;
+  bool conv = bnorm == 0.0;
+  const int check_every = 8;
+  while (!conv && it < maxit) {
+    const int nstep = std::min(check_every, maxit - it);
+    for (int s = 0; s < nstep; ++s) {
+      k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
+      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
+      k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, dinv, pa, pb);
+      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
+      k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
+    }
+    GD_CUDA_TRY(cudaGetLastError());
+    it += nstep;
+    GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+    if (!std::isfinite(h.rr)) break;
+    if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
+  }
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, nullptr, pa, pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(x, dx, sizeof(double) * n,
+                              where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  const double rel = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
+  if (stats) {
+    stats->iterations = it;
+    stats->converged = rel <= rtol;
+    stats->rel_residual = rel;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, "gd_solve_noalloc: residual is not finite");
+  if (rel > rtol) return fail(GD_ERR_NOTCONVERGED, "gd_solve_noalloc: tolerance not reached in " + std::to_string(it) + " iterations");
   return GD_OK;
 }

@@ -85,6 +85,7 @@ SIGNATURES = {
     "gd_spmv": [P, P, P, C.c_int],
     "gd_solve": [P, C.c_int, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_fe_function_local": [P, C.c_int, P, C.c_int, DP],
+    "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
 }
 _RESTYPES = {"gd_last_error": C.c_char_p, "gd_version": C.c_char_p}
 

@@ -197,6 +197,17 @@ typedef struct gd_solve_stats {
  * relative residual rtol.  x: global vector (ngdofs). */
 int gd_solve(gd_asm* a, int method, double rtol, int maxit, double* x, int where,
              gd_solve_stats* stats);
+/* gd_solve without device allocation.  No counterpart in the reference: for callers
+ * that cannot allocate device memory while they run (an application whose device
+ * memory belongs to its own pool allocator, or a loop where a cudaMalloc -- which can
+ * synchronise the device or fail mid-run -- is not acceptable).  Same Jacobi-PCG and
+ * arguments as gd_solve; all scratch lives in one file-scope device array of fixed size
+ * (about 12.6 MB per device that loads the library, held until the process exits).
+ * At most 262,144 global DOFs: larger systems return GD_ERR_ARG.  The first call on a
+ * device looks up the array's address with that device current: make it before any
+ * stream capture.  Every call shares the array and clears what must start at zero;
+ * calls that overlap on the GPU race on it. */
+int gd_solve_noalloc(gd_asm* a, double rtol, int maxit, double* x, int where, gd_solve_stats* stats);
 /* FEFunction(U, x) / consistent!: the local (owned+ghost) free values of one part
  * from a global vector (FESpaces.jl:354-371, Algebra.jl:270-293). */
 int gd_fe_function_local(const gd_space* space, int part, const double* x_global, int where,
