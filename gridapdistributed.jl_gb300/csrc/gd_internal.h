@@ -160,6 +160,24 @@ int exclusive_scan_i32(const int32_t* in, int64_t* out, int64_t n, cudaStream_t 
 
 }  // namespace gd
 
+namespace gd {
+// Workspace of the mixed-precision solver (gd_solve_mixed.cu).
+struct MixedState {
+  bool ready = false;
+  bool matrix_free = false;
+  int64_t numeric_epoch = -1;
+  float ratio = 0.f;
+  int last_outer = 0;
+  DBuf<float> f32;        // x r z p q dinv (FP32, 6 n)
+  DBuf<double> f64;       // x r (FP64, 2 n)
+  DBuf<double> red;       // block partials + scalars
+  DBuf<int32_t> node_gid; // lattice node -> gid (-1 Dirichlet)
+  DBuf<float> wf;         // prescaled cell coefficients (FP32)
+  DBuf<float> vals32;     // FP32 copy of the owned-row values (non-cube spaces)
+  DBuf<float> zold;       // previous preconditioned residual (flexible CG)
+};
+}  // namespace gd
+
 // ---------------------------------------------------------------------------------
 // Opaque objects of the C ABI
 // ---------------------------------------------------------------------------------
@@ -249,6 +267,10 @@ struct gd_asm {
   // profiling events: start, after ghost zeroing, after matrix, after rhs
   bool profiling = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+  // mixed-precision solver
+  gd::MixedState mx;
+  int64_t numeric_epoch = 0;
+  double mf_ratio = 0.0;
   // solver workspace
   gd::DBuf<double> w;              // vectors
   gd::DBuf<double> dred;           // reduction partials

@@ -770,6 +770,7 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
   Q1Const q;
   bool cube = false;
   GD_TRY(q1_constants(A, f_nodal ? 0.0 : f_const, q, cube));
+  A->mf_ratio = q.ratio;
   int64_t ncells = 1;
   for (int d = 0; d < DIM; ++d) ncells *= A->test->geom.n[d];
   const double* coef = kappa;
@@ -905,6 +906,7 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
                                               " cell visits");
   }
   A->numeric_done = true;
+  ++A->numeric_epoch;
   return GD_OK;
 }
 

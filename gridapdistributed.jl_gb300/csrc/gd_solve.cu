@@ -13,6 +13,7 @@
 #include <string>
 
 #include "gd_internal.h"
+#include "gd_solve_mixed.h"
 
 namespace gd {
 
@@ -238,6 +239,10 @@ extern "C" int gd_spmv(gd_asm* A, const double* x, double* y, int where) {
 
 extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x, int where, gd_solve_stats* stats) {
   GD_TRY(check_ready(A, "gd_solve"));
+  if (method == GD_SOLVE_MIXED_IR) {
+    if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve: bad argument");
+    return mixed_solve(A, rtol, maxit, x, where, stats, nullptr);
+  }
   if (method != GD_SOLVE_JACOBI_PCG) return fail(GD_ERR_UNSUPPORTED, "gd_solve: unknown method");
   if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve: bad argument");
   cudaStream_t st = A->test->model->ctx->stream;

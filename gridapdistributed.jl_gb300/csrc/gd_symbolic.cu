@@ -612,6 +612,13 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->row_pat);
   dfreeb(A->pat);
   dfreeb(A->w_cells);
+  dfreeb(A->mx.f32);
+  dfreeb(A->mx.f64);
+  dfreeb(A->mx.red);
+  dfreeb(A->mx.node_gid);
+  dfreeb(A->mx.wf);
+  dfreeb(A->mx.vals32);
+  dfreeb(A->mx.zold);
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;

@@ -17,6 +17,7 @@ GD_OK = 0
 GD_SUB_ASSEMBLED_ROWS = 0
 GD_FULLY_ASSEMBLED_ROWS = 1
 GD_SOLVE_JACOBI_PCG = 1
+GD_SOLVE_MIXED_IR = 2
 GD_HOST = 0
 GD_DEVICE = 1
 

@@ -451,11 +451,15 @@ class PSparseMatrix:
         L.call("gd_spmv", self.assem.handle, L.vptr(x), L.vptr(y), L.GD_HOST)
         return y
 
-    def solve(self, rtol=1e-12, maxit=100000):
-        """``A \\ b`` for the assembled right-hand side: Jacobi-PCG in FP64."""
+    def solve(self, rtol=1e-12, maxit=100000, method="jacobi_pcg"):
+        """``A \\ b`` for the assembled right-hand side.
+
+        ``method``: "jacobi_pcg" (FP64 Jacobi-PCG) or "mixed_ir" (FP64 iterative
+        refinement around FP32 Jacobi-PCG with FP64 inner products)."""
+        codes = {"jacobi_pcg": L.GD_SOLVE_JACOBI_PCG, "mixed_ir": L.GD_SOLVE_MIXED_IR}
         x = np.zeros(self.n_global)
         st = L.gd_solve_stats()
-        L.call("gd_solve", self.assem.handle, L.GD_SOLVE_JACOBI_PCG, float(rtol), int(maxit), L.vptr(x), L.GD_HOST,
+        L.call("gd_solve", self.assem.handle, codes[method], float(rtol), int(maxit), L.vptr(x), L.GD_HOST,
                C.byref(st))
         self.last_stats = st
         return x

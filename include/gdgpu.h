@@ -53,8 +53,12 @@ enum {
 /* Assembly strategies (src/Algebra.jl:397-398). */
 enum { GD_SUB_ASSEMBLED_ROWS = 0, GD_FULLY_ASSEMBLED_ROWS = 1 };
 
-/* Solver methods behind `\` (the reference's own is a gathered sparse LU). */
-enum { GD_SOLVE_JACOBI_PCG = 1 };
+/* Solver methods behind `\` (the reference's own is a gathered sparse LU).
+ * JACOBI_PCG: FP64 Jacobi-preconditioned CG.
+ * MIXED_IR: FP64 iterative refinement (true residual b - Ax with the assembled FP64
+ *   matrix) around FP32 Jacobi-PCG with FP64 inner products and step lengths; for Q1 on
+ *   cube cells the inner operator is applied matrix-free. */
+enum { GD_SOLVE_JACOBI_PCG = 1, GD_SOLVE_MIXED_IR = 2 };
 
 /* Where a coefficient/input pointer lives. */
 enum { GD_HOST = 0, GD_DEVICE = 1 };

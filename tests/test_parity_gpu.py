@@ -109,6 +109,22 @@ def test_solve_matches_gathered_lu(backend, case):
     assert np.abs(x - x_ref).max() / np.abs(x_ref).max() <= SOL_TOL
 
 
+@pytest.mark.parametrize("case", [CASES[6], CASES[7], CASES[13],
+                                  dict(dim=3, n=(12, 10, 8), parts=(2, 2, 2), order=1, seed=30),
+                                  dict(dim=3, n=(9, 8, 7), parts=(2, 2, 1), order=1, seed=31,
+                                       sides=(1, 0, 1, 1, 0, 1))], ids=case_id)
+def test_mixed_solver_matches_gathered_lu(backend, case):
+    """FP64 refinement around FP32 CG (matrix-free on cube Q1, FP32 CSR otherwise)."""
+    pb = make_problem(**case)
+    fe = go.build_fespace(pb)
+    x_ref = go.solve_lu(go.assemble(pb, fe, "sub"), fe.dofs[0].ngdofs)
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    x = op.matrix.solve(rtol=1e-12, method="mixed_ir")
+    assert op.matrix.last_stats.converged
+    assert op.matrix.last_stats.rel_residual <= 1e-12
+    assert np.abs(x - x_ref).max() / np.abs(x_ref).max() <= SOL_TOL
+
+
 @pytest.mark.parametrize("strategy", ["sub", "full"])
 @pytest.mark.parametrize("parts", [(2, 2), (1, 1), (2, 1), (1, 2)])
 def test_fespaces_kat_on_gpu(backend, parts, strategy):
