@@ -271,6 +271,8 @@ struct gd_asm {
   gd::MixedState mx;
   int64_t numeric_epoch = 0;
   double mf_ratio = 0.0;
+  double mf_k2 = 0.0;
+  const double* rhs_override = nullptr;   // solve with a caller-given right-hand side
   // solver workspace
   gd::DBuf<double> w;              // vectors
   gd::DBuf<double> dred;           // reduction partials

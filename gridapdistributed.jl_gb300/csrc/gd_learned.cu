@@ -1,0 +1,739 @@
+// Learned preconditioner for the mixed-precision flexible CG (Q1 spaces).
+//
+// A 3-level, 8-channel convolutional network on the structured node lattice, linear in
+// the residual and gated by the coefficient field:
+//   x0 = D^-1 r on the lattice (0 on Dirichlet nodes)
+//   f0 = log(kappa at the nodes), f1 = R f0, f2 = R f1          (computed once per problem)
+//   s_k = sigmoid(conv3(f_l; G_k) + b_k)                        (8 channels, per problem)
+//   h0 = conv3(x0; W0) * s0            (1 -> 8, level 0)
+//   h1 = conv3(R h0; W1) * s1          (8 -> 8, level 1)
+//   h2 = conv3(R h1; W2) * s2          (8 -> 8, level 2)
+//   v1 = conv3(P h2 + h1; W3) * s3     (8 -> 8, level 1)
+//   o  = conv3(P v1 + h0; W4)          (8 -> 1, level 0)
+//   z  = x0 + o  on the free nodes
+// R is full-weighting restriction (coarse node i <-> fine node 2i), P trilinear
+// prolongation (P = 8 R^T); conv3 is a 3x3x3 convolution with zero padding.  Training
+// minimises the relative A-norm error ||z - e||_A^2 / ||e||_A^2 over (residual, error)
+// pairs generated by the solver, with hand-written backward kernels and Adam.  All in
+// FP32; every reduction is two-stage in a fixed order (deterministic).
+#include <cmath>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gd_internal.h"
+#include "gd_solve_mixed.h"
+
+namespace gd {
+
+constexpr int kC = 8;          // channels
+constexpr int kTaps = 27;
+constexpr int kLT = 256;       // threads per block for lattice kernels
+constexpr int kTile = 8;       // weight-gradient tiles are 8^3 voxels
+
+// parameter layout (floats)
+struct NetLayout {
+  static constexpr int W0 = 0;                              // [8][1][27]
+  static constexpr int W1 = W0 + kC * kTaps;                // [8][8][27]
+  static constexpr int W2 = W1 + kC * kC * kTaps;
+  static constexpr int W3 = W2 + kC * kC * kTaps;
+  static constexpr int W4 = W3 + kC * kC * kTaps;           // [1][8][27]
+  static constexpr int G0 = W4 + kC * kTaps;                // [8][1][27] x 4 gates
+  static constexpr int G1 = G0 + kC * kTaps;
+  static constexpr int G2 = G1 + kC * kTaps;
+  static constexpr int G3 = G2 + kC * kTaps;
+  static constexpr int B0 = G3 + kC * kTaps;                // [8] x 4 gate biases
+  static constexpr int B1 = B0 + kC;
+  static constexpr int B2 = B1 + kC;
+  static constexpr int B3 = B2 + kC;
+  static constexpr int N = B3 + kC;
+};
+
+struct Dims {
+  int n[3];
+  __host__ __device__ int64_t size() const { return (int64_t)n[0] * n[1] * n[2]; }
+};
+
+__host__ __device__ inline Dims coarse_dims(const Dims& f) {
+  Dims c;
+  for (int d = 0; d < 3; ++d) c.n[d] = f.n[d] > 1 ? (f.n[d] + 1) / 2 : 1;
+  return c;
+}
+
+// ---- convolution --------------------------------------------------------------------------
+// out[co][v] (+)= sum_ci sum_tap W[co][ci][tap] * in[ci][v + off(tap)], zero padding.
+// mode 0: forward; mode 1: adjoint with respect to the input (W flipped and transposed).
+template <int CI, int CO>
+__global__ void __launch_bounds__(kLT) k_conv3(Dims d, const float* __restrict__ in, const float* __restrict__ W,
+                                               const float* __restrict__ gate, const float* __restrict__ bias,
+                                               float* __restrict__ out, int mode, int accumulate) {
+  __shared__ float sw[CO * CI * kTaps];
+  for (int i = threadIdx.x; i < CO * CI * kTaps; i += blockDim.x) {
+    if (mode == 0) {
+      sw[i] = W[i];
+    } else {   // sw[co'][ci'][tap] = W[ci'][co'][26 - tap] for the adjoint (here CO = original CI)
+      const int tap = i % kTaps, ci = (i / kTaps) % CI, co = i / (kTaps * CI);
+      sw[i] = W[(ci * CO + co) * kTaps + (kTaps - 1 - tap)];
+    }
+  }
+  __syncthreads();
+  const int64_t nv = d.size();
+  const int64_t plane = (int64_t)d.n[0] * d.n[1];
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(v % d.n[0]);
+    const int y = (int)((v / d.n[0]) % d.n[1]);
+    const int z = (int)(v / plane);
+    float acc[CO];
+#pragma unroll
+    for (int co = 0; co < CO; ++co) acc[co] = bias ? bias[co] : 0.f;
+#pragma unroll
+    for (int tap = 0; tap < kTaps; ++tap) {
+      const int dx = tap % 3 - 1, dy = (tap / 3) % 3 - 1, dz = tap / 9 - 1;
+      const int xx = x + dx, yy = y + dy, zz = z + dz;
+      if (xx < 0 || xx >= d.n[0] || yy < 0 || yy >= d.n[1] || zz < 0 || zz >= d.n[2]) continue;
+      const int64_t u = xx + (int64_t)d.n[0] * (yy + (int64_t)d.n[1] * zz);
+#pragma unroll
+      for (int ci = 0; ci < CI; ++ci) {
+        const float val = __ldg(in + ci * nv + u);
+#pragma unroll
+        for (int co = 0; co < CO; ++co) acc[co] = fmaf(sw[(co * CI + ci) * kTaps + tap], val, acc[co]);
+      }
+    }
+#pragma unroll
+    for (int co = 0; co < CO; ++co) {
+      float r = acc[co];
+      if (gate) r *= gate[co * nv + v];
+      if (accumulate) out[co * nv + v] += r;
+      else out[co * nv + v] = r;
+    }
+  }
+}
+
+// weight gradient partials: part[tile][co][ci][tap] = sum_{v in tile} in[ci][v+off] * g[co][v]
+template <int CI, int CO>
+__global__ void __launch_bounds__(kLT) k_conv3_wgrad(Dims d, const float* __restrict__ in, const float* __restrict__ g,
+                                                     float* __restrict__ part) {
+  constexpr int H = kTile + 2;
+  __shared__ float sin_[CI * H * H * H];
+  __shared__ float sg[CO * kTile * kTile * kTile];
+  const int tiles_x = (d.n[0] + kTile - 1) / kTile, tiles_y = (d.n[1] + kTile - 1) / kTile;
+  const int t = blockIdx.x;
+  const int tx = t % tiles_x, ty = (t / tiles_x) % tiles_y, tz = t / (tiles_x * tiles_y);
+  const int x0 = tx * kTile, y0 = ty * kTile, z0 = tz * kTile;
+  const int64_t nv = d.size();
+  for (int i = threadIdx.x; i < CI * H * H * H; i += blockDim.x) {
+    const int ci = i / (H * H * H), r = i % (H * H * H);
+    const int hx = r % H, hy = (r / H) % H, hz = r / (H * H);
+    const int xx = x0 + hx - 1, yy = y0 + hy - 1, zz = z0 + hz - 1;
+    float val = 0.f;
+    if (xx >= 0 && xx < d.n[0] && yy >= 0 && yy < d.n[1] && zz >= 0 && zz < d.n[2])
+      val = in[ci * nv + xx + (int64_t)d.n[0] * (yy + (int64_t)d.n[1] * zz)];
+    sin_[i] = val;
+  }
+  for (int i = threadIdx.x; i < CO * kTile * kTile * kTile; i += blockDim.x) {
+    const int co = i / (kTile * kTile * kTile), r = i % (kTile * kTile * kTile);
+    const int lx = r % kTile, ly = (r / kTile) % kTile, lz = r / (kTile * kTile);
+    const int xx = x0 + lx, yy = y0 + ly, zz = z0 + lz;
+    float val = 0.f;
+    if (xx < d.n[0] && yy < d.n[1] && zz < d.n[2]) val = g[co * nv + xx + (int64_t)d.n[0] * (yy + (int64_t)d.n[1] * zz)];
+    sg[i] = val;
+  }
+  __syncthreads();
+  constexpr int NW = CO * CI * kTaps;
+  for (int w = threadIdx.x; w < NW; w += blockDim.x) {
+    const int tap = w % kTaps, ci = (w / kTaps) % CI, co = w / (kTaps * CI);
+    const int dx = tap % 3, dy = (tap / 3) % 3, dz = tap / 9;   // halo offsets (off + 1)
+    float acc = 0.f;
+    for (int lz = 0; lz < kTile; ++lz)
+      for (int ly = 0; ly < kTile; ++ly)
+#pragma unroll
+        for (int lx = 0; lx < kTile; ++lx)
+          acc = fmaf(sin_[ci * H * H * H + (lx + dx) + H * ((ly + dy) + H * (lz + dz))],
+                     sg[co * kTile * kTile * kTile + lx + kTile * (ly + kTile * lz)], acc);
+    part[(int64_t)t * NW + w] = acc;
+  }
+}
+
+// bias gradient partials: part[block][co] = sum_v g[co][v]
+__global__ void k_bias_grad(Dims d, int co_n, const float* __restrict__ g, float* __restrict__ part) {
+  __shared__ float sh[kLT];
+  const int64_t nv = d.size();
+  for (int co = 0; co < co_n; ++co) {
+    float a = 0.f;
+    for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x)
+      a += g[co * nv + v];
+    sh[threadIdx.x] = a;
+    __syncthreads();
+    for (int s = blockDim.x / 2; s > 0; s >>= 1) {
+      if ((int)threadIdx.x < s) sh[threadIdx.x] += sh[threadIdx.x + s];
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) part[blockIdx.x * co_n + co] = sh[0];
+    __syncthreads();
+  }
+}
+
+// out[w] (+)= sum_p part[p][w] (fixed order)
+__global__ void k_sum_partials(int nparts, int nw, const float* __restrict__ part, float* __restrict__ out) {
+  const int w = blockIdx.x * blockDim.x + threadIdx.x;
+  if (w >= nw) return;
+  float a = 0.f;
+  for (int p = 0; p < nparts; ++p) a += part[(int64_t)p * nw + w];
+  out[w] += a;
+}
+
+// ---- restriction / prolongation (per channel) ---------------------------------------------
+// coarse[i] = sum_{o in {-1,0,1}^3} w(o) fine[2i+o], w = prod(1/2 if o=0 else 1/4)
+__global__ void k_restrict(int C, Dims f, Dims c, const float* __restrict__ fine, float* __restrict__ coarse,
+                           float scale) {
+  const int64_t nc = c.size(), nf = f.size();
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < (int64_t)C * nc;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int ch = (int)(v / nc);
+    const int64_t i = v % nc;
+    const int ix = (int)(i % c.n[0]), iy = (int)((i / c.n[0]) % c.n[1]), iz = (int)(i / ((int64_t)c.n[0] * c.n[1]));
+    float acc = 0.f;
+    for (int oz = -1; oz <= 1; ++oz)
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int fx = 2 * ix + ox, fy = 2 * iy + oy, fz = 2 * iz + oz;
+          if (fx < 0 || fx >= f.n[0] || fy < 0 || fy >= f.n[1] || fz < 0 || fz >= f.n[2]) continue;
+          const float w = (ox == 0 ? 0.5f : 0.25f) * (oy == 0 ? 0.5f : 0.25f) * (oz == 0 ? 0.5f : 0.25f);
+          acc = fmaf(w, fine[ch * nf + fx + (int64_t)f.n[0] * (fy + (int64_t)f.n[1] * fz)], acc);
+        }
+    coarse[ch * nc + i] = scale * acc;
+  }
+}
+
+// fine[j] (+)= scale * sum_i w'(j - 2i) coarse[i], trilinear w' = prod(1 if 0 else 1/2)
+__global__ void k_prolong(int C, Dims c, Dims f, const float* __restrict__ coarse, float* __restrict__ fine,
+                          float scale, int accumulate) {
+  const int64_t nc = c.size(), nf = f.size();
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < (int64_t)C * nf;
+       v += (int64_t)gridDim.x * blockDim.x) {
+    const int ch = (int)(v / nf);
+    const int64_t j = v % nf;
+    const int jx = (int)(j % f.n[0]), jy = (int)((j / f.n[0]) % f.n[1]), jz = (int)(j / ((int64_t)f.n[0] * f.n[1]));
+    float acc = 0.f;
+    for (int oz = -1; oz <= 1; ++oz)
+      for (int oy = -1; oy <= 1; ++oy)
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int cx2 = jx - ox, cy2 = jy - oy, cz2 = jz - oz;   // 2i = j - o
+          if ((cx2 & 1) || (cy2 & 1) || (cz2 & 1)) continue;
+          const int cx = cx2 / 2, cy = cy2 / 2, cz = cz2 / 2;
+          if (cx2 < 0 || cy2 < 0 || cz2 < 0 || cx >= c.n[0] || cy >= c.n[1] || cz >= c.n[2]) continue;
+          const float w = (ox == 0 ? 1.f : 0.5f) * (oy == 0 ? 1.f : 0.5f) * (oz == 0 ? 1.f : 0.5f);
+          acc = fmaf(w, coarse[ch * nc + cx + (int64_t)c.n[0] * (cy + (int64_t)c.n[1] * cz)], acc);
+        }
+    if (accumulate) fine[ch * nf + j] += scale * acc;
+    else fine[ch * nf + j] = scale * acc;
+  }
+}
+
+// ---- elementwise ---------------------------------------------------------------------------
+__global__ void k_sigmoid(int64_t n, float* __restrict__ a) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    a[i] = 1.f / (1.f + __expf(-a[i]));
+}
+// gy -> grad of the pre-gate value (ga = gy*s) and of the gate pre-activation (gp = gy*a*s*(1-s));
+// a = ungated value.
+__global__ void k_gate_bwd(int64_t n, const float* __restrict__ gy, const float* __restrict__ a,
+                           const float* __restrict__ s, float* __restrict__ ga, float* __restrict__ gp) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const float si = s[i];
+    ga[i] = gy[i] * si;
+    if (gp) gp[i] = gy[i] * a[i] * si * (1.f - si);
+  }
+}
+__global__ void k_mul(int64_t n, const float* __restrict__ a, const float* __restrict__ b, float* __restrict__ c) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    c[i] = a[i] * b[i];
+}
+__global__ void k_copyf(int64_t n, const float* __restrict__ a, float* __restrict__ b) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    b[i] = a[i];
+}
+
+// lattice[X] = scale * dinv[gid] * v[gid] (0 on Dirichlet nodes); v in gid order
+__global__ void k_to_lattice(int64_t nlat, const int32_t* __restrict__ node_gid, const float* __restrict__ v,
+                             const float* __restrict__ dinv, float* __restrict__ lat) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlat; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = node_gid[i];
+    lat[i] = g >= 0 ? (dinv ? dinv[g] * v[g] : v[g]) : 0.f;
+  }
+}
+// out[r] = a[X_r] + b[X_r] over the owned rows (X_r = row_node[r]); b may be null
+__global__ void k_from_lattice(int64_t n, const int32_t* __restrict__ row_node, const float* __restrict__ a,
+                               const float* __restrict__ b, float* __restrict__ out) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t X = row_node[r];
+    out[r] = a[X] + (b ? b[X] : 0.f);
+  }
+}
+
+// node feature: log of the mean coefficient of the valid cells around the node (cube Q1:
+// w = K2 * kappa, so kappa = w / K2)
+__global__ void k_node_logk(Dims d, const int64_t* __restrict__ ncell, const double* __restrict__ w, double inv_k2,
+                            float* __restrict__ f) {
+  const int64_t nv = d.size();
+  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < nv; v += (int64_t)gridDim.x * blockDim.x) {
+    const int x = (int)(v % d.n[0]), y = (int)((v / d.n[0]) % d.n[1]), z = (int)(v / ((int64_t)d.n[0] * d.n[1]));
+    double s = 0.0;
+    int c = 0;
+    for (int a = 0; a < 8; ++a) {
+      const int64_t cx = x - 1 + (a & 1), cy = y - 1 + ((a >> 1) & 1), cz = z - 1 + ((a >> 2) & 1);
+      if (cx < 0 || cx >= ncell[0] || cy < 0 || cy >= ncell[1] || cz < 0 || cz >= ncell[2]) continue;
+      s += w[cx + ncell[0] * (cy + ncell[1] * cz)] * inv_k2;
+      ++c;
+    }
+    f[v] = c ? (float)log(s / c) : 0.f;
+  }
+}
+
+// Adam on the flat parameter vector
+__global__ void k_adam(int n, float* __restrict__ p, const float* __restrict__ g, float* __restrict__ m,
+                       float* __restrict__ v, float lr, float b1, float b2, float eps, float c1, float c2, float scale) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float gi = g[i] * scale;
+  const float mi = b1 * m[i] + (1.f - b1) * gi;
+  const float vi = b2 * v[i] + (1.f - b2) * gi * gi;
+  m[i] = mi;
+  v[i] = vi;
+  p[i] -= lr * (mi / c1) / (sqrtf(vi / c2) + eps);
+}
+
+// y = s * (a - b) (gid order)
+__global__ void k_axmb(int64_t n, float s, const float* __restrict__ a, const float* __restrict__ b,
+                       float* __restrict__ y) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    y[i] = s * (a[i] - (b ? b[i] : 0.f));
+}
+
+__device__ inline double blk_sum(double v, double* sh) {
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < (int)(blockDim.x >> 5); ++i) s += sh[i];
+  __syncthreads();
+  return s;
+}
+__global__ void k_sum_d(int nb, const double* __restrict__ p, double* __restrict__ out) {
+  __shared__ double sh[kLT / 32];
+  double a = 0.0;
+  for (int i = threadIdx.x; i < nb; i += blockDim.x) a += p[i];
+  const double s = blk_sum(a, sh);
+  if (threadIdx.x == 0) *out = s;
+}
+
+static inline unsigned nb_for(int64_t n) {
+  int64_t b = (n + kLT - 1) / kLT;
+  return (unsigned)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
+}
+
+}  // namespace gd
+
+using namespace gd;
+
+// ---------------------------------------------------------------------------------
+// Network object
+// ---------------------------------------------------------------------------------
+struct gd_learned {
+  gd_asm* A = nullptr;
+  Dims L[3];
+  int64_t nl[3] = {0, 0, 0};
+  DBuf<float> params, grads, adam_m, adam_v;
+  int64_t adam_t = 0;
+  // per-problem static features and gates (8 channels per gate)
+  DBuf<float> f[3];
+  DBuf<float> s0, s1, s2, s3;   // gate values
+  bool prepared = false;
+  int64_t prepared_epoch = -1;
+  // forward cache
+  DBuf<float> x0, h0a, h0, x1, h1a, h1, x2, h2a, h2, u1, v1a, v1, u0, o;
+  // backward scratch
+  DBuf<float> g0, g0b, gl1, gl1b, gl2, gl2b, gp0, gp1;
+  DBuf<float> part;   // weight-gradient partials
+  DBuf<double> dred;  // reductions for the loss
+  DBuf<float> zv, ev, dv, yv;   // gid-order vectors
+};
+
+namespace gd {
+
+static int conv_launch(int ci, int co, const Dims& d, const float* in, const float* W, const float* gate,
+                       const float* bias, float* out, int mode, int acc, cudaStream_t st) {
+  const unsigned nb = nb_for(d.size());
+  if (ci == 1 && co == 8) k_conv3<1, 8><<<nb, kLT, 0, st>>>(d, in, W, gate, bias, out, mode, acc);
+  else if (ci == 8 && co == 8) k_conv3<8, 8><<<nb, kLT, 0, st>>>(d, in, W, gate, bias, out, mode, acc);
+  else if (ci == 8 && co == 1) k_conv3<8, 1><<<nb, kLT, 0, st>>>(d, in, W, gate, bias, out, mode, acc);
+  else return fail(GD_ERR_UNSUPPORTED, "learned: unsupported convolution shape");
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+static int ntiles(const Dims& d) {
+  return ((d.n[0] + kTile - 1) / kTile) * ((d.n[1] + kTile - 1) / kTile) * ((d.n[2] + kTile - 1) / kTile);
+}
+
+// dW += wgrad(in, g)
+static int wgrad_launch(gd_learned* N, int ci, int co, const Dims& d, const float* in, const float* g, float* dW,
+                        cudaStream_t st) {
+  const int nt = ntiles(d);
+  const int nw = ci * co * kTaps;
+  if (N->part.n < (size_t)nt * nw) GD_TRY(dalloc(N->part, (size_t)nt * nw));
+  if (ci == 1 && co == 8) k_conv3_wgrad<1, 8><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
+  else if (ci == 8 && co == 8) k_conv3_wgrad<8, 8><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
+  else if (ci == 8 && co == 1) k_conv3_wgrad<8, 1><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
+  else return fail(GD_ERR_UNSUPPORTED, "learned: unsupported gradient shape");
+  k_sum_partials<<<(nw + 127) / 128, 128, 0, st>>>(nt, nw, N->part.p, dW);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+static int bgrad_launch(gd_learned* N, const Dims& d, const float* g, float* dB, cudaStream_t st) {
+  const int nb = 256;
+  if (N->part.n < (size_t)nb * kC) GD_TRY(dalloc(N->part, (size_t)nb * kC));
+  k_bias_grad<<<nb, kLT, 0, st>>>(d, kC, g, N->part.p);
+  k_sum_partials<<<1, 128, 0, st>>>(nb, kC, N->part.p, dB);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// static part: features and gates (after every numeric assembly)
+static int net_prepare(gd_learned* N, cudaStream_t st) {
+  gd_asm* A = N->A;
+  if (N->prepared && N->prepared_epoch == A->numeric_epoch) return GD_OK;
+  GD_TRY(mixed_setup(A));
+  const Geom& g = A->test->geom;
+  int64_t hn[3] = {g.n[0], g.n[1], g.n[2]};
+  DBuf<int64_t> dn;
+  GD_TRY(dalloc(dn, 3));
+  GD_CUDA_TRY(cudaMemcpyAsync(dn.p, hn, sizeof(hn), cudaMemcpyHostToDevice, st));
+  const float* P = N->params.p;
+  k_node_logk<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->L[0], dn.p, A->w_cells.p, 1.0 / A->mf_k2, N->f[0].p);
+  k_restrict<<<nb_for(N->nl[1]), kLT, 0, st>>>(1, N->L[0], N->L[1], N->f[0].p, N->f[1].p, 1.f);
+  k_restrict<<<nb_for(N->nl[2]), kLT, 0, st>>>(1, N->L[1], N->L[2], N->f[1].p, N->f[2].p, 1.f);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_TRY(conv_launch(1, 8, N->L[0], N->f[0].p, P + NetLayout::G0, nullptr, P + NetLayout::B0, N->s0.p, 0, 0, st));
+  GD_TRY(conv_launch(1, 8, N->L[1], N->f[1].p, P + NetLayout::G1, nullptr, P + NetLayout::B1, N->s1.p, 0, 0, st));
+  GD_TRY(conv_launch(1, 8, N->L[2], N->f[2].p, P + NetLayout::G2, nullptr, P + NetLayout::B2, N->s2.p, 0, 0, st));
+  GD_TRY(conv_launch(1, 8, N->L[1], N->f[1].p, P + NetLayout::G3, nullptr, P + NetLayout::B3, N->s3.p, 0, 0, st));
+  k_sigmoid<<<nb_for(kC * N->nl[0]), kLT, 0, st>>>(kC * N->nl[0], N->s0.p);
+  k_sigmoid<<<nb_for(kC * N->nl[1]), kLT, 0, st>>>(kC * N->nl[1], N->s1.p);
+  k_sigmoid<<<nb_for(kC * N->nl[2]), kLT, 0, st>>>(kC * N->nl[2], N->s2.p);
+  k_sigmoid<<<nb_for(kC * N->nl[1]), kLT, 0, st>>>(kC * N->nl[1], N->s3.p);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  dfreeb(dn);
+  N->prepared = true;
+  N->prepared_epoch = A->numeric_epoch;
+  return GD_OK;
+}
+
+// forward: r (gid order, FP32) -> z (gid order); keeps activations for backward
+static int net_forward(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const float* P = N->params.p;
+  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
+  const Dims *L = N->L;
+  const int64_t* nl = N->nl;
+  k_to_lattice<<<nb_for(nl[0]), kLT, 0, st>>>(nl[0], A->mx.node_gid.p, r, dinv, N->x0.p);
+  GD_TRY(conv_launch(1, 8, L[0], N->x0.p, P + NetLayout::W0, nullptr, nullptr, N->h0a.p, 0, 0, st));
+  k_mul<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->h0a.p, N->s0.p, N->h0.p);
+  k_restrict<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[0], L[1], N->h0.p, N->x1.p, 1.f);
+  GD_TRY(conv_launch(8, 8, L[1], N->x1.p, P + NetLayout::W1, nullptr, nullptr, N->h1a.p, 0, 0, st));
+  k_mul<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->h1a.p, N->s1.p, N->h1.p);
+  k_restrict<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC, L[1], L[2], N->h1.p, N->x2.p, 1.f);
+  GD_TRY(conv_launch(8, 8, L[2], N->x2.p, P + NetLayout::W2, nullptr, nullptr, N->h2a.p, 0, 0, st));
+  k_mul<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC * nl[2], N->h2a.p, N->s2.p, N->h2.p);
+  k_copyf<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->h1.p, N->u1.p);
+  k_prolong<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[2], L[1], N->h2.p, N->u1.p, 1.f, 1);
+  GD_TRY(conv_launch(8, 8, L[1], N->u1.p, P + NetLayout::W3, nullptr, nullptr, N->v1a.p, 0, 0, st));
+  k_mul<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->v1a.p, N->s3.p, N->v1.p);
+  k_copyf<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->h0.p, N->u0.p);
+  k_prolong<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC, L[1], L[0], N->v1.p, N->u0.p, 1.f, 1);
+  GD_TRY(conv_launch(8, 1, L[0], N->u0.p, P + NetLayout::W4, nullptr, nullptr, N->o.p, 0, 0, st));
+  k_from_lattice<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, N->x0.p, N->o.p, z);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// backward of the loss gradient gz (gid order) into N->grads (accumulated)
+static int net_backward(gd_learned* N, const float* gz, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const float* P = N->params.p;
+  float* G = N->grads.p;
+  const Dims* L = N->L;
+  const int64_t* nl = N->nl;
+  // grad o on the lattice (o only reaches the free nodes)
+  k_to_lattice<<<nb_for(nl[0]), kLT, 0, st>>>(nl[0], A->mx.node_gid.p, gz, nullptr, N->g0b.p);   // 1 channel
+  // o = conv(u0; W4)
+  GD_TRY(wgrad_launch(N, 8, 1, L[0], N->u0.p, N->g0b.p, G + NetLayout::W4, st));
+  GD_TRY(conv_launch(1, 8, L[0], N->g0b.p, P + NetLayout::W4, nullptr, nullptr, N->g0.p, 1, 0, st));   // g u0
+  // u0 = h0 + P v1  ->  g h0 = g u0 (kept in g0), g v1 = 8 R(g u0)
+  k_restrict<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[0], L[1], N->g0.p, N->gl1.p, 8.f);
+  // v1 = v1a * s3
+  k_gate_bwd<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->gl1.p, N->v1a.p, N->s3.p, N->gl1b.p, N->gp1.p);
+  GD_TRY(wgrad_launch(N, 1, 8, L[1], N->f[1].p, N->gp1.p, G + NetLayout::G3, st));
+  GD_TRY(bgrad_launch(N, L[1], N->gp1.p, G + NetLayout::B3, st));
+  // v1a = conv(u1; W3)
+  GD_TRY(wgrad_launch(N, 8, 8, L[1], N->u1.p, N->gl1b.p, G + NetLayout::W3, st));
+  GD_TRY(conv_launch(8, 8, L[1], N->gl1b.p, P + NetLayout::W3, nullptr, nullptr, N->gl1.p, 1, 0, st));   // g u1
+  // u1 = h1 + P h2 -> g h2 = 8 R(g u1); g h1 = g u1 (+ from x2 = R h1 below)
+  k_restrict<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC, L[1], L[2], N->gl1.p, N->gl2.p, 8.f);
+  // h2 = h2a * s2
+  k_gate_bwd<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC * nl[2], N->gl2.p, N->h2a.p, N->s2.p, N->gl2b.p, N->gp1.p);
+  GD_TRY(wgrad_launch(N, 1, 8, L[2], N->f[2].p, N->gp1.p, G + NetLayout::G2, st));
+  GD_TRY(bgrad_launch(N, L[2], N->gp1.p, G + NetLayout::B2, st));
+  // h2a = conv(x2; W2)
+  GD_TRY(wgrad_launch(N, 8, 8, L[2], N->x2.p, N->gl2b.p, G + NetLayout::W2, st));
+  GD_TRY(conv_launch(8, 8, L[2], N->gl2b.p, P + NetLayout::W2, nullptr, nullptr, N->gl2.p, 1, 0, st));   // g x2
+  // x2 = R h1 -> g h1 += (1/8) P(g x2)
+  k_prolong<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[2], L[1], N->gl2.p, N->gl1.p, 0.125f, 1);
+  // h1 = h1a * s1
+  k_gate_bwd<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->gl1.p, N->h1a.p, N->s1.p, N->gl1b.p, N->gp1.p);
+  GD_TRY(wgrad_launch(N, 1, 8, L[1], N->f[1].p, N->gp1.p, G + NetLayout::G1, st));
+  GD_TRY(bgrad_launch(N, L[1], N->gp1.p, G + NetLayout::B1, st));
+  // h1a = conv(x1; W1)
+  GD_TRY(wgrad_launch(N, 8, 8, L[1], N->x1.p, N->gl1b.p, G + NetLayout::W1, st));
+  GD_TRY(conv_launch(8, 8, L[1], N->gl1b.p, P + NetLayout::W1, nullptr, nullptr, N->gl1.p, 1, 0, st));   // g x1
+  // x1 = R h0 -> g h0 += (1/8) P(g x1)
+  k_prolong<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC, L[1], L[0], N->gl1.p, N->g0.p, 0.125f, 1);
+  // h0 = h0a * s0  (u0 is free again: its last use was the W4 gradient above)
+  k_gate_bwd<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->g0.p, N->h0a.p, N->s0.p, N->u0.p, N->gp0.p);
+  GD_TRY(wgrad_launch(N, 1, 8, L[0], N->f[0].p, N->gp0.p, G + NetLayout::G0, st));
+  GD_TRY(bgrad_launch(N, L[0], N->gp0.p, G + NetLayout::B0, st));
+  // h0a = conv(x0; W0)
+  GD_TRY(wgrad_launch(N, 1, 8, L[0], N->x0.p, N->u0.p, G + NetLayout::W0, st));
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// loss for one pair and its gradient wrt z: L = (z-e)A(z-e) / eAe, gz = 2 A(z-e) / eAe
+static int net_loss(gd_learned* N, const float* z, const float* e, double* loss, float* gz, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const int64_t n = A->ngdofs;
+  double* red = N->dred.p;   // [0..1023] partials, [2048] eAe, [2049] dAd
+  k_axmb<<<nb_for(n), kLT, 0, st>>>(n, 1.f, z, e, N->dv.p);
+  GD_TRY(mixed_apply(A, N->dv.p, N->yv.p, red, st));   // yv = A d, partial d.Ad
+  int nbm = (int)std::min<int64_t>((n + 255) / 256, 1024);
+  k_sum_d<<<1, kLT, 0, st>>>(nbm, red, red + 2049);
+  GD_TRY(mixed_apply(A, e, N->zv.p, red, st));         // partial e.Ae
+  k_sum_d<<<1, kLT, 0, st>>>(nbm, red, red + 2048);
+  double h[2];
+  GD_CUDA_TRY(cudaMemcpyAsync(h, red + 2048, sizeof(h), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  const double eAe = h[0] > 0 ? h[0] : 1.0;
+  *loss = h[1] / eAe;
+  if (gz) {
+    k_axmb<<<nb_for(n), kLT, 0, st>>>(n, (float)(2.0 / eAe), N->yv.p, nullptr, gz);
+    GD_CUDA_TRY(cudaGetLastError());
+  }
+  return GD_OK;
+}
+
+static int apply_as_precond(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st) {
+  (void)A;
+  return net_forward(static_cast<gd_learned*>(ctx), r, z, st);
+}
+
+}  // namespace gd
+
+// ---------------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------------
+extern "C" int gd_learned_create(gd_asm* A, uint64_t seed, gd_learned** out) {
+  if (!A || !out) return fail(GD_ERR_ARG, "gd_learned_create: null argument");
+  if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_learned_create: assemble the system first");
+  if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3))
+    return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells");
+  gd_learned* N = new gd_learned();
+  N->A = A;
+  const Geom& g = A->test->geom;
+  for (int d = 0; d < 3; ++d) N->L[0].n[d] = (int)g.N[d];
+  N->L[1] = coarse_dims(N->L[0]);
+  N->L[2] = coarse_dims(N->L[1]);
+  for (int l = 0; l < 3; ++l) N->nl[l] = N->L[l].size();
+  auto fail_clean = [&](int s) {
+    std::string msg = gd_last_error();
+    gd_learned_destroy(N);
+    return fail(s, msg);
+  };
+  int s = GD_OK;
+#define ALLOC(buf, count) \
+  if ((s = dalloc(buf, (size_t)(count))) != GD_OK) return fail_clean(s);
+  ALLOC(N->params, NetLayout::N);
+  ALLOC(N->grads, NetLayout::N);
+  ALLOC(N->adam_m, NetLayout::N);
+  ALLOC(N->adam_v, NetLayout::N);
+  for (int l = 0; l < 3; ++l) ALLOC(N->f[l], N->nl[l]);
+  ALLOC(N->s0, kC * N->nl[0]);
+  ALLOC(N->s1, kC * N->nl[1]);
+  ALLOC(N->s2, kC * N->nl[2]);
+  ALLOC(N->s3, kC * N->nl[1]);
+  ALLOC(N->x0, N->nl[0]);
+  ALLOC(N->h0a, kC * N->nl[0]);
+  ALLOC(N->h0, kC * N->nl[0]);
+  ALLOC(N->x1, kC * N->nl[1]);
+  ALLOC(N->h1a, kC * N->nl[1]);
+  ALLOC(N->h1, kC * N->nl[1]);
+  ALLOC(N->x2, kC * N->nl[2]);
+  ALLOC(N->h2a, kC * N->nl[2]);
+  ALLOC(N->h2, kC * N->nl[2]);
+  ALLOC(N->u1, kC * N->nl[1]);
+  ALLOC(N->v1a, kC * N->nl[1]);
+  ALLOC(N->v1, kC * N->nl[1]);
+  ALLOC(N->u0, kC * N->nl[0]);
+  ALLOC(N->o, N->nl[0]);
+  ALLOC(N->g0, kC * N->nl[0]);
+  ALLOC(N->g0b, kC * N->nl[0]);
+  ALLOC(N->gp0, kC * N->nl[0]);
+  ALLOC(N->gl1, kC * N->nl[1]);
+  ALLOC(N->gl1b, kC * N->nl[1]);
+  ALLOC(N->gp1, kC * N->nl[1]);
+  ALLOC(N->gl2, kC * N->nl[2]);
+  ALLOC(N->gl2b, kC * N->nl[2]);
+  ALLOC(N->dred, 4096);
+  ALLOC(N->zv, A->ngdofs);
+  ALLOC(N->ev, A->ngdofs);
+  ALLOC(N->dv, A->ngdofs);
+  ALLOC(N->yv, A->ngdofs);
+#undef ALLOC
+  // deterministic initialisation: small convolutions (the network starts close to Jacobi),
+  // gates at 0.5
+  std::vector<float> p(NetLayout::N, 0.f);
+  uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+  auto rnd = [&]() {   // uniform in (-1, 1), 64-bit LCG
+    st = st * 6364136223846793005ull + 1442695040888963407ull;
+    return (float)((double)(st >> 11) / 9007199254740992.0 * 2.0 - 1.0);
+  };
+  auto fill = [&](int off, int count, float scale) {
+    for (int i = 0; i < count; ++i) p[off + i] = scale * rnd();
+  };
+  fill(NetLayout::W0, kC * kTaps, 0.2f);
+  fill(NetLayout::W1, kC * kC * kTaps, 0.05f);
+  fill(NetLayout::W2, kC * kC * kTaps, 0.05f);
+  fill(NetLayout::W3, kC * kC * kTaps, 0.05f);
+  fill(NetLayout::W4, kC * kTaps, 0.02f);
+  fill(NetLayout::G0, 4 * kC * kTaps, 0.05f);
+  cudaStream_t cs = A->test->model->ctx->stream;
+  cudaError_t e = cudaMemcpyAsync(N->params.p, p.data(), sizeof(float) * NetLayout::N, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_m.p, 0, sizeof(float) * NetLayout::N, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_v.p, 0, sizeof(float) * NetLayout::N, cs);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
+  if (e != cudaSuccess) {
+    fail(GD_ERR_CUDA, std::string("gd_learned_create: ") + cudaGetErrorString(e));
+    return fail_clean(GD_ERR_CUDA);
+  }
+  *out = N;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_destroy(gd_learned* N) {
+  if (!N) return GD_OK;
+  DBuf<float>* bufs[] = {&N->params, &N->grads, &N->adam_m, &N->adam_v, &N->f[0], &N->f[1], &N->f[2], &N->s0,
+                         &N->s1, &N->s2, &N->s3, &N->x0, &N->h0a, &N->h0, &N->x1, &N->h1a, &N->h1, &N->x2,
+                         &N->h2a, &N->h2, &N->u1, &N->v1a, &N->v1, &N->u0, &N->o, &N->g0, &N->g0b, &N->gp0,
+                         &N->gl1, &N->gl1b, &N->gp1, &N->gl2, &N->gl2b, &N->part, &N->zv, &N->ev, &N->dv, &N->yv};
+  for (auto* b : bufs) dfreeb(*b);
+  dfreeb(N->dred);
+  delete N;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_num_params(const gd_learned* N, int64_t* n) {
+  if (!N || !n) return fail(GD_ERR_ARG, "gd_learned_num_params: null argument");
+  *n = NetLayout::N;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_get_params(const gd_learned* N, float* host) {
+  if (!N || !host) return fail(GD_ERR_ARG, "gd_learned_get_params: null argument");
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  GD_CUDA_TRY(cudaMemcpyAsync(host, N->params.p, sizeof(float) * NetLayout::N, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return GD_OK;
+}
+
+extern "C" int gd_learned_set_params(gd_learned* N, const float* host) {
+  if (!N || !host) return fail(GD_ERR_ARG, "gd_learned_set_params: null argument");
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  GD_CUDA_TRY(cudaMemcpyAsync(N->params.p, host, sizeof(float) * NetLayout::N, cudaMemcpyHostToDevice, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  N->prepared = false;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_apply(gd_learned* N, const float* r, float* z) {
+  if (!N || !r || !z) return fail(GD_ERR_ARG, "gd_learned_apply: null argument");
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  GD_TRY(net_prepare(N, st));
+  GD_TRY(net_forward(N, r, z, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return GD_OK;
+}
+
+extern "C" int gd_learned_gradient(gd_learned* N, const float* r, const float* e, int batch, double* loss,
+                                   float* grads_host) {
+  if (!N || !r || !e || batch < 1 || !loss) return fail(GD_ERR_ARG, "gd_learned_gradient: bad argument");
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  const int64_t n = N->A->ngdofs;
+  GD_TRY(net_prepare(N, st));
+  N->prepared = false;   // gate caches are rebuilt after the parameters change
+  GD_CUDA_TRY(cudaMemsetAsync(N->grads.p, 0, sizeof(float) * NetLayout::N, st));
+  double total = 0.0;
+  for (int b = 0; b < batch; ++b) {
+    GD_TRY(net_forward(N, r + b * n, N->zv.p, st));
+    double l = 0.0;
+    GD_TRY(net_loss(N, N->zv.p, e + b * n, &l, N->ev.p, st));
+    GD_TRY(net_backward(N, N->ev.p, st));
+    total += l;
+  }
+  *loss = total / batch;
+  if (grads_host) {
+    GD_CUDA_TRY(cudaMemcpyAsync(grads_host, N->grads.p, sizeof(float) * NetLayout::N, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return GD_OK;
+}
+
+extern "C" int gd_learned_train_step(gd_learned* N, const float* r, const float* e, int batch, float lr,
+                                     double* loss) {
+  GD_TRY(gd_learned_gradient(N, r, e, batch, loss, nullptr));
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  ++N->adam_t;
+  const float b1 = 0.9f, b2 = 0.999f;
+  const float c1 = 1.f - std::pow(b1, (float)N->adam_t), c2 = 1.f - std::pow(b2, (float)N->adam_t);
+  k_adam<<<(NetLayout::N + 255) / 256, 256, 0, st>>>(NetLayout::N, N->params.p, N->grads.p, N->adam_m.p, N->adam_v.p,
+                                                     lr, b1, b2, 1e-8f, c1, c2, 1.f / batch);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  N->prepared = false;
+  return GD_OK;
+}
+
+// Mixed-precision flexible CG with the network as preconditioner; Jacobi-PCG (same
+// refinement) is the fallback when the learned iteration stalls or does not converge.
+extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit, double* x, int where,
+                                gd_solve_stats* stats, int32_t* fallback_used) {
+  if (!A || !N || N->A != A || !x) return fail(GD_ERR_ARG, "gd_solve_learned: bad argument");
+  if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_solve_learned: assemble the system first");
+  cudaStream_t st = A->test->model->ctx->stream;
+  GD_TRY(net_prepare(N, st));
+  MixedPrecond pc{N, apply_as_precond};
+  if (fallback_used) *fallback_used = 0;
+  gd_solve_stats s1{};
+  int rc = mixed_solve(A, rtol, maxit, x, where, &s1, &pc);
+  if (rc == GD_ERR_STALL || rc == GD_ERR_NOTCONVERGED) {
+    gd_solve_stats s2{};
+    rc = mixed_solve(A, rtol, maxit, x, where, &s2, nullptr);
+    if (fallback_used) *fallback_used = 1;
+    s2.iterations += s1.iterations;
+    s2.seconds += s1.seconds;
+    s1 = s2;
+  }
+  if (stats) *stats = s1;
+  return rc;
+}

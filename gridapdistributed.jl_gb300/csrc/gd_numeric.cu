@@ -771,6 +771,7 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
   bool cube = false;
   GD_TRY(q1_constants(A, f_nodal ? 0.0 : f_const, q, cube));
   A->mf_ratio = q.ratio;
+  A->mf_k2 = q.Kc[3];
   int64_t ncells = 1;
   for (int d = 0; d < DIM; ++d) ncells *= A->test->geom.n[d];
   const double* coef = kappa;

@@ -195,6 +195,18 @@ __global__ void k_gather_local(int64_t n, const int64_t* __restrict__ lid_gid, c
   if (i < n) xl[i] = xg[lid_gid[i]];
 }
 
+static int grid_for(int64_t n, int per_block);
+
+// FP64 residual r = b - A x with per-block partials of r.r and b.b; returns the block count
+int residual_fp64(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, const double* x,
+                  const double* b, double* r, double* prr, double* pbb, cudaStream_t st, int* nblocks) {
+  const int gs = grid_for(n, kRowsPerSpmvBlock);
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, col, val, x, b, r, prr, pbb);
+  GD_CUDA_TRY(cudaGetLastError());
+  *nblocks = gs;
+  return GD_OK;
+}
+
 static int grid_for(int64_t n, int per_block) {
   int64_t b = (n + per_block - 1) / per_block;
   if (b > kMaxPartials) b = kMaxPartials;
@@ -261,6 +273,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   double* pb = pa + kMaxPartials;
   Scalars* sc = (Scalars*)(A->dred.p + 16 + 2 * kMaxPartials);
   int32_t* bad = (int32_t*)A->dred.p;
+  const double* rhs = A->rhs_override ? A->rhs_override : A->rhs.p;
   GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
   GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
   k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, A->dinv.p, bad);
@@ -268,7 +281,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   const int gs = grid_for(n, kRowsPerSpmvBlock);
   const int gv = grid_for(n, kVecThreads);
   // r = b - A*0 = b ; bb
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, dr, pa, pb);
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, dr, pa, pb);
   k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);   // rz <- bb (temp), rr <- rr
   GD_CUDA_TRY(cudaGetLastError());
   Scalars h{};
@@ -301,7 +314,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
     if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
   }
   // true FP64 residual
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, nullptr, pa, pb);
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, nullptr, pa, pb);
   k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
   GD_CUDA_TRY(cudaGetLastError());
   GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
@@ -478,4 +491,25 @@ extern "C" int gd_solve_noalloc(gd_asm* A, double rtol, int maxit, double* x, in
   if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, "gd_solve_noalloc: residual is not finite");
   if (rel > rtol) return fail(GD_ERR_NOTCONVERGED, "gd_solve_noalloc: tolerance not reached in " + std::to_string(it) + " iterations");
   return GD_OK;
+}
+
+// x = A \ b for a caller-given right-hand side (device or host), same methods as gd_solve.
+extern "C" int gd_solve_rhs(gd_asm* A, int method, double rtol, int maxit, const double* b, double* x, int where,
+                            gd_solve_stats* stats) {
+  GD_TRY(check_ready(A, "gd_solve_rhs"));
+  if (!b || !x) return fail(GD_ERR_ARG, "gd_solve_rhs: null vector");
+  cudaStream_t st = A->test->model->ctx->stream;
+  const int64_t n = A->ngdofs;
+  DBuf<double> tb;
+  const double* db = b;
+  if (where == GD_HOST) {
+    GD_TRY(dalloc(tb, std::max<int64_t>(n, 1)));
+    GD_CUDA_TRY(cudaMemcpyAsync(tb.p, b, sizeof(double) * n, cudaMemcpyHostToDevice, st));
+    db = tb.p;
+  }
+  A->rhs_override = db;
+  const int rc = gd_solve(A, method, rtol, maxit, x, where, stats);
+  A->rhs_override = nullptr;
+  dfreeb(tb);
+  return rc;
 }

@@ -267,38 +267,6 @@ __global__ void k_mx_accumulate(int64_t n, double s, const float* __restrict__ x
     x64[i] += s * (double)x32[i];
 }
 
-// FP64 residual r = b - A x and its partial sums (r.r, b.b); 8 lanes per row
-constexpr int kResGroup = 8;
-__global__ void __launch_bounds__(kMxThreads)
-k_mx_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
-              const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ b,
-              double* __restrict__ r, double* __restrict__ prr, double* __restrict__ pbb) {
-  __shared__ double sh[kMxThreads / 32];
-  const int g = threadIdx.x / kResGroup, l = threadIdx.x % kResGroup;
-  constexpr int kRows = kMxThreads / kResGroup;
-  double rr = 0.0, bb = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * kRows;
-  for (int64_t base = (int64_t)blockIdx.x * kRows + (g & ~(32 / kResGroup - 1)); base < n; base += stride) {
-    const int64_t row = base + (g & (32 / kResGroup - 1));
-    const bool valid = row < n;
-    const int64_t e0 = valid ? rowptr[row] : 0, e1 = valid ? rowptr[row + 1] : 0;
-    double s = 0.0;
-    for (int64_t e = e0 + l; e < e1; e += kResGroup) s += val[e] * __ldg(x + col[e]);
-#pragma unroll
-    for (int o = kResGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kResGroup);
-    if (l == 0 && valid) {
-      const double rv = b[row] - s;
-      r[row] = rv;
-      rr += rv * rv;
-      bb += b[row] * b[row];
-    }
-  }
-  double t = block_sum_d(rr, sh);
-  if (threadIdx.x == 0) prr[blockIdx.x] = t;
-  t = block_sum_d(bb, sh);
-  if (threadIdx.x == 0) pbb[blockIdx.x] = t;
-}
-
 static int grid_mx(int64_t n) {
   int64_t b = (n + kMxThreads - 1) / kMxThreads;
   if (b > kMxMaxBlocks) b = kMxMaxBlocks;
@@ -396,8 +364,9 @@ int mixed_solve(gd_asm* A, double rtol, int maxit, double* x_out, int where, gd_
   int status = GD_OK;
   while (true) {
     // FP64 residual of the current iterate
-    const int gr = grid_mx(n);
-    k_mx_residual<<<gr, kMxThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, x64, A->rhs.p, r64, pa, pb);
+    int gr = 0;
+    GD_TRY(residual_fp64(n, A->rowptr.p, A->colgid.p, A->vals.p, x64, A->rhs_override ? A->rhs_override : A->rhs.p,
+                         r64, pa, pb, st, &gr));
     k_mx_scalars<<<1, kMxThreads, 0, st>>>(0, gr, pa, pb, nullptr, sc);
     GD_CUDA_TRY(cudaGetLastError());
     MxScalars h{};

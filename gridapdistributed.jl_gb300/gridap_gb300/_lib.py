@@ -86,7 +86,17 @@ SIGNATURES = {
     "gd_spmv": [P, P, P, C.c_int],
     "gd_solve": [P, C.c_int, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_fe_function_local": [P, C.c_int, P, C.c_int, DP],
+    "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
+    "gd_learned_create": [P, C.c_uint64, PP],
+    "gd_learned_destroy": [P],
+    "gd_learned_num_params": [P, I64P],
+    "gd_learned_get_params": [P, C.POINTER(C.c_float)],
+    "gd_learned_set_params": [P, C.POINTER(C.c_float)],
+    "gd_learned_apply": [P, P, P],
+    "gd_learned_gradient": [P, P, P, C.c_int, DP, C.POINTER(C.c_float)],
+    "gd_learned_train_step": [P, P, P, C.c_int, C.c_float, DP],
+    "gd_solve_learned": [P, P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats), I32P],
 }
 _RESTYPES = {"gd_last_error": C.c_char_p, "gd_version": C.c_char_p}
 

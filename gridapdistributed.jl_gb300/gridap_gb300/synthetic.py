@@ -46,3 +46,34 @@ def lognormal_kappa(cells, sigma=1.0, corr_len=0.1, seed=0):
 POISSON3D_128 = dict(name="poisson3d_q1_128^3_parts2x2x2", dim=3, cells=(128, 128, 128), parts=(2, 2, 2),
                      domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=1, degree=2, sigma=1.0, corr_len=0.1,
                      f=1.0, seed=1000)
+
+
+def gaussian_random_field_torch(cells, sigma=1.0, corr_len=0.1, seed=0, domain_len=1.0, device="cuda"):
+    """Same spectral synthesis as gaussian_random_field, on the GPU with torch (for
+    generating many training fields); a different random stream than the numpy one."""
+    import torch
+    cells = tuple(int(c) for c in cells)
+    dim = len(cells)
+    g = torch.Generator(device=device)
+    g.manual_seed(int(seed))
+    M = tuple(2 * c for c in cells)
+    ks = [2 * torch.pi * torch.fft.fftfreq(M[d], d=domain_len / cells[d], device=device, dtype=torch.float64)
+          for d in range(dim)]
+    grids = torch.meshgrid(*[ks[d] for d in reversed(range(dim))], indexing="ij")
+    k2 = sum(x * x for x in grids)
+    amp = torch.exp(-k2 * corr_len * corr_len / 4.0)
+    shape = tuple(reversed(M))
+    noise = torch.complex(torch.randn(shape, generator=g, device=device, dtype=torch.float64),
+                          torch.randn(shape, generator=g, device=device, dtype=torch.float64))
+    field = torch.fft.ifftn(amp * noise).real[tuple(slice(0, c) for c in reversed(cells))]
+    field = field - field.mean()
+    field = field * (sigma / field.std())
+    return field.reshape(-1).contiguous()
+
+
+# Learned-preconditioner workload: 96^3 Q1 cells on the unit cube, parts (2,2,2),
+# kappa = exp(g) (sigma 1.5, correlation length 0.05), load M f with f ~ N(0,1) per node,
+# homogeneous Dirichlet, solve to 1e-8 FP64 relative residual.
+DIFFUSION3D_96 = dict(name="diffusion3d_q1_96^3_parts2x2x2_sigma1.5", dim=3, cells=(96, 96, 96), parts=(2, 2, 2),
+                      domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=1, degree=2, sigma=1.5, corr_len=0.05,
+                      seed=5000)

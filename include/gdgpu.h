@@ -201,6 +201,10 @@ typedef struct gd_solve_stats {
  * relative residual rtol.  x: global vector (ngdofs). */
 int gd_solve(gd_asm* a, int method, double rtol, int maxit, double* x, int where,
              gd_solve_stats* stats);
+/* x = A \ b for a caller-given right-hand side b (ngdofs, gid order); same methods
+ * and arguments as gd_solve. */
+int gd_solve_rhs(gd_asm* a, int method, double rtol, int maxit, const double* b, double* x, int where,
+                 gd_solve_stats* stats);
 /* gd_solve without device allocation.  No counterpart in the reference: for callers
  * that cannot allocate device memory while they run (an application whose device
  * memory belongs to its own pool allocator, or a loop where a cudaMalloc -- which can
@@ -216,6 +220,30 @@ int gd_solve_noalloc(gd_asm* a, double rtol, int maxit, double* x, int where, gd
  * from a global vector (FESpaces.jl:354-371, Algebra.jl:270-293). */
 int gd_fe_function_local(const gd_space* space, int part, const double* x_global, int where,
                          double* x_local);
+
+/* ---- learned preconditioner (3D Q1 on cube cells) ---------------------------------
+ * No counterpart in the reference (whose `\` is a gathered LU).  A 3-level, 8-channel
+ * convolutional network on the node lattice, linear in the residual and gated by the
+ * coefficient field, used as the preconditioner of the mixed-precision flexible CG.
+ * Vectors r, e, z are FP32 device arrays over the owned DOFs in gid order. */
+typedef struct gd_learned gd_learned;
+int gd_learned_create(gd_asm* a, uint64_t seed, gd_learned** out);
+int gd_learned_destroy(gd_learned* net);
+int gd_learned_num_params(const gd_learned* net, int64_t* n);
+int gd_learned_get_params(const gd_learned* net, float* host_params);
+int gd_learned_set_params(gd_learned* net, const float* host_params);
+/* z = M(r) for the assembler's current coefficients. */
+int gd_learned_apply(gd_learned* net, const float* r, float* z);
+/* Mean relative A-norm error ||M(r_b) - e_b||_A^2 / ||e_b||_A^2 over `batch` pairs stored
+ * back to back, and (optionally) the summed parameter gradients copied to the host. */
+int gd_learned_gradient(gd_learned* net, const float* r, const float* e, int batch, double* loss,
+                        float* grads_host);
+/* One Adam step on a batch of pairs (mean loss returned). */
+int gd_learned_train_step(gd_learned* net, const float* r, const float* e, int batch, float lr, double* loss);
+/* x = A \ b with the learned flexible CG inside FP64 refinement; falls back to Jacobi
+ * (reported in *fallback_used) if the learned iteration stalls or does not converge. */
+int gd_solve_learned(gd_asm* a, gd_learned* net, double rtol, int maxit, double* x, int where,
+                     gd_solve_stats* stats, int32_t* fallback_used);
 
 #ifdef __cplusplus
 }
