@@ -1,18 +1,18 @@
-// Learned preconditioner for the mixed-precision flexible CG (Q1 spaces).
+// Learned preconditioner for the mixed-precision flexible CG (3D Q1 spaces).
 //
-// A 3-level, 8-channel convolutional network on the structured node lattice, linear in
-// the residual and gated by the coefficient field:
-//   x0 = D^-1 r on the lattice (0 on Dirichlet nodes)
-//   f0 = log(kappa at the nodes), f1 = R f0, f2 = R f1          (computed once per problem)
-//   s_k = sigmoid(conv3(f_l; G_k) + b_k)                        (8 channels, per problem)
-//   h0 = conv3(x0; W0) * s0            (1 -> 8, level 0)
-//   h1 = conv3(R h0; W1) * s1          (8 -> 8, level 1)
-//   h2 = conv3(R h1; W2) * s2          (8 -> 8, level 2)
-//   v1 = conv3(P h2 + h1; W3) * s3     (8 -> 8, level 1)
-//   o  = conv3(P v1 + h0; W4)          (8 -> 1, level 0)
-//   z  = x0 + o  on the free nodes
-// R is full-weighting restriction (coarse node i <-> fine node 2i), P trilinear
-// prolongation (P = 8 R^T); conv3 is a 3x3x3 convolution with zero padding.  Training
+// An L-level (default 3), 8-channel convolutional network on the structured node
+// lattice, used in a form that is symmetric positive definite by construction:
+//   z = D^-1 r + D^-1/2 S^T S D^-1/2 r
+// S is a coefficient-gated encoder (features at every level):
+//   f_0 = log(kappa at the nodes), f_l = R f_{l-1}                 (once per problem)
+//   s_l = sigmoid(conv3(f_l; G_l) + b_l)                            (8 channels, per problem)
+//   x_0 = D^-1/2 r on the lattice (0 on Dirichlet nodes), x_l = R h_{l-1}
+//   h_l = conv3(x_l; W_l) * s_l                                     (1->8, then 8->8)
+//   S x_0 = (h_0, ..., h_{L-1})
+// and S^T is its exact adjoint (the decoder shares the encoder's weights: a U-net with
+// tied weights), so the learned term is positive semi-definite and plain (or flexible)
+// CG applies.  R is full-weighting restriction (coarse node i <-> fine node 2i), P = 8 R^T
+// trilinear prolongation, conv3 a 3x3x3 convolution with zero padding.  Training
 // minimises the relative A-norm error ||z - e||_A^2 / ||e||_A^2 over (residual, error)
 // pairs generated by the solver, with hand-written backward kernels and Adam.  All in
 // FP32; every reduction is two-stage in a fixed order (deterministic).
@@ -30,24 +30,6 @@ constexpr int kC = 8;          // channels
 constexpr int kTaps = 27;
 constexpr int kLT = 256;       // threads per block for lattice kernels
 constexpr int kTile = 8;       // weight-gradient tiles are 8^3 voxels
-
-// parameter layout (floats)
-struct NetLayout {
-  static constexpr int W0 = 0;                              // [8][1][27]
-  static constexpr int W1 = W0 + kC * kTaps;                // [8][8][27]
-  static constexpr int W2 = W1 + kC * kC * kTaps;
-  static constexpr int W3 = W2 + kC * kC * kTaps;
-  static constexpr int W4 = W3 + kC * kC * kTaps;           // [1][8][27]
-  static constexpr int G0 = W4 + kC * kTaps;                // [8][1][27] x 4 gates
-  static constexpr int G1 = G0 + kC * kTaps;
-  static constexpr int G2 = G1 + kC * kTaps;
-  static constexpr int G3 = G2 + kC * kTaps;
-  static constexpr int B0 = G3 + kC * kTaps;                // [8] x 4 gate biases
-  static constexpr int B1 = B0 + kC;
-  static constexpr int B2 = B1 + kC;
-  static constexpr int B3 = B2 + kC;
-  static constexpr int N = B3 + kC;
-};
 
 struct Dims {
   int n[3];
@@ -333,31 +315,63 @@ static inline unsigned nb_for(int64_t n) {
   return (unsigned)(b > 4096 ? 4096 : (b < 1 ? 1 : b));
 }
 
+
+// lattice[X] = sc[X] * v[gid(X)] (0 on Dirichlet nodes); v in gid order
+__global__ void k_to_lattice_scaled(int64_t nlat, const int32_t* __restrict__ node_gid, const float* __restrict__ v,
+                                    const float* __restrict__ sc, float* __restrict__ lat) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlat; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = node_gid[i];
+    lat[i] = g >= 0 ? sc[i] * v[g] : 0.f;
+  }
+}
+// dsq[X] = sqrt(dinv[gid(X)]) at free nodes, 0 elsewhere
+__global__ void k_dsqrt_lattice(int64_t nlat, const int32_t* __restrict__ node_gid, const float* __restrict__ dinv,
+                                float* __restrict__ dsq) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nlat; i += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t g = node_gid[i];
+    dsq[i] = g >= 0 ? sqrtf(dinv[g]) : 0.f;
+  }
+}
+// z[r] = dinv[r] v[r] + dsq[X_r] zl[X_r] over the owned rows
+__global__ void k_learned_out(int64_t n, const int32_t* __restrict__ row_node, const float* __restrict__ dinv,
+                              const float* __restrict__ v, const float* __restrict__ dsq, const float* __restrict__ zl,
+                              float* __restrict__ z) {
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int32_t X = row_node[r];
+    z[r] = dinv[r] * v[r] + dsq[X] * zl[X];
+  }
+}
+
 }  // namespace gd
 
 using namespace gd;
+
+constexpr int kMaxLevels = 6;
 
 // ---------------------------------------------------------------------------------
 // Network object
 // ---------------------------------------------------------------------------------
 struct gd_learned {
   gd_asm* A = nullptr;
-  Dims L[3];
-  int64_t nl[3] = {0, 0, 0};
+  int levels = 3;
+  Dims L[kMaxLevels];
+  int64_t nl[kMaxLevels] = {0};
+  int64_t nparams = 0;
+  int offW[kMaxLevels] = {0}, offG[kMaxLevels] = {0}, offB[kMaxLevels] = {0};
   DBuf<float> params, grads, adam_m, adam_v;
   int64_t adam_t = 0;
-  // per-problem static features and gates (8 channels per gate)
-  DBuf<float> f[3];
-  DBuf<float> s0, s1, s2, s3;   // gate values
+  DBuf<float> f[kMaxLevels], s[kMaxLevels];   // features (1 ch) and gates (8 ch)
+  DBuf<float> dsq;                            // lattice sqrt(D^-1) (0 on Dirichlet nodes)
+  // encoder caches of the two inputs used in training (path 0: D^-1/2 r, path 1: the
+  // loss gradient); the decoder and the backward pass use the scratch maps below
+  DBuf<float> x[2][kMaxLevels], a[2][kMaxLevels], h[2][kMaxLevels];
+  DBuf<float> u[kMaxLevels], gx[kMaxLevels], d[kMaxLevels], da[kMaxLevels], gp[kMaxLevels];
+  DBuf<float> zl;
+  DBuf<float> part;
+  DBuf<double> dred;
+  DBuf<float> zv, ev, dv, yv;
   bool prepared = false;
   int64_t prepared_epoch = -1;
-  // forward cache
-  DBuf<float> x0, h0a, h0, x1, h1a, h1, x2, h2a, h2, u1, v1a, v1, u0, o;
-  // backward scratch
-  DBuf<float> g0, g0b, gl1, gl1b, gl2, gl2b, gp0, gp1;
-  DBuf<float> part;   // weight-gradient partials
-  DBuf<double> dred;  // reductions for the loss
-  DBuf<float> zv, ev, dv, yv;   // gid-order vectors
 };
 
 namespace gd {
@@ -377,7 +391,7 @@ static int ntiles(const Dims& d) {
   return ((d.n[0] + kTile - 1) / kTile) * ((d.n[1] + kTile - 1) / kTile) * ((d.n[2] + kTile - 1) / kTile);
 }
 
-// dW += wgrad(in, g)
+// dW += wgrad(in, g); W has shape [co][ci][27]
 static int wgrad_launch(gd_learned* N, int ci, int co, const Dims& d, const float* in, const float* g, float* dW,
                         cudaStream_t st) {
   const int nt = ntiles(d);
@@ -385,7 +399,6 @@ static int wgrad_launch(gd_learned* N, int ci, int co, const Dims& d, const floa
   if (N->part.n < (size_t)nt * nw) GD_TRY(dalloc(N->part, (size_t)nt * nw));
   if (ci == 1 && co == 8) k_conv3_wgrad<1, 8><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
   else if (ci == 8 && co == 8) k_conv3_wgrad<8, 8><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
-  else if (ci == 8 && co == 1) k_conv3_wgrad<8, 1><<<nt, kLT, 0, st>>>(d, in, g, N->part.p);
   else return fail(GD_ERR_UNSUPPORTED, "learned: unsupported gradient shape");
   k_sum_partials<<<(nw + 127) / 128, 128, 0, st>>>(nt, nw, N->part.p, dW);
   GD_CUDA_TRY(cudaGetLastError());
@@ -401,7 +414,9 @@ static int bgrad_launch(gd_learned* N, const Dims& d, const float* g, float* dB,
   return GD_OK;
 }
 
-// static part: features and gates (after every numeric assembly)
+static inline int cin_of(int l) { return l == 0 ? 1 : kC; }
+
+// static part: features, gates and the diagonal scaling (after every numeric assembly)
 static int net_prepare(gd_learned* N, cudaStream_t st) {
   gd_asm* A = N->A;
   if (N->prepared && N->prepared_epoch == A->numeric_epoch) return GD_OK;
@@ -412,18 +427,16 @@ static int net_prepare(gd_learned* N, cudaStream_t st) {
   GD_TRY(dalloc(dn, 3));
   GD_CUDA_TRY(cudaMemcpyAsync(dn.p, hn, sizeof(hn), cudaMemcpyHostToDevice, st));
   const float* P = N->params.p;
+  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
   k_node_logk<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->L[0], dn.p, A->w_cells.p, 1.0 / A->mf_k2, N->f[0].p);
-  k_restrict<<<nb_for(N->nl[1]), kLT, 0, st>>>(1, N->L[0], N->L[1], N->f[0].p, N->f[1].p, 1.f);
-  k_restrict<<<nb_for(N->nl[2]), kLT, 0, st>>>(1, N->L[1], N->L[2], N->f[1].p, N->f[2].p, 1.f);
+  for (int l = 1; l < N->levels; ++l)
+    k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(1, N->L[l - 1], N->L[l], N->f[l - 1].p, N->f[l].p, 1.f);
   GD_CUDA_TRY(cudaGetLastError());
-  GD_TRY(conv_launch(1, 8, N->L[0], N->f[0].p, P + NetLayout::G0, nullptr, P + NetLayout::B0, N->s0.p, 0, 0, st));
-  GD_TRY(conv_launch(1, 8, N->L[1], N->f[1].p, P + NetLayout::G1, nullptr, P + NetLayout::B1, N->s1.p, 0, 0, st));
-  GD_TRY(conv_launch(1, 8, N->L[2], N->f[2].p, P + NetLayout::G2, nullptr, P + NetLayout::B2, N->s2.p, 0, 0, st));
-  GD_TRY(conv_launch(1, 8, N->L[1], N->f[1].p, P + NetLayout::G3, nullptr, P + NetLayout::B3, N->s3.p, 0, 0, st));
-  k_sigmoid<<<nb_for(kC * N->nl[0]), kLT, 0, st>>>(kC * N->nl[0], N->s0.p);
-  k_sigmoid<<<nb_for(kC * N->nl[1]), kLT, 0, st>>>(kC * N->nl[1], N->s1.p);
-  k_sigmoid<<<nb_for(kC * N->nl[2]), kLT, 0, st>>>(kC * N->nl[2], N->s2.p);
-  k_sigmoid<<<nb_for(kC * N->nl[1]), kLT, 0, st>>>(kC * N->nl[1], N->s3.p);
+  for (int l = 0; l < N->levels; ++l) {
+    GD_TRY(conv_launch(1, 8, N->L[l], N->f[l].p, P + N->offG[l], nullptr, P + N->offB[l], N->s[l].p, 0, 0, st));
+    k_sigmoid<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->s[l].p);
+  }
+  k_dsqrt_lattice<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, dinv, N->dsq.p);
   GD_CUDA_TRY(cudaGetLastError());
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   dfreeb(dn);
@@ -432,82 +445,84 @@ static int net_prepare(gd_learned* N, cudaStream_t st) {
   return GD_OK;
 }
 
-// forward: r (gid order, FP32) -> z (gid order); keeps activations for backward
-static int net_forward(gd_learned* N, const float* r, float* z, cudaStream_t st) {
-  gd_asm* A = N->A;
+// encoder of path p on the lattice input x[p][0]: h[p][l] = conv(x_l; W_l) * s_l
+static int net_encode(gd_learned* N, int p, cudaStream_t st) {
   const float* P = N->params.p;
-  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
-  const Dims *L = N->L;
-  const int64_t* nl = N->nl;
-  k_to_lattice<<<nb_for(nl[0]), kLT, 0, st>>>(nl[0], A->mx.node_gid.p, r, dinv, N->x0.p);
-  GD_TRY(conv_launch(1, 8, L[0], N->x0.p, P + NetLayout::W0, nullptr, nullptr, N->h0a.p, 0, 0, st));
-  k_mul<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->h0a.p, N->s0.p, N->h0.p);
-  k_restrict<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[0], L[1], N->h0.p, N->x1.p, 1.f);
-  GD_TRY(conv_launch(8, 8, L[1], N->x1.p, P + NetLayout::W1, nullptr, nullptr, N->h1a.p, 0, 0, st));
-  k_mul<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->h1a.p, N->s1.p, N->h1.p);
-  k_restrict<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC, L[1], L[2], N->h1.p, N->x2.p, 1.f);
-  GD_TRY(conv_launch(8, 8, L[2], N->x2.p, P + NetLayout::W2, nullptr, nullptr, N->h2a.p, 0, 0, st));
-  k_mul<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC * nl[2], N->h2a.p, N->s2.p, N->h2.p);
-  k_copyf<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->h1.p, N->u1.p);
-  k_prolong<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[2], L[1], N->h2.p, N->u1.p, 1.f, 1);
-  GD_TRY(conv_launch(8, 8, L[1], N->u1.p, P + NetLayout::W3, nullptr, nullptr, N->v1a.p, 0, 0, st));
-  k_mul<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->v1a.p, N->s3.p, N->v1.p);
-  k_copyf<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->h0.p, N->u0.p);
-  k_prolong<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC, L[1], L[0], N->v1.p, N->u0.p, 1.f, 1);
-  GD_TRY(conv_launch(8, 1, L[0], N->u0.p, P + NetLayout::W4, nullptr, nullptr, N->o.p, 0, 0, st));
-  k_from_lattice<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, N->x0.p, N->o.p, z);
+  for (int l = 0; l < N->levels; ++l) {
+    if (l > 0)
+      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[p][l - 1].p, N->x[p][l].p,
+                                                        1.f);
+    GD_TRY(conv_launch(cin_of(l), kC, N->L[l], N->x[p][l].p, P + N->offW[l], nullptr, nullptr, N->a[p][l].p, 0, 0, st));
+    k_mul<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->a[p][l].p, N->s[l].p, N->h[p][l].p);
+  }
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
 
-// backward of the loss gradient gz (gid order) into N->grads (accumulated)
-static int net_backward(gd_learned* N, const float* gz, cudaStream_t st) {
-  gd_asm* A = N->A;
+// decoder: zl = S^T (h[p][0..L-1])  (the adjoint of the encoder, summed over levels)
+static int net_decode(gd_learned* N, int p, cudaStream_t st) {
+  const float* P = N->params.p;
+  const int Lv = N->levels;
+  k_copyf<<<nb_for(kC * N->nl[Lv - 1]), kLT, 0, st>>>(kC * N->nl[Lv - 1], N->h[p][Lv - 1].p, N->u[Lv - 1].p);
+  for (int l = Lv - 1; l >= 0; --l) {
+    k_mul<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->u[l].p, N->s[l].p, N->da[l].p);
+    float* out = l == 0 ? N->zl.p : N->gx[l].p;
+    GD_TRY(conv_launch(kC, cin_of(l), N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, out, 1, 0, st));
+    if (l > 0) {
+      k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[p][l - 1].p, N->u[l - 1].p);
+      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->u[l - 1].p,
+                                                           0.125f, 1);
+    }
+  }
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// backward of the encoder of path p with cotangents (h[q][l]) at every level; accumulates
+// W, G, b gradients
+static int net_encoder_backward(gd_learned* N, int p, int q, cudaStream_t st) {
   const float* P = N->params.p;
   float* G = N->grads.p;
-  const Dims* L = N->L;
-  const int64_t* nl = N->nl;
-  // grad o on the lattice (o only reaches the free nodes)
-  k_to_lattice<<<nb_for(nl[0]), kLT, 0, st>>>(nl[0], A->mx.node_gid.p, gz, nullptr, N->g0b.p);   // 1 channel
-  // o = conv(u0; W4)
-  GD_TRY(wgrad_launch(N, 8, 1, L[0], N->u0.p, N->g0b.p, G + NetLayout::W4, st));
-  GD_TRY(conv_launch(1, 8, L[0], N->g0b.p, P + NetLayout::W4, nullptr, nullptr, N->g0.p, 1, 0, st));   // g u0
-  // u0 = h0 + P v1  ->  g h0 = g u0 (kept in g0), g v1 = 8 R(g u0)
-  k_restrict<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[0], L[1], N->g0.p, N->gl1.p, 8.f);
-  // v1 = v1a * s3
-  k_gate_bwd<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->gl1.p, N->v1a.p, N->s3.p, N->gl1b.p, N->gp1.p);
-  GD_TRY(wgrad_launch(N, 1, 8, L[1], N->f[1].p, N->gp1.p, G + NetLayout::G3, st));
-  GD_TRY(bgrad_launch(N, L[1], N->gp1.p, G + NetLayout::B3, st));
-  // v1a = conv(u1; W3)
-  GD_TRY(wgrad_launch(N, 8, 8, L[1], N->u1.p, N->gl1b.p, G + NetLayout::W3, st));
-  GD_TRY(conv_launch(8, 8, L[1], N->gl1b.p, P + NetLayout::W3, nullptr, nullptr, N->gl1.p, 1, 0, st));   // g u1
-  // u1 = h1 + P h2 -> g h2 = 8 R(g u1); g h1 = g u1 (+ from x2 = R h1 below)
-  k_restrict<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC, L[1], L[2], N->gl1.p, N->gl2.p, 8.f);
-  // h2 = h2a * s2
-  k_gate_bwd<<<nb_for(kC * nl[2]), kLT, 0, st>>>(kC * nl[2], N->gl2.p, N->h2a.p, N->s2.p, N->gl2b.p, N->gp1.p);
-  GD_TRY(wgrad_launch(N, 1, 8, L[2], N->f[2].p, N->gp1.p, G + NetLayout::G2, st));
-  GD_TRY(bgrad_launch(N, L[2], N->gp1.p, G + NetLayout::B2, st));
-  // h2a = conv(x2; W2)
-  GD_TRY(wgrad_launch(N, 8, 8, L[2], N->x2.p, N->gl2b.p, G + NetLayout::W2, st));
-  GD_TRY(conv_launch(8, 8, L[2], N->gl2b.p, P + NetLayout::W2, nullptr, nullptr, N->gl2.p, 1, 0, st));   // g x2
-  // x2 = R h1 -> g h1 += (1/8) P(g x2)
-  k_prolong<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC, L[2], L[1], N->gl2.p, N->gl1.p, 0.125f, 1);
-  // h1 = h1a * s1
-  k_gate_bwd<<<nb_for(kC * nl[1]), kLT, 0, st>>>(kC * nl[1], N->gl1.p, N->h1a.p, N->s1.p, N->gl1b.p, N->gp1.p);
-  GD_TRY(wgrad_launch(N, 1, 8, L[1], N->f[1].p, N->gp1.p, G + NetLayout::G1, st));
-  GD_TRY(bgrad_launch(N, L[1], N->gp1.p, G + NetLayout::B1, st));
-  // h1a = conv(x1; W1)
-  GD_TRY(wgrad_launch(N, 8, 8, L[1], N->x1.p, N->gl1b.p, G + NetLayout::W1, st));
-  GD_TRY(conv_launch(8, 8, L[1], N->gl1b.p, P + NetLayout::W1, nullptr, nullptr, N->gl1.p, 1, 0, st));   // g x1
-  // x1 = R h0 -> g h0 += (1/8) P(g x1)
-  k_prolong<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC, L[1], L[0], N->gl1.p, N->g0.p, 0.125f, 1);
-  // h0 = h0a * s0  (u0 is free again: its last use was the W4 gradient above)
-  k_gate_bwd<<<nb_for(kC * nl[0]), kLT, 0, st>>>(kC * nl[0], N->g0.p, N->h0a.p, N->s0.p, N->u0.p, N->gp0.p);
-  GD_TRY(wgrad_launch(N, 1, 8, L[0], N->f[0].p, N->gp0.p, G + NetLayout::G0, st));
-  GD_TRY(bgrad_launch(N, L[0], N->gp0.p, G + NetLayout::B0, st));
-  // h0a = conv(x0; W0)
-  GD_TRY(wgrad_launch(N, 1, 8, L[0], N->x0.p, N->u0.p, G + NetLayout::W0, st));
+  const int Lv = N->levels;
+  k_copyf<<<nb_for(kC * N->nl[Lv - 1]), kLT, 0, st>>>(kC * N->nl[Lv - 1], N->h[q][Lv - 1].p, N->d[Lv - 1].p);
+  for (int l = Lv - 1; l >= 0; --l) {
+    const int64_t m = kC * N->nl[l];
+    k_gate_bwd<<<nb_for(m), kLT, 0, st>>>(m, N->d[l].p, N->a[p][l].p, N->s[l].p, N->da[l].p, N->gp[l].p);
+    GD_TRY(wgrad_launch(N, 1, kC, N->L[l], N->f[l].p, N->gp[l].p, G + N->offG[l], st));
+    GD_TRY(bgrad_launch(N, N->L[l], N->gp[l].p, G + N->offB[l], st));
+    GD_TRY(wgrad_launch(N, cin_of(l), kC, N->L[l], N->x[p][l].p, N->da[l].p, G + N->offW[l], st));
+    if (l > 0) {
+      GD_TRY(conv_launch(kC, kC, N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, N->gx[l].p, 1, 0, st));
+      k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[q][l - 1].p, N->d[l - 1].p);
+      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->d[l - 1].p,
+                                                           0.125f, 1);
+    }
+  }
   GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// z = D^-1 r + D^-1/2 S^T S D^-1/2 r  (r, z in gid order); keeps the path-0 encoder cache
+static int net_forward(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
+  k_to_lattice_scaled<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, r, N->dsq.p, N->x[0][0].p);
+  GD_TRY(net_encode(N, 0, st));
+  GD_TRY(net_decode(N, 0, st));
+  k_learned_out<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, dinv, r, N->dsq.p, N->zl.p, z);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// parameter gradient of <gz, z(r)> (gz = dL/dz in gid order), accumulated into grads
+static int net_backward(gd_learned* N, const float* gz, cudaStream_t st) {
+  gd_asm* A = N->A;
+  // path 1 input: D^-1/2 gz on the lattice
+  k_to_lattice_scaled<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, gz, N->dsq.p, N->x[1][0].p);
+  GD_TRY(net_encode(N, 1, st));
+  // d<g, S^T S x> = <S g, dS x> + <S x, dS g>
+  GD_TRY(net_encoder_backward(N, 0, 1, st));
+  GD_TRY(net_encoder_backward(N, 1, 0, st));
   return GD_OK;
 }
 
@@ -518,7 +533,7 @@ static int net_loss(gd_learned* N, const float* z, const float* e, double* loss,
   double* red = N->dred.p;   // [0..1023] partials, [2048] eAe, [2049] dAd
   k_axmb<<<nb_for(n), kLT, 0, st>>>(n, 1.f, z, e, N->dv.p);
   GD_TRY(mixed_apply(A, N->dv.p, N->yv.p, red, st));   // yv = A d, partial d.Ad
-  int nbm = (int)std::min<int64_t>((n + 255) / 256, 1024);
+  const int nbm = (int)std::min<int64_t>((n + 255) / 256, 1024);
   k_sum_d<<<1, kLT, 0, st>>>(nbm, red, red + 2049);
   GD_TRY(mixed_apply(A, e, N->zv.p, red, st));         // partial e.Ae
   k_sum_d<<<1, kLT, 0, st>>>(nbm, red, red + 2048);
@@ -544,18 +559,33 @@ static int apply_as_precond(void* ctx, gd_asm* A, const float* r, float* z, cuda
 // ---------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------
-extern "C" int gd_learned_create(gd_asm* A, uint64_t seed, gd_learned** out) {
+extern "C" int gd_learned_create(gd_asm* A, int levels, uint64_t seed, gd_learned** out) {
   if (!A || !out) return fail(GD_ERR_ARG, "gd_learned_create: null argument");
+  if (levels < 1 || levels > kMaxLevels) return fail(GD_ERR_ARG, "gd_learned_create: levels must be 1..6");
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_learned_create: assemble the system first");
   if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3))
     return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells");
   gd_learned* N = new gd_learned();
   N->A = A;
+  N->levels = levels;
   const Geom& g = A->test->geom;
   for (int d = 0; d < 3; ++d) N->L[0].n[d] = (int)g.N[d];
-  N->L[1] = coarse_dims(N->L[0]);
-  N->L[2] = coarse_dims(N->L[1]);
-  for (int l = 0; l < 3; ++l) N->nl[l] = N->L[l].size();
+  for (int l = 1; l < levels; ++l) N->L[l] = coarse_dims(N->L[l - 1]);
+  for (int l = 0; l < levels; ++l) N->nl[l] = N->L[l].size();
+  int off = 0;
+  for (int l = 0; l < levels; ++l) {
+    N->offW[l] = off;
+    off += kC * cin_of(l) * kTaps;
+  }
+  for (int l = 0; l < levels; ++l) {
+    N->offG[l] = off;
+    off += kC * kTaps;
+  }
+  for (int l = 0; l < levels; ++l) {
+    N->offB[l] = off;
+    off += kC;
+  }
+  N->nparams = off;
   auto fail_clean = [&](int s) {
     std::string msg = gd_last_error();
     gd_learned_destroy(N);
@@ -564,64 +594,49 @@ extern "C" int gd_learned_create(gd_asm* A, uint64_t seed, gd_learned** out) {
   int s = GD_OK;
 #define ALLOC(buf, count) \
   if ((s = dalloc(buf, (size_t)(count))) != GD_OK) return fail_clean(s);
-  ALLOC(N->params, NetLayout::N);
-  ALLOC(N->grads, NetLayout::N);
-  ALLOC(N->adam_m, NetLayout::N);
-  ALLOC(N->adam_v, NetLayout::N);
-  for (int l = 0; l < 3; ++l) ALLOC(N->f[l], N->nl[l]);
-  ALLOC(N->s0, kC * N->nl[0]);
-  ALLOC(N->s1, kC * N->nl[1]);
-  ALLOC(N->s2, kC * N->nl[2]);
-  ALLOC(N->s3, kC * N->nl[1]);
-  ALLOC(N->x0, N->nl[0]);
-  ALLOC(N->h0a, kC * N->nl[0]);
-  ALLOC(N->h0, kC * N->nl[0]);
-  ALLOC(N->x1, kC * N->nl[1]);
-  ALLOC(N->h1a, kC * N->nl[1]);
-  ALLOC(N->h1, kC * N->nl[1]);
-  ALLOC(N->x2, kC * N->nl[2]);
-  ALLOC(N->h2a, kC * N->nl[2]);
-  ALLOC(N->h2, kC * N->nl[2]);
-  ALLOC(N->u1, kC * N->nl[1]);
-  ALLOC(N->v1a, kC * N->nl[1]);
-  ALLOC(N->v1, kC * N->nl[1]);
-  ALLOC(N->u0, kC * N->nl[0]);
-  ALLOC(N->o, N->nl[0]);
-  ALLOC(N->g0, kC * N->nl[0]);
-  ALLOC(N->g0b, kC * N->nl[0]);
-  ALLOC(N->gp0, kC * N->nl[0]);
-  ALLOC(N->gl1, kC * N->nl[1]);
-  ALLOC(N->gl1b, kC * N->nl[1]);
-  ALLOC(N->gp1, kC * N->nl[1]);
-  ALLOC(N->gl2, kC * N->nl[2]);
-  ALLOC(N->gl2b, kC * N->nl[2]);
+  ALLOC(N->params, N->nparams);
+  ALLOC(N->grads, N->nparams);
+  ALLOC(N->adam_m, N->nparams);
+  ALLOC(N->adam_v, N->nparams);
+  ALLOC(N->dsq, N->nl[0]);
+  ALLOC(N->zl, N->nl[0]);
+  for (int l = 0; l < levels; ++l) {
+    ALLOC(N->f[l], N->nl[l]);
+    ALLOC(N->s[l], kC * N->nl[l]);
+    for (int p = 0; p < 2; ++p) {
+      ALLOC(N->x[p][l], cin_of(l) * N->nl[l]);
+      ALLOC(N->a[p][l], kC * N->nl[l]);
+      ALLOC(N->h[p][l], kC * N->nl[l]);
+    }
+    ALLOC(N->u[l], kC * N->nl[l]);
+    ALLOC(N->gx[l], kC * N->nl[l]);
+    ALLOC(N->d[l], kC * N->nl[l]);
+    ALLOC(N->da[l], kC * N->nl[l]);
+    ALLOC(N->gp[l], kC * N->nl[l]);
+  }
   ALLOC(N->dred, 4096);
   ALLOC(N->zv, A->ngdofs);
   ALLOC(N->ev, A->ngdofs);
   ALLOC(N->dv, A->ngdofs);
   ALLOC(N->yv, A->ngdofs);
 #undef ALLOC
-  // deterministic initialisation: small convolutions (the network starts close to Jacobi),
-  // gates at 0.5
-  std::vector<float> p(NetLayout::N, 0.f);
-  uint64_t st = seed * 6364136223846793005ull + 1442695040888963407ull;
+  // deterministic initialisation: small convolutions (the network starts close to
+  // Jacobi), gates at 0.5
+  std::vector<float> p(N->nparams, 0.f);
+  uint64_t rs = seed * 6364136223846793005ull + 1442695040888963407ull;
   auto rnd = [&]() {   // uniform in (-1, 1), 64-bit LCG
-    st = st * 6364136223846793005ull + 1442695040888963407ull;
-    return (float)((double)(st >> 11) / 9007199254740992.0 * 2.0 - 1.0);
+    rs = rs * 6364136223846793005ull + 1442695040888963407ull;
+    return (float)((double)(rs >> 11) / 9007199254740992.0 * 2.0 - 1.0);
   };
-  auto fill = [&](int off, int count, float scale) {
-    for (int i = 0; i < count; ++i) p[off + i] = scale * rnd();
-  };
-  fill(NetLayout::W0, kC * kTaps, 0.2f);
-  fill(NetLayout::W1, kC * kC * kTaps, 0.05f);
-  fill(NetLayout::W2, kC * kC * kTaps, 0.05f);
-  fill(NetLayout::W3, kC * kC * kTaps, 0.05f);
-  fill(NetLayout::W4, kC * kTaps, 0.02f);
-  fill(NetLayout::G0, 4 * kC * kTaps, 0.05f);
+  for (int l = 0; l < levels; ++l) {
+    const int nw = kC * cin_of(l) * kTaps;
+    for (int i = 0; i < nw; ++i) p[N->offW[l] + i] = 0.05f * rnd();
+    for (int i = 0; i < kC * kTaps; ++i) p[N->offG[l] + i] = 0.05f * rnd();
+  }
   cudaStream_t cs = A->test->model->ctx->stream;
-  cudaError_t e = cudaMemcpyAsync(N->params.p, p.data(), sizeof(float) * NetLayout::N, cudaMemcpyHostToDevice, cs);
-  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_m.p, 0, sizeof(float) * NetLayout::N, cs);
-  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_v.p, 0, sizeof(float) * NetLayout::N, cs);
+  cudaError_t e = cudaMemcpyAsync(N->params.p, p.data(), sizeof(float) * N->nparams, cudaMemcpyHostToDevice, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_m.p, 0, sizeof(float) * N->nparams, cs);
+  if (e == cudaSuccess) e = cudaMemsetAsync(N->adam_v.p, 0, sizeof(float) * N->nparams, cs);
   if (e == cudaSuccess) e = cudaStreamSynchronize(cs);
   if (e != cudaSuccess) {
     fail(GD_ERR_CUDA, std::string("gd_learned_create: ") + cudaGetErrorString(e));
@@ -633,26 +648,52 @@ extern "C" int gd_learned_create(gd_asm* A, uint64_t seed, gd_learned** out) {
 
 extern "C" int gd_learned_destroy(gd_learned* N) {
   if (!N) return GD_OK;
-  DBuf<float>* bufs[] = {&N->params, &N->grads, &N->adam_m, &N->adam_v, &N->f[0], &N->f[1], &N->f[2], &N->s0,
-                         &N->s1, &N->s2, &N->s3, &N->x0, &N->h0a, &N->h0, &N->x1, &N->h1a, &N->h1, &N->x2,
-                         &N->h2a, &N->h2, &N->u1, &N->v1a, &N->v1, &N->u0, &N->o, &N->g0, &N->g0b, &N->gp0,
-                         &N->gl1, &N->gl1b, &N->gp1, &N->gl2, &N->gl2b, &N->part, &N->zv, &N->ev, &N->dv, &N->yv};
-  for (auto* b : bufs) dfreeb(*b);
+  dfreeb(N->params);
+  dfreeb(N->grads);
+  dfreeb(N->adam_m);
+  dfreeb(N->adam_v);
+  dfreeb(N->dsq);
+  dfreeb(N->zl);
+  for (int l = 0; l < kMaxLevels; ++l) {
+    dfreeb(N->f[l]);
+    dfreeb(N->s[l]);
+    for (int p = 0; p < 2; ++p) {
+      dfreeb(N->x[p][l]);
+      dfreeb(N->a[p][l]);
+      dfreeb(N->h[p][l]);
+    }
+    dfreeb(N->u[l]);
+    dfreeb(N->gx[l]);
+    dfreeb(N->d[l]);
+    dfreeb(N->da[l]);
+    dfreeb(N->gp[l]);
+  }
+  dfreeb(N->part);
   dfreeb(N->dred);
+  dfreeb(N->zv);
+  dfreeb(N->ev);
+  dfreeb(N->dv);
+  dfreeb(N->yv);
   delete N;
   return GD_OK;
 }
 
 extern "C" int gd_learned_num_params(const gd_learned* N, int64_t* n) {
   if (!N || !n) return fail(GD_ERR_ARG, "gd_learned_num_params: null argument");
-  *n = NetLayout::N;
+  *n = N->nparams;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_levels(const gd_learned* N, int32_t* levels) {
+  if (!N || !levels) return fail(GD_ERR_ARG, "gd_learned_levels: null argument");
+  *levels = N->levels;
   return GD_OK;
 }
 
 extern "C" int gd_learned_get_params(const gd_learned* N, float* host) {
   if (!N || !host) return fail(GD_ERR_ARG, "gd_learned_get_params: null argument");
   cudaStream_t st = N->A->test->model->ctx->stream;
-  GD_CUDA_TRY(cudaMemcpyAsync(host, N->params.p, sizeof(float) * NetLayout::N, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(host, N->params.p, sizeof(float) * N->nparams, cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   return GD_OK;
 }
@@ -660,7 +701,7 @@ extern "C" int gd_learned_get_params(const gd_learned* N, float* host) {
 extern "C" int gd_learned_set_params(gd_learned* N, const float* host) {
   if (!N || !host) return fail(GD_ERR_ARG, "gd_learned_set_params: null argument");
   cudaStream_t st = N->A->test->model->ctx->stream;
-  GD_CUDA_TRY(cudaMemcpyAsync(N->params.p, host, sizeof(float) * NetLayout::N, cudaMemcpyHostToDevice, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(N->params.p, host, sizeof(float) * N->nparams, cudaMemcpyHostToDevice, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   N->prepared = false;
   return GD_OK;
@@ -681,8 +722,8 @@ extern "C" int gd_learned_gradient(gd_learned* N, const float* r, const float* e
   cudaStream_t st = N->A->test->model->ctx->stream;
   const int64_t n = N->A->ngdofs;
   GD_TRY(net_prepare(N, st));
-  N->prepared = false;   // gate caches are rebuilt after the parameters change
-  GD_CUDA_TRY(cudaMemsetAsync(N->grads.p, 0, sizeof(float) * NetLayout::N, st));
+  N->prepared = false;   // gates are rebuilt once the parameters change
+  GD_CUDA_TRY(cudaMemsetAsync(N->grads.p, 0, sizeof(float) * N->nparams, st));
   double total = 0.0;
   for (int b = 0; b < batch; ++b) {
     GD_TRY(net_forward(N, r + b * n, N->zv.p, st));
@@ -693,7 +734,7 @@ extern "C" int gd_learned_gradient(gd_learned* N, const float* r, const float* e
   }
   *loss = total / batch;
   if (grads_host) {
-    GD_CUDA_TRY(cudaMemcpyAsync(grads_host, N->grads.p, sizeof(float) * NetLayout::N, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaMemcpyAsync(grads_host, N->grads.p, sizeof(float) * N->nparams, cudaMemcpyDeviceToHost, st));
     GD_CUDA_TRY(cudaStreamSynchronize(st));
   }
   return GD_OK;
@@ -706,8 +747,9 @@ extern "C" int gd_learned_train_step(gd_learned* N, const float* r, const float*
   ++N->adam_t;
   const float b1 = 0.9f, b2 = 0.999f;
   const float c1 = 1.f - std::pow(b1, (float)N->adam_t), c2 = 1.f - std::pow(b2, (float)N->adam_t);
-  k_adam<<<(NetLayout::N + 255) / 256, 256, 0, st>>>(NetLayout::N, N->params.p, N->grads.p, N->adam_m.p, N->adam_v.p,
-                                                     lr, b1, b2, 1e-8f, c1, c2, 1.f / batch);
+  k_adam<<<(unsigned)((N->nparams + 255) / 256), 256, 0, st>>>((int)N->nparams, N->params.p, N->grads.p,
+                                                                N->adam_m.p, N->adam_v.p, lr, b1, b2, 1e-8f, c1, c2,
+                                                                1.f / batch);
   GD_CUDA_TRY(cudaGetLastError());
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   N->prepared = false;
@@ -715,7 +757,8 @@ extern "C" int gd_learned_train_step(gd_learned* N, const float* r, const float*
 }
 
 // Mixed-precision flexible CG with the network as preconditioner; Jacobi-PCG (same
-// refinement) is the fallback when the learned iteration stalls or does not converge.
+// refinement) is the fallback when the learned iteration stagnates (64 inner iterations
+// without halving the residual), goes non-finite or does not converge.
 extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit, double* x, int where,
                                 gd_solve_stats* stats, int32_t* fallback_used) {
   if (!A || !N || N->A != A || !x) return fail(GD_ERR_ARG, "gd_solve_learned: bad argument");
@@ -726,7 +769,7 @@ extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit
   if (fallback_used) *fallback_used = 0;
   gd_solve_stats s1{};
   int rc = mixed_solve(A, rtol, maxit, x, where, &s1, &pc);
-  if (rc == GD_ERR_STALL || rc == GD_ERR_NOTCONVERGED) {
+  if (rc == GD_ERR_STALL || rc == GD_ERR_NOTCONVERGED || rc == GD_ERR_NUMERIC) {
     gd_solve_stats s2{};
     rc = mixed_solve(A, rtol, maxit, x, where, &s2, nullptr);
     if (fallback_used) *fallback_used = 1;

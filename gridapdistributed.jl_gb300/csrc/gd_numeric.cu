@@ -260,6 +260,97 @@ k_numeric_matrix(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, 
   }
 }
 
+// ---- Q_k (k >= 2) values: one warp per owned row -------------------------------------------
+// The row's node X and the coefficients of the (up to 2^DIM) cells around it are decoded
+// once per warp; the lanes then walk the row's entries (coalesced stencil codes in,
+// coalesced values out).  Along each direction the node sits either on a cell boundary
+// (X % K == 0: cells "below" = slot 0 and "above" = slot 1) or inside one cell (slot 1);
+// entry (X, X+o) sums kappa_c * Khat[X in c][X+o in c] over the slots whose cell holds
+// both nodes: o_d < 0 -> slot 0, o_d > 0 -> slot 1, o_d = 0 -> both.
+template <int DIM, int K, typename CodeT>
+__global__ void __launch_bounds__(256)
+k_numeric_qk_rows(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
+                  const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
+                  double* __restrict__ vals) {
+  using L = Lat<DIM, K>;
+  constexpr int NC = 1 << DIM;
+  __shared__ double s_K[L::NN * L::NN];
+  for (int i = threadIdx.x; i < L::NN * L::NN; i += blockDim.x) s_K[i] = Khat[i];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
+  for (int64_t r = warp; r < nrows_own; r += nwarps) {
+    const uint32_t lin = (uint32_t)row_node[r];
+    int X[3], q[3], rm[3];
+    X[0] = (int)(lin % N0);
+    if (DIM == 3) {
+      const uint32_t t = lin / N0;
+      X[1] = (int)(t % N1);
+      X[2] = (int)(t / N1);
+    } else {
+      X[1] = (int)(lin / N0);
+      X[2] = 0;
+    }
+#pragma unroll
+    for (int d = 0; d < DIM; ++d) {
+      q[d] = X[d] / K;
+      rm[d] = X[d] % K;
+    }
+    // coefficient of slot a (lane a loads it, then broadcast)
+    double kv = 0.0;
+    bool slot_ok = false;
+    if (lane < NC) {
+      bool ok = true;
+      int64_t cl = 0, stride = 1;
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        const int sd = (lane >> d) & 1;
+        const int c = sd ? q[d] : q[d] - 1;
+        if (!sd && rm[d] != 0) ok = false;
+        if (c < 0 || c >= g.n[d]) ok = false;
+        cl += stride * c;
+        stride *= g.n[d];
+      }
+      kv = ok ? __ldg(kappa + cl) : 0.0;
+      slot_ok = ok;
+    }
+    const uint32_t vmask = __ballot_sync(0xffffffffu, slot_ok);   // valid slots (integer test, not FP64)
+    double kap[NC];
+#pragma unroll
+    for (int a = 0; a < NC; ++a) kap[a] = __shfl_sync(0xffffffffu, kv, a);
+    const int64_t e0 = rowptr[r], e1 = rowptr[r + 1];
+    for (int64_t e = e0 + lane; e < e1; e += 32) {
+      int cv = (int)code[e];
+      int o[3] = {0, 0, 0};
+#pragma unroll
+      for (int d = 0; d < DIM; ++d) {
+        o[d] = cv % L::W - K;
+        cv /= L::W;
+      }
+      double v = 0.0;
+#pragma unroll
+      for (int a = 0; a < NC; ++a) {
+        bool ok = (vmask >> a) & 1u;
+        int lx = 0, ly = 0, mul = 1;
+#pragma unroll
+        for (int d = 0; d < DIM; ++d) {
+          const int sd = (a >> d) & 1;
+          if (sd == 0 && (rm[d] != 0 || o[d] > 0)) ok = false;
+          if (sd == 1 && rm[d] == 0 && o[d] < 0) ok = false;
+          const int lxd = sd ? rm[d] : K;
+          lx += mul * lxd;
+          ly += mul * (lxd + o[d]);
+          mul *= L::KP1;
+        }
+        if (ok) v = fma(kap[a], s_K[lx * L::NN + ly], v);
+      }
+      vals[e] = v;
+    }
+  }
+}
+
 // ---- right-hand side: f-term and Dirichlet lifting, one thread per owned row -----------
 template <int DIM, int K>
 __global__ void k_numeric_rhs(Geom g, int64_t nrows_own, const int32_t* __restrict__ row_node,
@@ -832,13 +923,15 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   if (R == 0) return GD_OK;
   const unsigned nb = (unsigned)((R + kRowsPerBlock - 1) / kRowsPerBlock);
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
+  (void)nb;
+  // one warp per row; grid sized for a few waves of resident blocks
+  const unsigned nbw = (unsigned)std::min<int64_t>((R + 7) / 8, 152 * 64);
   if (A->code_bytes == 1)
-    k_numeric_matrix<DIM, K, uint8_t><<<nb, kNumericThreads, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, A->code.p,
-                                                                       kappa, A->Khat.p, A->vals.p);
+    k_numeric_qk_rows<DIM, K, uint8_t><<<nbw, 256, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, A->code.p, kappa,
+                                                            A->Khat.p, A->vals.p);
   else
-    k_numeric_matrix<DIM, K, uint16_t><<<nb, kNumericThreads, 0, st>>>(g, R, A->rowptr.p, A->row_node.p,
-                                                                        (const uint16_t*)A->code.p, kappa,
-                                                                        A->Khat.p, A->vals.p);
+    k_numeric_qk_rows<DIM, K, uint16_t><<<nbw, 256, 0, st>>>(g, R, A->rowptr.p, A->row_node.p,
+                                                             (const uint16_t*)A->code.p, kappa, A->Khat.p, A->vals.p);
   GD_CUDA_TRY(cudaGetLastError());
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;

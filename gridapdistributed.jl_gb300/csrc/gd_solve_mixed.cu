@@ -407,6 +407,11 @@ int mixed_solve(gd_asm* A, double rtol, int maxit, double* x_out, int where, gd_
     int it = 0;
     const int batch = 16;
     const int inner_max = maxit - total_inner;
+    // external preconditioner: give up when 64 iterations do not halve the inner
+    // residual, so a weak preconditioner hands over to Jacobi early
+    bool inner_stall = false;
+    double check_res = 1.0;
+    int check_it = 0;
     while (it < inner_max) {
       const int nstep = std::min(batch, inner_max - it);
       for (int s = 0; s < nstep; ++s) {
@@ -427,10 +432,25 @@ int mixed_solve(gd_asm* A, double rtol, int maxit, double* x_out, int where, gd_
       it += nstep;
       GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(h), cudaMemcpyDeviceToHost, st));
       GD_CUDA_TRY(cudaStreamSynchronize(st));
-      if (!std::isfinite(h.rr)) break;
+      if (!std::isfinite(h.rr)) {
+        inner_stall = ext;
+        break;
+      }
       if (std::sqrt(h.rr) <= tol_in) break;
+      if (ext && it - check_it >= 64) {
+        if (std::sqrt(h.rr) > 0.5 * check_res) {
+          inner_stall = true;
+          break;
+        }
+        check_res = std::sqrt(h.rr);
+        check_it = it;
+      }
     }
     total_inner += it;
+    if (inner_stall) {
+      status = fail(GD_ERR_STALL, "mixed solve: preconditioned inner iteration stagnated");
+      break;
+    }
     k_mx_accumulate<<<gb, kMxThreads, 0, st>>>(n, rnorm, x, x64);
     GD_CUDA_TRY(cudaGetLastError());
   }

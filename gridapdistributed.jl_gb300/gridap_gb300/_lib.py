@@ -88,7 +88,8 @@ SIGNATURES = {
     "gd_fe_function_local": [P, C.c_int, P, C.c_int, DP],
     "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
-    "gd_learned_create": [P, C.c_uint64, PP],
+    "gd_learned_create": [P, C.c_int, C.c_uint64, PP],
+    "gd_learned_levels": [P, I32P],
     "gd_learned_destroy": [P],
     "gd_learned_num_params": [P, I64P],
     "gd_learned_get_params": [P, C.POINTER(C.c_float)],

@@ -22,7 +22,7 @@ import numpy as np
 from . import _lib as L
 
 MAGIC = b"GDLP"
-FORMAT_VERSION = 1
+FORMAT_VERSION = 2   # header: magic, version, levels, parameter count, CRC32 of the float32 payload
 
 
 def _torch():
@@ -31,13 +31,15 @@ def _torch():
 
 
 class LearnedPreconditioner:
-    """The 3-level, 8-channel network bound to one assembler (one problem size)."""
+    """The L-level (default 3), 8-channel network bound to one assembler (one problem
+    size), applied as z = D^-1 r + D^-1/2 S^T S D^-1/2 r (symmetric positive definite)."""
 
-    def __init__(self, matrix, seed: int = 0):
+    def __init__(self, matrix, seed: int = 0, levels: int = 3):
         self.matrix = matrix
         self.assem = matrix.assem
+        self.levels = int(levels)
         h = C.c_void_p()
-        L.call("gd_learned_create", self.assem.handle, C.c_uint64(seed), C.byref(h))
+        L.call("gd_learned_create", self.assem.handle, self.levels, C.c_uint64(seed), C.byref(h))
         self.handle = h
         n = C.c_int64()
         L.call("gd_learned_num_params", self.handle, C.byref(n))
@@ -56,19 +58,35 @@ class LearnedPreconditioner:
         L.call("gd_learned_set_params", self.handle, p.ctypes.data_as(C.POINTER(C.c_float)))
 
     def save(self, path):
-        """Versioned file: magic, format version, parameter count, CRC32, float32 params."""
+        """Versioned little-endian file: magic, format version, levels, parameter count,
+        CRC32, float32 params.  The parameters do not depend on the mesh size."""
         p = self.get_params()
         blob = p.tobytes()
-        Path(path).write_bytes(MAGIC + struct.pack("<III", FORMAT_VERSION, p.size, zlib.crc32(blob)) + blob)
+        Path(path).write_bytes(MAGIC + struct.pack("<IIII", FORMAT_VERSION, self.levels, p.size, zlib.crc32(blob))
+                               + blob)
+
+    @staticmethod
+    def file_levels(path) -> int:
+        """Number of levels stored in a parameter file (for constructing a matching net)."""
+        data = Path(path).read_bytes()[:20]
+        if data[:4] != MAGIC:
+            raise ValueError(f"{path}: not a learned-preconditioner file")
+        version, levels = struct.unpack("<II", data[4:12])
+        if version != FORMAT_VERSION:
+            raise ValueError(f"{path}: format version {version}, expected {FORMAT_VERSION}")
+        return levels
 
     def load(self, path):
         data = Path(path).read_bytes()
         if data[:4] != MAGIC:
             raise ValueError(f"{path}: not a learned-preconditioner file")
-        version, count, crc = struct.unpack("<III", data[4:16])
+        version, = struct.unpack("<I", data[4:8])
         if version != FORMAT_VERSION:
             raise ValueError(f"{path}: format version {version}, expected {FORMAT_VERSION}")
-        blob = data[16:]
+        levels, count, crc = struct.unpack("<III", data[8:20])
+        if levels != self.levels:
+            raise ValueError(f"{path}: {levels}-level network, this one has {self.levels}")
+        blob = data[20:]
         if count != self.num_params or len(blob) != 4 * count or zlib.crc32(blob) != crc:
             raise ValueError(f"{path}: parameter count or checksum mismatch")
         self.set_params(np.frombuffer(blob, dtype=np.float32))
@@ -99,7 +117,8 @@ class LearnedPreconditioner:
         return loss.value
 
     def solve(self, rtol=1e-8, maxit=100000):
-        """x = A \\ b with the learned flexible CG (Jacobi fallback on stall)."""
+        """x = A \\ b with the learned flexible CG; Jacobi fallback when the learned
+        iteration stagnates.  Returns (x, stats, fallback_used)."""
         x = np.zeros(self.matrix.n_global)
         st = L.gd_solve_stats()
         fb = C.c_int32()

@@ -222,12 +222,15 @@ int gd_fe_function_local(const gd_space* space, int part, const double* x_global
                          double* x_local);
 
 /* ---- learned preconditioner (3D Q1 on cube cells) ---------------------------------
- * No counterpart in the reference (whose `\` is a gathered LU).  A 3-level, 8-channel
- * convolutional network on the node lattice, linear in the residual and gated by the
- * coefficient field, used as the preconditioner of the mixed-precision flexible CG.
+ * No counterpart in the reference (whose `\` is a gathered LU).  An L-level (1..6,
+ * default 3), 8-channel convolutional network on the node lattice, gated by the
+ * coefficient field, in the symmetric positive definite form
+ * z = D^-1 r + D^-1/2 S^T S D^-1/2 r (S the gated encoder, S^T its adjoint), used as the
+ * preconditioner of the mixed-precision flexible CG.
  * Vectors r, e, z are FP32 device arrays over the owned DOFs in gid order. */
 typedef struct gd_learned gd_learned;
-int gd_learned_create(gd_asm* a, uint64_t seed, gd_learned** out);
+int gd_learned_create(gd_asm* a, int levels, uint64_t seed, gd_learned** out);
+int gd_learned_levels(const gd_learned* net, int32_t* levels);
 int gd_learned_destroy(gd_learned* net);
 int gd_learned_num_params(const gd_learned* net, int64_t* n);
 int gd_learned_get_params(const gd_learned* net, float* host_params);

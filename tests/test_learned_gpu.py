@@ -53,8 +53,11 @@ def global_matrix(op):
     return sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
 
 
-def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, A):
-    """The same network in float64 PyTorch on the CPU; returns z (gid order)."""
+def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, levels):
+    """The same network in float64 PyTorch on the CPU; returns z (gid order).
+
+    S^T S x is taken as the gradient of 0.5 |S x|^2 (autograd), an independent route to
+    the decoder that the device computes as the explicit adjoint of the encoder."""
     N = [c + 1 for c in cells]
     nlat = int(np.prod(N))
     off = 0
@@ -64,19 +67,16 @@ def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, A):
         t = params[off:off + count].reshape(shape)
         off += count
         return t
-    W0 = take(C8 * TAPS, (C8, 1, 3, 3, 3))
-    W1 = take(C8 * C8 * TAPS, (C8, C8, 3, 3, 3))
-    W2 = take(C8 * C8 * TAPS, (C8, C8, 3, 3, 3))
-    W3 = take(C8 * C8 * TAPS, (C8, C8, 3, 3, 3))
-    W4 = take(C8 * TAPS, (1, C8, 3, 3, 3))
-    G = [take(C8 * TAPS, (C8, 1, 3, 3, 3)) for _ in range(4)]
-    Bs = [take(C8, (C8,)) for _ in range(4)]
+    W = [take(C8 * (1 if l == 0 else C8) * TAPS, (C8, 1 if l == 0 else C8, 3, 3, 3)) for l in range(levels)]
+    G = [take(C8 * TAPS, (C8, 1, 3, 3, 3)) for _ in range(levels)]
+    Bs = [take(C8, (C8,)) for _ in range(levels)]
+    assert off == params.numel()
     # node feature: log mean kappa of the cells around each node
     kc = torch.tensor(kappa_cells, dtype=torch.float64).reshape(cells[2], cells[1], cells[0])
     kp = F.pad(kc[None, None], (1, 1, 1, 1, 1, 1))
     ones = F.pad(torch.ones_like(kc)[None, None], (1, 1, 1, 1, 1, 1))
     box = torch.ones(1, 1, 2, 2, 2, dtype=torch.float64)
-    f0 = torch.log(F.conv3d(kp, box) / F.conv3d(ones, box))
+    f = [torch.log(F.conv3d(kp, box) / F.conv3d(ones, box))]
     w1 = torch.tensor([0.25, 0.5, 0.25], dtype=torch.float64)
     Rw = (w1[:, None, None] * w1[None, :, None] * w1[None, None, :])[None, None]
 
@@ -84,35 +84,39 @@ def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, A):
         c = x.shape[1]
         return F.conv3d(x, Rw.repeat(c, 1, 1, 1, 1), stride=2, padding=1, groups=c)
 
-    def P(x):
-        c = x.shape[1]
-        return F.conv_transpose3d(x, 8 * Rw.repeat(c, 1, 1, 1, 1), stride=2, padding=1, groups=c)
-
-    f1 = R(f0)
-    f2 = R(f1)
-    gate = lambda f, k: torch.sigmoid(F.conv3d(f, G[k], bias=Bs[k], padding=1))
-    s0, s1, s2, s3 = gate(f0, 0), gate(f1, 1), gate(f2, 2), gate(f1, 3)
-    # input lattice
+    for _ in range(1, levels):
+        f.append(R(f[-1]))
+    s = [torch.sigmoid(F.conv3d(f[l], G[l], bias=Bs[l], padding=1)) for l in range(levels)]
+    dsq = torch.sqrt(dinv)
     x0 = torch.zeros(nlat, dtype=torch.float64)
-    x0[node_of_gid] = dinv * r_gid
-    x0 = x0.reshape(1, 1, N[2], N[1], N[0])
-    h0 = F.conv3d(x0, W0, padding=1) * s0
-    h1 = F.conv3d(R(h0), W1, padding=1) * s1
-    h2 = F.conv3d(R(h1), W2, padding=1) * s2
-    v1 = F.conv3d(P(h2) + h1, W3, padding=1) * s3
-    o = F.conv3d(P(v1) + h0, W4, padding=1)
-    z = (x0 + o).reshape(-1)[node_of_gid]
-    return z
+    x0[node_of_gid] = dsq * r_gid
+    x0 = x0.reshape(1, 1, N[2], N[1], N[0]).requires_grad_(True)
+    hs, x = [], x0
+    for l in range(levels):
+        if l > 0:
+            x = R(hs[-1])
+        hs.append(F.conv3d(x, W[l], padding=1) * s[l])
+    q = 0.5 * sum((h * h).sum() for h in hs)
+    y, = torch.autograd.grad(q, x0, create_graph=True)
+    return dinv * r_gid + dsq * y.reshape(-1)[node_of_gid]
 
 
-def test_network_gradient_matches_pytorch():
+def small_system(be, seed=41):
+    pb = make_problem(3, (8, 8, 8), (2, 2, 2), 1, seed=seed)
+    model, V, op = build(be, pb)
+    A = torch.tensor(global_matrix(op).toarray(), dtype=torch.float64)
+    return pb, V, op, A
+
+
+@pytest.mark.parametrize("levels", [1, 3, 4])
+def test_network_gradient_matches_pytorch(levels):
     import gridap_gb300 as G
     from gridap_gb300.learned import LearnedPreconditioner
     be = G.GB300Backend(0)
     try:
-        pb = make_problem(3, (8, 8, 8), (2, 2, 2), 1, seed=41)
-        model, V, op = build(be, pb)
-        net = LearnedPreconditioner(op.matrix, seed=7)
+        pb, V, op, A = small_system(be)
+        net = LearnedPreconditioner(op.matrix, seed=7, levels=levels)
+        assert net.num_params == C8 * TAPS + (levels - 1) * C8 * C8 * TAPS + levels * (C8 * TAPS + C8)
         n = V.num_free_dofs()
         rng = np.random.default_rng(5)
         r = rng.standard_normal((2, n)).astype(np.float32)
@@ -121,13 +125,12 @@ def test_network_gradient_matches_pytorch():
         loss_gpu, grad_gpu = net.gradient(rd, ed)
         z_gpu = net.apply(rd[0].contiguous()).cpu().numpy()
         # PyTorch CPU restatement
-        A = torch.tensor(global_matrix(op).toarray(), dtype=torch.float64)
         dinv = 1.0 / torch.diagonal(A)
         node_of_gid = torch.tensor(gid_to_node(V))
         params = torch.tensor(net.get_params().astype(np.float64), requires_grad=True)
         total = 0.0
         for b in range(2):
-            z = torch_net(params, pb.kappa, pb.n, torch.tensor(r[b], dtype=torch.float64), node_of_gid, dinv, A)
+            z = torch_net(params, pb.kappa, pb.n, torch.tensor(r[b], dtype=torch.float64), node_of_gid, dinv, levels)
             if b == 0:
                 assert np.abs(z.detach().numpy() - z_gpu).max() <= 1e-4 * np.abs(z_gpu).max()
             ev = torch.tensor(e[b], dtype=torch.float64)
@@ -139,6 +142,31 @@ def test_network_gradient_matches_pytorch():
         gref = params.grad.numpy()
         rel = np.linalg.norm(grad_gpu - gref) / np.linalg.norm(gref)
         assert rel <= 2e-3, rel
+        net.close()
+    finally:
+        be.close()
+
+
+def test_network_is_symmetric_positive_definite():
+    """<r1, M r2> = <M r1, r2> and <r, M r> > 0 for the device network, also with
+    parameters far from the initial ones."""
+    import gridap_gb300 as G
+    from gridap_gb300.learned import LearnedPreconditioner
+    be = G.GB300Backend(0)
+    try:
+        pb, V, op, A = small_system(be, seed=43)
+        net = LearnedPreconditioner(op.matrix, seed=11, levels=3)
+        rng = np.random.default_rng(9)
+        net.set_params(rng.standard_normal(net.num_params).astype(np.float32) * 0.5)
+        n = V.num_free_dofs()
+        r = torch.tensor(rng.standard_normal((3, n)), device="cuda", dtype=torch.float32)
+        z = [net.apply(r[i].contiguous()).double() for i in range(3)]
+        rr = r.double()
+        a, b = torch.dot(rr[0], z[1]).item(), torch.dot(z[0], rr[1]).item()
+        scale = (torch.linalg.vector_norm(rr[0]) * torch.linalg.vector_norm(z[1])).item()
+        assert abs(a - b) <= 1e-5 * scale, (a, b)
+        for i in range(3):
+            assert torch.dot(rr[i], z[i]).item() > 0
         net.close()
     finally:
         be.close()
