@@ -175,7 +175,12 @@ struct MixedState {
   DBuf<float> wf;         // prescaled cell coefficients (FP32)
   DBuf<float> vals32;     // FP32 copy of the owned-row values (non-cube spaces)
   DBuf<float> zold;       // previous preconditioned residual (flexible CG)
+  // lattice-order inner iteration (3D cube Q1): x r z0 z1 p0 p1 q dinv, node-lattice sized
+  DBuf<float> lat;
+  DBuf<double> latred;    // block partials, arrival counter and CG scalars
+  int64_t lat_epoch = -1;
 };
+constexpr int kLatVectors = 8;
 }  // namespace gd
 
 // ---------------------------------------------------------------------------------

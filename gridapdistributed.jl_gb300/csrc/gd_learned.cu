@@ -164,51 +164,258 @@ __global__ void k_sum_partials(int nparts, int nw, const float* __restrict__ par
   out[w] += a;
 }
 
-// ---- restriction / prolongation (per channel) ---------------------------------------------
-// coarse[i] = sum_{o in {-1,0,1}^3} w(o) fine[2i+o], w = prod(1/2 if o=0 else 1/4)
+// ---- restriction / prolongation ----------------------------------------------------------
+// One thread per output voxel for all C channels; neighbour indices and weights are
+// formed once per voxel in 32-bit arithmetic (lattices stay below 2^31 nodes).
+// coarse[i] = scale * sum_{o in {-1,0,1}^3} w(o) fine[2i+o], w = prod(1/2 if o=0 else 1/4)
 __global__ void k_restrict(int C, Dims f, Dims c, const float* __restrict__ fine, float* __restrict__ coarse,
                            float scale) {
-  const int64_t nc = c.size(), nf = f.size();
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < (int64_t)C * nc;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const int ch = (int)(v / nc);
-    const int64_t i = v % nc;
-    const int ix = (int)(i % c.n[0]), iy = (int)((i / c.n[0]) % c.n[1]), iz = (int)(i / ((int64_t)c.n[0] * c.n[1]));
-    float acc = 0.f;
-    for (int oz = -1; oz <= 1; ++oz)
-      for (int oy = -1; oy <= 1; ++oy)
+  const int nc = (int)c.size(), nf = (int)f.size();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int ix = i % c.n[0], iy = (i / c.n[0]) % c.n[1], iz = i / (c.n[0] * c.n[1]);
+    float acc[kC];
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
+    for (int oz = -1; oz <= 1; ++oz) {
+      const int fz = 2 * iz + oz;
+      if (fz < 0 || fz >= f.n[2]) continue;
+      for (int oy = -1; oy <= 1; ++oy) {
+        const int fy = 2 * iy + oy;
+        if (fy < 0 || fy >= f.n[1]) continue;
         for (int ox = -1; ox <= 1; ++ox) {
-          const int fx = 2 * ix + ox, fy = 2 * iy + oy, fz = 2 * iz + oz;
-          if (fx < 0 || fx >= f.n[0] || fy < 0 || fy >= f.n[1] || fz < 0 || fz >= f.n[2]) continue;
+          const int fx = 2 * ix + ox;
+          if (fx < 0 || fx >= f.n[0]) continue;
           const float w = (ox == 0 ? 0.5f : 0.25f) * (oy == 0 ? 0.5f : 0.25f) * (oz == 0 ? 0.5f : 0.25f);
-          acc = fmaf(w, fine[ch * nf + fx + (int64_t)f.n[0] * (fy + (int64_t)f.n[1] * fz)], acc);
+          const int u = fx + f.n[0] * (fy + f.n[1] * fz);
+#pragma unroll
+          for (int ch = 0; ch < kC; ++ch)
+            if (ch < C) acc[ch] = fmaf(w, __ldg(fine + (size_t)ch * nf + u), acc[ch]);
         }
-    coarse[ch * nc + i] = scale * acc;
+      }
+    }
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch)
+      if (ch < C) coarse[(size_t)ch * nc + i] = scale * acc[ch];
   }
 }
 
-// fine[j] (+)= scale * sum_i w'(j - 2i) coarse[i], trilinear w' = prod(1 if 0 else 1/2)
+// trilinear neighbours of fine voxel j along one axis: j even -> coarse j/2 (weight 1);
+// j odd -> (j-1)/2 and (j+1)/2 (weights 1/2, the second only inside the coarse lattice)
+struct Lin1 {
+  int i0, i1, cnt;
+  float w;
+};
+__device__ inline Lin1 lin1(int j, int nc) {
+  Lin1 r;
+  if ((j & 1) == 0) {
+    r.i0 = r.i1 = j >> 1;
+    r.cnt = 1;
+    r.w = 1.f;
+  } else {
+    r.i0 = j >> 1;
+    r.i1 = (j >> 1) + 1;
+    r.cnt = r.i1 < nc ? 2 : 1;
+    r.w = 0.5f;
+  }
+  return r;
+}
+
+// fine[j] (+)= scale * sum_i w'(j - 2i) coarse[i] (P = 8 R^T, trilinear)
 __global__ void k_prolong(int C, Dims c, Dims f, const float* __restrict__ coarse, float* __restrict__ fine,
                           float scale, int accumulate) {
-  const int64_t nc = c.size(), nf = f.size();
-  for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < (int64_t)C * nf;
-       v += (int64_t)gridDim.x * blockDim.x) {
-    const int ch = (int)(v / nf);
-    const int64_t j = v % nf;
-    const int jx = (int)(j % f.n[0]), jy = (int)((j / f.n[0]) % f.n[1]), jz = (int)(j / ((int64_t)f.n[0] * f.n[1]));
-    float acc = 0.f;
-    for (int oz = -1; oz <= 1; ++oz)
-      for (int oy = -1; oy <= 1; ++oy)
-        for (int ox = -1; ox <= 1; ++ox) {
-          const int cx2 = jx - ox, cy2 = jy - oy, cz2 = jz - oz;   // 2i = j - o
-          if ((cx2 & 1) || (cy2 & 1) || (cz2 & 1)) continue;
-          const int cx = cx2 / 2, cy = cy2 / 2, cz = cz2 / 2;
-          if (cx2 < 0 || cy2 < 0 || cz2 < 0 || cx >= c.n[0] || cy >= c.n[1] || cz >= c.n[2]) continue;
-          const float w = (ox == 0 ? 1.f : 0.5f) * (oy == 0 ? 1.f : 0.5f) * (oz == 0 ? 1.f : 0.5f);
-          acc = fmaf(w, coarse[ch * nc + cx + (int64_t)c.n[0] * (cy + (int64_t)c.n[1] * cz)], acc);
+  const int nc = (int)c.size(), nf = (int)f.size();
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
+    const int jx = j % f.n[0], jy = (j / f.n[0]) % f.n[1], jz = j / (f.n[0] * f.n[1]);
+    const Lin1 X = lin1(jx, c.n[0]), Y = lin1(jy, c.n[1]), Z = lin1(jz, c.n[2]);
+    float acc[kC];
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
+    for (int b = 0; b < Z.cnt; ++b)
+      for (int a = 0; a < Y.cnt; ++a)
+        for (int e = 0; e < X.cnt; ++e) {
+          const int u = (e ? X.i1 : X.i0) + c.n[0] * ((a ? Y.i1 : Y.i0) + c.n[1] * (b ? Z.i1 : Z.i0));
+          const float w = X.w * Y.w * Z.w;
+#pragma unroll
+          for (int ch = 0; ch < kC; ++ch)
+            if (ch < C) acc[ch] = fmaf(w, __ldg(coarse + (size_t)ch * nc + u), acc[ch]);
         }
-    if (accumulate) fine[ch * nf + j] += scale * acc;
-    else fine[ch * nf + j] = scale * acc;
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch)
+      if (ch < C) {
+        if (accumulate) fine[(size_t)ch * nf + j] += scale * acc[ch];
+        else fine[(size_t)ch * nf + j] = scale * acc[ch];
+      }
+  }
+}
+
+// decoder step below the top level: out = (h + scale * P gx) * s, all kC channels
+__global__ void k_prolong_gate(Dims c, Dims f, const float* __restrict__ gx, const float* __restrict__ h,
+                               const float* __restrict__ s, float scale, float* __restrict__ out) {
+  const int nc = (int)c.size(), nf = (int)f.size();
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
+    const int jx = j % f.n[0], jy = (j / f.n[0]) % f.n[1], jz = j / (f.n[0] * f.n[1]);
+    const Lin1 X = lin1(jx, c.n[0]), Y = lin1(jy, c.n[1]), Z = lin1(jz, c.n[2]);
+    float acc[kC];
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
+    for (int b = 0; b < Z.cnt; ++b)
+      for (int a = 0; a < Y.cnt; ++a)
+        for (int e = 0; e < X.cnt; ++e) {
+          const int u = (e ? X.i1 : X.i0) + c.n[0] * ((a ? Y.i1 : Y.i0) + c.n[1] * (b ? Z.i1 : Z.i0));
+          const float w = X.w * Y.w * Z.w;
+#pragma unroll
+          for (int ch = 0; ch < kC; ++ch) acc[ch] = fmaf(w, __ldg(gx + (size_t)ch * nc + u), acc[ch]);
+        }
+#pragma unroll
+    for (int ch = 0; ch < kC; ++ch)
+      out[(size_t)ch * nf + j] = fmaf(scale, acc[ch], __ldg(h + (size_t)ch * nf + j)) * __ldg(s + (size_t)ch * nf + j);
+  }
+}
+
+// ---- tiled convolution for the preconditioner application ---------------------------------
+// Each CTA computes a TX x TY x TZ block of output voxels for all CO channels from a
+// shared-memory copy of the (TX+2)(TY+2)(TZ+2) input halo (all CI channels) and of the
+// weights laid out [ci][tap][co]; each thread holds XT consecutive x-voxels in registers so
+// a weight fetched from shared memory feeds XT FMAs and an input row feeds 3 taps.
+//   load modes : LD_PLAIN  in[ci][u]
+//                LD_GATED  in[ci][u] * in_gate[ci][u]              (decoder, top level)
+//                LD_GATHER sqrt(dinv[g]) r[g] at g = node_gid[u]    (encoder, level 0; CI = 1)
+//   epilogues  : EP_GATE   out[co][v] = acc * out_gate[co][v]       (encoder)
+//                EP_PLAIN  out[co][v] = acc                         (decoder)
+//                EP_OUT    z[g] = dinv[g] r[g] + sqrt(dinv[g]) acc  (decoder, level 0; CO = 1)
+//                EP_OUTLAT z[v] = dinv[v] r[v] + dsq[v] acc         (same, vectors on the lattice)
+enum { LD_PLAIN = 0, LD_GATED = 1, LD_GATHER = 2 };
+enum { EP_GATE = 0, EP_PLAIN = 1, EP_OUT = 2, EP_OUTLAT = 3 };
+constexpr int kTX = 16, kTY = 8;
+
+struct TConvArgs {
+  Dims d;
+  const float* in;
+  const float* in_gate;
+  const float* W;   // forward layout [co_f][ci_f][27]
+  int adjoint;      // 1: apply the adjoint of the forward convolution W
+  const float* out_gate;
+  float* out;
+  const int32_t* node_gid;
+  const float* r;
+  const float* dinv;
+  const float* dsq;
+  float* z;
+};
+
+template <int CI, int CO, int XT, int TZ>
+struct TConvShape {
+  static constexpr int HX = kTX + 2, HY = kTY + 2, HZ = TZ + 2;
+  static constexpr int HP = HX * HY * HZ;
+  static constexpr int LX = kTX / XT;
+  static constexpr int threads = LX * kTY * TZ;
+  static constexpr int nw = CI * kTaps * CO;
+  static constexpr size_t smem = sizeof(float) * (size_t)(nw + CI * HP);
+};
+
+template <int CI, int CO, int XT, int TZ, int LD, int EP>
+__global__ void __launch_bounds__(TConvShape<CI, CO, XT, TZ>::threads) k_tconv(TConvArgs a) {
+  using S = TConvShape<CI, CO, XT, TZ>;
+  extern __shared__ __align__(16) float tsm[];
+  float* sw = tsm;          // [ci][tap][co]
+  float* sx = tsm + S::nw;  // [ci][hz][hy][hx]
+  const int nx = a.d.n[0], ny = a.d.n[1], nz = a.d.n[2];
+  const int nv = nx * ny * nz;
+  const int tiles_x = (nx + kTX - 1) / kTX, tiles_y = (ny + kTY - 1) / kTY;
+  const int bx = blockIdx.x % tiles_x, by = (blockIdx.x / tiles_x) % tiles_y, bz = blockIdx.x / (tiles_x * tiles_y);
+  const int x0 = bx * kTX, y0 = by * kTY, z0 = bz * TZ;
+  for (int i = threadIdx.x; i < S::nw; i += S::threads) {
+    const int co = i % CO, tap = (i / CO) % kTaps, ci = i / (kTaps * CO);
+    sw[i] = a.adjoint ? a.W[(ci * CO + co) * kTaps + (kTaps - 1 - tap)] : a.W[(co * CI + ci) * kTaps + tap];
+  }
+  for (int i = threadIdx.x; i < S::HP; i += S::threads) {
+    const int hx = i % S::HX, hy = (i / S::HX) % S::HY, hz = i / (S::HX * S::HY);
+    const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+    const bool inb = gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz;
+    const int u = gx + nx * (gy + ny * gz);
+    if (LD == LD_GATHER) {
+      float v = 0.f;
+      if (inb) {
+        const int32_t g = __ldg(a.node_gid + u);
+        if (g >= 0) v = sqrtf(__ldg(a.dinv + g)) * __ldg(a.r + g);
+      }
+      sx[i] = v;
+    } else {
+#pragma unroll
+      for (int ci = 0; ci < CI; ++ci) {
+        float v = 0.f;
+        if (inb) {
+          v = __ldg(a.in + (size_t)ci * nv + u);
+          if (LD == LD_GATED) v *= __ldg(a.in_gate + (size_t)ci * nv + u);
+        }
+        sx[ci * S::HP + i] = v;
+      }
+    }
+  }
+  __syncthreads();
+  const int tx = threadIdx.x % S::LX, ty = (threadIdx.x / S::LX) % kTY, tz = threadIdx.x / (S::LX * kTY);
+  float acc[XT][CO];
+#pragma unroll
+  for (int j = 0; j < XT; ++j)
+#pragma unroll
+    for (int co = 0; co < CO; ++co) acc[j][co] = 0.f;
+#pragma unroll 1
+  for (int ci = 0; ci < CI; ++ci) {
+#pragma unroll
+    for (int dz = 0; dz < 3; ++dz)
+#pragma unroll
+      for (int dy = 0; dy < 3; ++dy) {
+        const float* row = sx + ci * S::HP + (tz + dz) * (S::HX * S::HY) + (ty + dy) * S::HX + tx * XT;
+        float v[XT + 2];
+#pragma unroll
+        for (int k = 0; k < XT + 2; ++k) v[k] = row[k];
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx) {
+          const float* wp = sw + (ci * kTaps + dz * 9 + dy * 3 + dx) * CO;
+          float w[CO];
+          if constexpr (CO % 4 == 0) {
+#pragma unroll
+            for (int q = 0; q < CO / 4; ++q) {
+              const float4 t = reinterpret_cast<const float4*>(wp)[q];
+              w[4 * q] = t.x;
+              w[4 * q + 1] = t.y;
+              w[4 * q + 2] = t.z;
+              w[4 * q + 3] = t.w;
+            }
+          } else {
+#pragma unroll
+            for (int co = 0; co < CO; ++co) w[co] = wp[co];
+          }
+#pragma unroll
+          for (int j = 0; j < XT; ++j)
+#pragma unroll
+            for (int co = 0; co < CO; ++co) acc[j][co] = fmaf(w[co], v[j + dx], acc[j][co]);
+        }
+      }
+  }
+  const int y = y0 + ty, zz = z0 + tz;
+  if (y >= ny || zz >= nz) return;
+#pragma unroll
+  for (int j = 0; j < XT; ++j) {
+    const int x = x0 + tx * XT + j;
+    if (x >= nx) break;
+    const int v = x + nx * (y + ny * zz);
+    if (EP == EP_OUTLAT) {
+      a.z[v] = fmaf(__ldg(a.dsq + v), acc[j][0], __ldg(a.dinv + v) * __ldg(a.r + v));
+    } else if (EP == EP_OUT) {
+      const int32_t g = __ldg(a.node_gid + v);
+      if (g >= 0) {
+        const float di = __ldg(a.dinv + g);
+        a.z[g] = fmaf(sqrtf(di), acc[j][0], di * __ldg(a.r + g));
+      }
+    } else {
+#pragma unroll
+      for (int co = 0; co < CO; ++co) {
+        float o = acc[j][co];
+        if (EP == EP_GATE) o *= __ldg(a.out_gate + (size_t)co * nv + v);
+        a.out[(size_t)co * nv + v] = o;
+      }
+    }
   }
 }
 
@@ -450,7 +657,7 @@ static int net_encode(gd_learned* N, int p, cudaStream_t st) {
   const float* P = N->params.p;
   for (int l = 0; l < N->levels; ++l) {
     if (l > 0)
-      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[p][l - 1].p, N->x[p][l].p,
+      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[p][l - 1].p, N->x[p][l].p,
                                                         1.f);
     GD_TRY(conv_launch(cin_of(l), kC, N->L[l], N->x[p][l].p, P + N->offW[l], nullptr, nullptr, N->a[p][l].p, 0, 0, st));
     k_mul<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->a[p][l].p, N->s[l].p, N->h[p][l].p);
@@ -470,7 +677,7 @@ static int net_decode(gd_learned* N, int p, cudaStream_t st) {
     GD_TRY(conv_launch(kC, cin_of(l), N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, out, 1, 0, st));
     if (l > 0) {
       k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[p][l - 1].p, N->u[l - 1].p);
-      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->u[l - 1].p,
+      k_prolong<<<nb_for(N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->u[l - 1].p,
                                                            0.125f, 1);
     }
   }
@@ -494,7 +701,7 @@ static int net_encoder_backward(gd_learned* N, int p, int q, cudaStream_t st) {
     if (l > 0) {
       GD_TRY(conv_launch(kC, kC, N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, N->gx[l].p, 1, 0, st));
       k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[q][l - 1].p, N->d[l - 1].p);
-      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->d[l - 1].p,
+      k_prolong<<<nb_for(N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->d[l - 1].p,
                                                            0.125f, 1);
     }
   }
@@ -549,9 +756,140 @@ static int net_loss(gd_learned* N, const float* z, const float* e, double* loss,
   return GD_OK;
 }
 
+template <int CI, int CO, int XT, int TZ, int LD, int EP>
+static int tconv_launch(const TConvArgs& a, cudaStream_t st) {
+  using S = TConvShape<CI, CO, XT, TZ>;
+  auto kern = k_tconv<CI, CO, XT, TZ, LD, EP>;
+  if (S::smem > 48 * 1024)
+    GD_CUDA_TRY(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)S::smem));
+  const unsigned nb = (unsigned)(((a.d.n[0] + kTX - 1) / kTX) * ((a.d.n[1] + kTY - 1) / kTY) * ((a.d.n[2] + TZ - 1) / TZ));
+  kern<<<nb, S::threads, S::smem, st>>>(a);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// z = D^-1 r + D^-1/2 S^T S D^-1/2 r for the solver (no training caches): tiled
+// convolutions with the gates, the gather of r and the output fused in; 4L - 1 launches.
+static int net_apply_fast(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const float* P = N->params.p;
+  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
+  const int Lv = N->levels;
+  TConvArgs t{};
+  t.node_gid = A->mx.node_gid.p;
+  t.r = r;
+  t.dinv = dinv;
+  t.z = z;
+  // encoder
+  for (int l = 0; l < Lv; ++l) {
+    t.d = N->L[l];
+    t.W = P + N->offW[l];
+    t.adjoint = 0;
+    t.out_gate = N->s[l].p;
+    t.out = N->h[0][l].p;
+    if (l == 0) {
+      t.in = nullptr;
+      GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATHER, EP_GATE>(t, st)));
+    } else {
+      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
+      t.in = N->x[0][l].p;
+      GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
+    }
+  }
+  // decoder (adjoint convolutions)
+  for (int l = Lv - 1; l >= 0; --l) {
+    t.d = N->L[l];
+    t.W = P + N->offW[l];
+    t.adjoint = 1;
+    t.out_gate = nullptr;
+    t.out = N->gx[l].p;
+    int ld = LD_PLAIN;
+    if (l == Lv - 1) {
+      t.in = N->h[0][l].p;
+      t.in_gate = N->s[l].p;
+      ld = LD_GATED;
+    } else {
+      k_prolong_gate<<<nb_for(N->nl[l]), kLT, 0, st>>>(N->L[l + 1], N->L[l], N->gx[l + 1].p, N->h[0][l].p,
+                                                       N->s[l].p, 0.125f, N->da[l].p);
+      GD_CUDA_TRY(cudaGetLastError());
+      t.in = N->da[l].p;
+      t.in_gate = nullptr;
+    }
+    if (l == 0) {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 8, 8, LD_GATED, EP_OUT>(t, st)));
+      else GD_TRY((tconv_launch<kC, 1, 8, 8, LD_PLAIN, EP_OUT>(t, st)));
+    } else {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
+      else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
+    }
+  }
+  return GD_OK;
+}
+
+// the same map with r and z on the node lattice (0 on Dirichlet nodes)
+static int net_apply_lattice(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+  gd_asm* A = N->A;
+  const float* P = N->params.p;
+  const int Lv = N->levels;
+  TConvArgs t{};
+  t.r = r;
+  t.dinv = lattice_dinv(A);
+  t.dsq = N->dsq.p;
+  t.z = z;
+  for (int l = 0; l < Lv; ++l) {
+    t.d = N->L[l];
+    t.W = P + N->offW[l];
+    t.adjoint = 0;
+    t.out_gate = N->s[l].p;
+    t.out = N->h[0][l].p;
+    if (l == 0) {
+      t.in = r;
+      t.in_gate = N->dsq.p;
+      GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATED, EP_GATE>(t, st)));
+    } else {
+      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
+      t.in = N->x[0][l].p;
+      t.in_gate = nullptr;
+      GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
+    }
+  }
+  for (int l = Lv - 1; l >= 0; --l) {
+    t.d = N->L[l];
+    t.W = P + N->offW[l];
+    t.adjoint = 1;
+    t.out_gate = nullptr;
+    t.out = N->gx[l].p;
+    int ld = LD_PLAIN;
+    if (l == Lv - 1) {
+      t.in = N->h[0][l].p;
+      t.in_gate = N->s[l].p;
+      ld = LD_GATED;
+    } else {
+      k_prolong_gate<<<nb_for(N->nl[l]), kLT, 0, st>>>(N->L[l + 1], N->L[l], N->gx[l + 1].p, N->h[0][l].p,
+                                                       N->s[l].p, 0.125f, N->da[l].p);
+      GD_CUDA_TRY(cudaGetLastError());
+      t.in = N->da[l].p;
+      t.in_gate = nullptr;
+    }
+    if (l == 0) {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 8, 8, LD_GATED, EP_OUTLAT>(t, st)));
+      else GD_TRY((tconv_launch<kC, 1, 8, 8, LD_PLAIN, EP_OUTLAT>(t, st)));
+    } else {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
+      else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
+    }
+  }
+  return GD_OK;
+}
+
 static int apply_as_precond(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st) {
   (void)A;
-  return net_forward(static_cast<gd_learned*>(ctx), r, z, st);
+  return net_apply_fast(static_cast<gd_learned*>(ctx), r, z, st);
+}
+
+static int apply_as_precond_lattice(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st) {
+  (void)A;
+  return net_apply_lattice(static_cast<gd_learned*>(ctx), r, z, st);
 }
 
 }  // namespace gd
@@ -565,10 +903,12 @@ extern "C" int gd_learned_create(gd_asm* A, int levels, uint64_t seed, gd_learne
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_learned_create: assemble the system first");
   if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3))
     return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells");
+  const Geom& g = A->test->geom;
+  if ((double)g.N[0] * g.N[1] * g.N[2] * kC >= 2147483647.0)
+    return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: node lattice too large (8 channels must index in 32 bits)");
   gd_learned* N = new gd_learned();
   N->A = A;
   N->levels = levels;
-  const Geom& g = A->test->geom;
   for (int d = 0; d < 3; ++d) N->L[0].n[d] = (int)g.N[d];
   for (int l = 1; l < levels; ++l) N->L[l] = coarse_dims(N->L[l - 1]);
   for (int l = 0; l < levels; ++l) N->nl[l] = N->L[l].size();
@@ -711,6 +1051,16 @@ extern "C" int gd_learned_apply(gd_learned* N, const float* r, float* z) {
   if (!N || !r || !z) return fail(GD_ERR_ARG, "gd_learned_apply: null argument");
   cudaStream_t st = N->A->test->model->ctx->stream;
   GD_TRY(net_prepare(N, st));
+  GD_TRY(net_apply_fast(N, r, z, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return GD_OK;
+}
+
+// the same map through the training kernels (used to check the two paths agree)
+extern "C" int gd_learned_apply_reference(gd_learned* N, const float* r, float* z) {
+  if (!N || !r || !z) return fail(GD_ERR_ARG, "gd_learned_apply_reference: null argument");
+  cudaStream_t st = N->A->test->model->ctx->stream;
+  GD_TRY(net_prepare(N, st));
   GD_TRY(net_forward(N, r, z, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   return GD_OK;
@@ -765,7 +1115,7 @@ extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_solve_learned: assemble the system first");
   cudaStream_t st = A->test->model->ctx->stream;
   GD_TRY(net_prepare(N, st));
-  MixedPrecond pc{N, apply_as_precond};
+  MixedPrecond pc{N, apply_as_precond, apply_as_precond_lattice};
   if (fallback_used) *fallback_used = 0;
   gd_solve_stats s1{};
   int rc = mixed_solve(A, rtol, maxit, x, where, &s1, &pc);

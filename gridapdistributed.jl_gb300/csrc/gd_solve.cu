@@ -17,9 +17,9 @@
 
 namespace gd {
 
-constexpr int kSpmvThreads = 256;
-constexpr int kGroup = 8;                      // lanes per row
-constexpr int kRowsPerSpmvBlock = kSpmvThreads / kGroup;
+constexpr int kSpmvThreads = 128;                // one row per thread
+constexpr int kRowsPerSpmvBlock = kSpmvThreads;
+constexpr int kSpmvCap = 3584;                   // staged entries per chunk (43 KB)
 constexpr int kVecThreads = 256;
 constexpr int kMaxPartials = 1024;             // blocks that write partial sums
 
@@ -40,62 +40,94 @@ __device__ inline double block_sum(double v, double* sh) {
   return s;   // valid in thread 0
 }
 
-// y = A x over owned rows; optional partial dot(y, w) per block (grid-stride over row groups)
+// Block sum of one FP64 value per thread with 127 adds (a shuffle tree would issue
+// 5 adds per lane; GB300's FP64 pipe is the scarce unit in these kernels).
+__device__ inline double block_sum_serial(double v, double* sh) {
+  sh[threadIdx.x] = v;
+  __syncthreads();
+  if (threadIdx.x < kSpmvThreads / 32) {
+    double s = 0.0;
+    for (int i = 0; i < 32; ++i) s += sh[threadIdx.x * 32 + i];
+    sh[kSpmvThreads + threadIdx.x] = s;
+  }
+  __syncthreads();
+  double s = 0.0;
+  if (threadIdx.x == 0)
+    for (int i = 0; i < kSpmvThreads / 32; ++i) s += sh[kSpmvThreads + i];
+  __syncthreads();
+  return s;   // valid in thread 0
+}
+
+// CSR rows on GB300: one thread per row, so a row costs one FP64 FMA per entry and no
+// cross-lane adds; the block's contiguous entry range is staged through shared memory
+// with coalesced loads (in chunks, so rows of any length work).  MODE 0: y = A x with an
+// optional partial of y.w; MODE 1: r = b - A x with partials of r.r and b.b.
+template <int MODE>
+__device__ __forceinline__ void csr_rows(int64_t n, const int64_t* __restrict__ rowptr,
+                                         const int32_t* __restrict__ col, const double* __restrict__ val,
+                                         const double* __restrict__ x, const double* __restrict__ b,
+                                         double* __restrict__ out, const double* __restrict__ w, double& s1,
+                                         double& s2) {
+  __shared__ double sval[kSpmvCap];
+  __shared__ int32_t scol[kSpmvCap];
+  for (int64_t r0 = (int64_t)blockIdx.x * kSpmvThreads; r0 < n; r0 += (int64_t)gridDim.x * kSpmvThreads) {
+    const int64_t r = r0 + threadIdx.x;
+    const int64_t rend = r0 + kSpmvThreads < n ? r0 + kSpmvThreads : n;
+    const int64_t E0 = rowptr[r0], E1 = rowptr[rend];
+    const bool valid = r < n;
+    const int64_t rs = valid ? rowptr[r] : 0, re = valid ? rowptr[r + 1] : 0;
+    double acc = 0.0;
+    for (int64_t c0 = E0; c0 < E1; c0 += kSpmvCap) {
+      const int cn = (int)(E1 - c0 < kSpmvCap ? E1 - c0 : kSpmvCap);
+      __syncthreads();   // the previous chunk has been consumed
+      for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
+        sval[i] = val[c0 + i];
+        scol[i] = col[c0 + i];
+      }
+      __syncthreads();
+      const int64_t lo = rs > c0 ? rs : c0, hi = re < c0 + cn ? re : c0 + cn;
+      for (int64_t e = lo; e < hi; ++e) acc = fma(sval[e - c0], __ldg(x + scol[e - c0]), acc);
+    }
+    if (valid) {
+      if (MODE == 0) {
+        out[r] = acc;
+        if (w) s1 = fma(acc, w[r], s1);
+      } else {
+        const double bv = b[r];
+        const double rv = bv - acc;
+        if (out) out[r] = rv;
+        s1 = fma(rv, rv, s1);
+        s2 = fma(bv, bv, s2);
+      }
+    }
+  }
+}
+
+// y = A x over owned rows; optional partial dot(y, w) per block
 __global__ void __launch_bounds__(kSpmvThreads)
 k_spmv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
        const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y,
        const double* __restrict__ w, double* __restrict__ partial) {
-  __shared__ double sh[kSpmvThreads / 32];
-  const int g = threadIdx.x / kGroup, l = threadIdx.x % kGroup;
-  double dot = 0.0;
-  // the loop bound is uniform across a warp so the shuffles see all 32 lanes
-  const int64_t stride = (int64_t)gridDim.x * kRowsPerSpmvBlock;
-  for (int64_t base = (int64_t)blockIdx.x * kRowsPerSpmvBlock + (g & ~(32 / kGroup - 1)); base < n; base += stride) {
-    const int64_t r = base + (g & (32 / kGroup - 1));
-    const bool valid = r < n;
-    const int64_t e0 = valid ? rowptr[r] : 0, e1 = valid ? rowptr[r + 1] : 0;
-    double s = 0.0;
-    for (int64_t e = e0 + l; e < e1; e += kGroup) s += val[e] * __ldg(x + col[e]);
-#pragma unroll
-    for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
-    if (l == 0 && valid) {
-      y[r] = s;
-      if (w) dot += s * w[r];
-    }
-  }
+  __shared__ double sh[kSpmvThreads + kSpmvThreads / 32];
+  double dot = 0.0, unused = 0.0;
+  csr_rows<0>(n, rowptr, col, val, x, nullptr, y, w, dot, unused);
   if (partial) {
-    double t = block_sum(dot, sh);
+    const double t = block_sum_serial(dot, sh);
     if (threadIdx.x == 0) partial[blockIdx.x] = t;
   }
 }
 
-// r = b - A x (partial of r.r)
+// r = b - A x (partials of r.r and b.b)
 __global__ void __launch_bounds__(kSpmvThreads)
 k_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
            const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ b,
            double* __restrict__ r_out, double* __restrict__ partial_rr, double* __restrict__ partial_bb) {
-  __shared__ double sh[kSpmvThreads / 32];
-  const int g = threadIdx.x / kGroup, l = threadIdx.x % kGroup;
+  __shared__ double sh[kSpmvThreads + kSpmvThreads / 32];
   double rr = 0.0, bb = 0.0;
-  const int64_t stride = (int64_t)gridDim.x * kRowsPerSpmvBlock;
-  for (int64_t base = (int64_t)blockIdx.x * kRowsPerSpmvBlock + (g & ~(32 / kGroup - 1)); base < n; base += stride) {
-    const int64_t r = base + (g & (32 / kGroup - 1));
-    const bool valid = r < n;
-    const int64_t e0 = valid ? rowptr[r] : 0, e1 = valid ? rowptr[r + 1] : 0;
-    double s = 0.0;
-    for (int64_t e = e0 + l; e < e1; e += kGroup) s += val[e] * __ldg(x + col[e]);
-#pragma unroll
-    for (int o = kGroup / 2; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o, kGroup);
-    if (l == 0 && valid) {
-      double rv = b[r] - s;
-      if (r_out) r_out[r] = rv;
-      rr += rv * rv;
-      bb += b[r] * b[r];
-    }
-  }
-  double t = block_sum(rr, sh);
+  csr_rows<1>(n, rowptr, col, val, x, b, r_out, nullptr, rr, bb);
+  double t = block_sum_serial(rr, sh);
   if (threadIdx.x == 0) partial_rr[blockIdx.x] = t;
-  t = block_sum(bb, sh);
+  t = block_sum_serial(bb, sh);
   if (threadIdx.x == 0) partial_bb[blockIdx.x] = t;
 }
 
@@ -211,6 +243,20 @@ static int grid_for(int64_t n, int per_block) {
   int64_t b = (n + per_block - 1) / per_block;
   if (b > kMaxPartials) b = kMaxPartials;
   if (b < 1) b = 1;
+  if (per_block == kRowsPerSpmvBlock) {
+    // the SpMV grid-strides over row groups: launch only what is resident at once
+    static int resident[64] = {0};
+    int dev = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+      if (!resident[dev]) {
+        int sms = 0, per_sm = 0;
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_residual, kSpmvThreads, 0);
+        resident[dev] = sms * per_sm > 0 ? sms * per_sm : kMaxPartials;
+      }
+      if (b > resident[dev]) b = resident[dev];
+    }
+  }
   return (int)b;
 }
 

@@ -334,6 +334,8 @@ int mixed_apply(gd_asm* A, const float* x, float* y, double* partial, cudaStream
 int mixed_solve(gd_asm* A, double rtol, int maxit, double* x_out, int where, gd_solve_stats* stats,
                 const MixedPrecond* precond) {
   GD_TRY(mixed_setup(A));
+  if (A->mx.matrix_free && (!precond || precond->apply_lattice))
+    return mixed_solve_lattice(A, rtol, maxit, x_out, where, stats, precond);
   cudaStream_t st = A->test->model->ctx->stream;
   const int64_t n = A->ngdofs;
   MixedState& M = A->mx;

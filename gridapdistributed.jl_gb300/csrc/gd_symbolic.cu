@@ -619,6 +619,8 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->mx.wf);
   dfreeb(A->mx.vals32);
   dfreeb(A->mx.zold);
+  dfreeb(A->mx.lat);
+  dfreeb(A->mx.latred);
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;

@@ -95,6 +95,7 @@ SIGNATURES = {
     "gd_learned_get_params": [P, C.POINTER(C.c_float)],
     "gd_learned_set_params": [P, C.POINTER(C.c_float)],
     "gd_learned_apply": [P, P, P],
+    "gd_learned_apply_reference": [P, P, P],
     "gd_learned_gradient": [P, P, P, C.c_int, DP, C.POINTER(C.c_float)],
     "gd_learned_train_step": [P, P, P, C.c_int, C.c_float, DP],
     "gd_solve_learned": [P, P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats), I32P],

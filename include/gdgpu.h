@@ -237,6 +237,8 @@ int gd_learned_get_params(const gd_learned* net, float* host_params);
 int gd_learned_set_params(gd_learned* net, const float* host_params);
 /* z = M(r) for the assembler's current coefficients. */
 int gd_learned_apply(gd_learned* net, const float* r, float* z);
+/* The same map through the training kernels (a check on the tiled application path). */
+int gd_learned_apply_reference(gd_learned* net, const float* r, float* z);
 /* Mean relative A-norm error ||M(r_b) - e_b||_A^2 / ||e_b||_A^2 over `batch` pairs stored
  * back to back, and (optionally) the summed parameter gradients copied to the host. */
 int gd_learned_gradient(gd_learned* net, const float* r, const float* e, int batch, double* loss,
