@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "gd_internal.h"
+#include "gd_rows.cuh"
 
 namespace gd {
 
@@ -176,236 +177,33 @@ int reference_element(gd_asm* A, int degree) {
   return GD_OK;
 }
 
-// ---- matrix values ------------------------------------------------------------------
-template <int DIM, int K>
-struct Lat {
-  static constexpr int KP1 = K + 1;
-  static constexpr int NN = DIM == 2 ? KP1 * KP1 : KP1 * KP1 * KP1;
-  static constexpr int W = 2 * K + 1;
-};
-
-constexpr int kRowsPerBlock = 128;
-constexpr int kNumericThreads = 256;
-
-template <int DIM, int K, typename CodeT>
-__global__ void __launch_bounds__(kNumericThreads)
-k_numeric_matrix(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
-                 const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
-                 double* __restrict__ vals) {
-  using L = Lat<DIM, K>;
-  __shared__ double s_K[L::NN * L::NN];
-  __shared__ int64_t s_rp[kRowsPerBlock + 1];
-  __shared__ int32_t s_node[kRowsPerBlock];
-  const int64_t r0 = (int64_t)blockIdx.x * kRowsPerBlock;
-  const int nr = (int)((nrows_own - r0) < kRowsPerBlock ? (nrows_own - r0) : kRowsPerBlock);
-  for (int i = threadIdx.x; i < L::NN * L::NN; i += blockDim.x) s_K[i] = Khat[i];
-  for (int i = threadIdx.x; i <= nr; i += blockDim.x) s_rp[i] = rowptr[r0 + i];
-  for (int i = threadIdx.x; i < nr; i += blockDim.x) s_node[i] = row_node[r0 + i];
-  __syncthreads();
-  const int64_t e0 = s_rp[0], e1 = s_rp[nr];
-  const int64_t N0 = g.N[0], N1 = g.N[1];
-  const int64_t n0 = g.n[0], n1 = g.n[1];
-  for (int64_t e = e0 + threadIdx.x; e < e1; e += blockDim.x) {
-    int lo = 0, hi = nr - 1;
-    while (lo < hi) {
-      int mid = (lo + hi + 1) >> 1;
-      if (s_rp[mid] <= e) lo = mid; else hi = mid - 1;
-    }
-    const int64_t lin = s_node[lo];
-    int64_t X[3], Y[3];
-    X[0] = lin % N0;
-    if (DIM == 2) {
-      X[1] = lin / N0;
-    } else {
-      int64_t t = lin / N0;
-      X[1] = t % N1;
-      X[2] = t / N1;
-    }
-    int c = (int)code[e];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      Y[d] = X[d] + (c % L::W) - K;
-      c /= L::W;
-    }
-    int64_t clo[3], chi[3];
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      int64_t mn = X[d] < Y[d] ? X[d] : Y[d];
-      int64_t mx = X[d] < Y[d] ? Y[d] : X[d];
-      int64_t lo_c = mx <= K ? 0 : (mx - 1) / K;
-      int64_t hi_c = mn / K;
-      const int64_t nd = d == 0 ? n0 : (d == 1 ? n1 : g.n[2]);
-      if (hi_c > nd - 1) hi_c = nd - 1;
-      clo[d] = lo_c;
-      chi[d] = hi_c;
-    }
-    double v = 0.0;
-    if (DIM == 2) {
-      for (int64_t cy = clo[1]; cy <= chi[1]; ++cy)
-        for (int64_t cx = clo[0]; cx <= chi[0]; ++cx) {
-          const int li = (int)(X[0] - K * cx) + L::KP1 * (int)(X[1] - K * cy);
-          const int lj = (int)(Y[0] - K * cx) + L::KP1 * (int)(Y[1] - K * cy);
-          v += __ldg(kappa + cx + n0 * cy) * s_K[li * L::NN + lj];
-        }
-    } else {
-      for (int64_t cz = clo[2]; cz <= chi[2]; ++cz)
-        for (int64_t cy = clo[1]; cy <= chi[1]; ++cy)
-          for (int64_t cx = clo[0]; cx <= chi[0]; ++cx) {
-            const int li = (int)(X[0] - K * cx) + L::KP1 * ((int)(X[1] - K * cy) + L::KP1 * (int)(X[2] - K * cz));
-            const int lj = (int)(Y[0] - K * cx) + L::KP1 * ((int)(Y[1] - K * cy) + L::KP1 * (int)(Y[2] - K * cz));
-            v += __ldg(kappa + cx + n0 * (cy + n1 * cz)) * s_K[li * L::NN + lj];
-          }
-    }
-    vals[e] = v;
-  }
-}
-
-// ---- Q_k (k >= 2) values: one warp per owned row -------------------------------------------
-// The row's node X and the coefficients of the (up to 2^DIM) cells around it are decoded
-// once per warp; the lanes then walk the row's entries (coalesced stencil codes in,
-// coalesced values out).  Along each direction the node sits either on a cell boundary
-// (X % K == 0: cells "below" = slot 0 and "above" = slot 1) or inside one cell (slot 1);
-// entry (X, X+o) sums kappa_c * Khat[X in c][X+o in c] over the slots whose cell holds
-// both nodes: o_d < 0 -> slot 0, o_d > 0 -> slot 1, o_d = 0 -> both.
+// ---- Q_k values and right-hand side (row bodies in gd_rows.cuh) ---------------------------
+// One warp per owned row; the reference stiffness table is staged in shared memory.
 template <int DIM, int K, typename CodeT>
 __global__ void __launch_bounds__(256)
 k_numeric_qk_rows(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
                   const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
                   double* __restrict__ vals) {
   using L = Lat<DIM, K>;
-  constexpr int NC = 1 << DIM;
   __shared__ double s_K[L::NN * L::NN];
   for (int i = threadIdx.x; i < L::NN * L::NN; i += blockDim.x) s_K[i] = Khat[i];
   __syncthreads();
-  const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
-  for (int64_t r = warp; r < nrows_own; r += nwarps) {
-    const uint32_t lin = (uint32_t)row_node[r];
-    int X[3], q[3], rm[3];
-    X[0] = (int)(lin % N0);
-    if (DIM == 3) {
-      const uint32_t t = lin / N0;
-      X[1] = (int)(t % N1);
-      X[2] = (int)(t / N1);
-    } else {
-      X[1] = (int)(lin / N0);
-      X[2] = 0;
-    }
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      q[d] = X[d] / K;
-      rm[d] = X[d] % K;
-    }
-    // coefficient of slot a (lane a loads it, then broadcast)
-    double kv = 0.0;
-    bool slot_ok = false;
-    if (lane < NC) {
-      bool ok = true;
-      int64_t cl = 0, stride = 1;
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        const int sd = (lane >> d) & 1;
-        const int c = sd ? q[d] : q[d] - 1;
-        if (!sd && rm[d] != 0) ok = false;
-        if (c < 0 || c >= g.n[d]) ok = false;
-        cl += stride * c;
-        stride *= g.n[d];
-      }
-      kv = ok ? __ldg(kappa + cl) : 0.0;
-      slot_ok = ok;
-    }
-    const uint32_t vmask = __ballot_sync(0xffffffffu, slot_ok);   // valid slots (integer test, not FP64)
-    double kap[NC];
-#pragma unroll
-    for (int a = 0; a < NC; ++a) kap[a] = __shfl_sync(0xffffffffu, kv, a);
-    const int64_t e0 = rowptr[r], e1 = rowptr[r + 1];
-    for (int64_t e = e0 + lane; e < e1; e += 32) {
-      int cv = (int)code[e];
-      int o[3] = {0, 0, 0};
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        o[d] = cv % L::W - K;
-        cv /= L::W;
-      }
-      double v = 0.0;
-#pragma unroll
-      for (int a = 0; a < NC; ++a) {
-        bool ok = (vmask >> a) & 1u;
-        int lx = 0, ly = 0, mul = 1;
-#pragma unroll
-        for (int d = 0; d < DIM; ++d) {
-          const int sd = (a >> d) & 1;
-          if (sd == 0 && (rm[d] != 0 || o[d] > 0)) ok = false;
-          if (sd == 1 && rm[d] == 0 && o[d] < 0) ok = false;
-          const int lxd = sd ? rm[d] : K;
-          lx += mul * lxd;
-          ly += mul * (lxd + o[d]);
-          mul *= L::KP1;
-        }
-        if (ok) v = fma(kap[a], s_K[lx * L::NN + ly], v);
-      }
-      vals[e] = v;
-    }
-  }
+  for (int64_t r = warp; r < nrows_own; r += nwarps)
+    qk_matrix_row<DIM, K, CodeT>(g, r, rowptr, row_node, code, kappa, s_K, vals);
 }
 
-// ---- right-hand side: f-term and Dirichlet lifting, one thread per owned row -----------
+// one thread per owned row
 template <int DIM, int K>
 __global__ void k_numeric_rhs(Geom g, int64_t nrows_own, const int32_t* __restrict__ row_node,
                               const double* __restrict__ kappa, const double* __restrict__ Khat,
                               const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
                               const double* __restrict__ f_nodal, const double* __restrict__ u_dir,
                               double* __restrict__ rhs, int32_t* __restrict__ bad) {
-  using L = Lat<DIM, K>;
-  // The element tables are small and read through the read-only cache.
-  const double* __restrict__ s_K = Khat;
-  const double* __restrict__ s_M = Mhat;
-  const double* __restrict__ s_F = Fhat;
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows_own) return;
-  int64_t lin = row_node[r];
-  int64_t X[3] = {0, 0, 0};
-  for (int d = 0; d < DIM; ++d) {
-    X[d] = lin % g.N[d];
-    lin /= g.N[d];
-  }
-  int64_t clo[3] = {0, 0, 0}, chi[3] = {0, 0, 0};
-  for (int d = 0; d < DIM; ++d) {
-    int64_t c = X[d] / K;
-    if (X[d] % K == 0) {
-      clo[d] = c - 1 < 0 ? 0 : c - 1;
-      chi[d] = c > g.n[d] - 1 ? g.n[d] - 1 : c;
-    } else {
-      clo[d] = chi[d] = c;
-    }
-  }
-  double b = 0.0;
-  int nbad = 0;
-  for (int64_t cz = clo[2]; cz <= chi[2]; ++cz)
-    for (int64_t cy = clo[1]; cy <= chi[1]; ++cy)
-      for (int64_t cx = clo[0]; cx <= chi[0]; ++cx) {
-        const int64_t cc[3] = {cx, cy, cz};
-        const double kap = kappa ? __ldg(kappa + cell_lin(g, cc)) : 1.0;
-        if (!(kap > 0.0) || !isfinite(kap)) ++nbad;
-        int li = 0;
-        for (int d = DIM - 1; d >= 0; --d) li = li * L::KP1 + (int)(X[d] - K * cc[d]);
-        if (!f_nodal) b += f_const * s_F[li];
-        if (f_nodal || u_dir) {
-          for (int lj = 0; lj < L::NN; ++lj) {
-            int64_t Y[3] = {0, 0, 0};
-            for (int d = 0, rest = lj; d < DIM; ++d) {
-              Y[d] = K * cc[d] + rest % L::KP1;
-              rest /= L::KP1;
-            }
-            const int64_t ylin = lattice_lin(g, Y);
-            if (f_nodal) b += s_M[li * L::NN + lj] * __ldg(f_nodal + ylin);
-            if (u_dir && node_is_dirichlet(g, Y)) b -= kap * s_K[li * L::NN + lj] * __ldg(u_dir + ylin);
-          }
-        }
-      }
-  rhs[r] = b;
+  const int nbad = qk_rhs_row<DIM, K>(g, r, row_node, kappa, Khat, Mhat, Fhat, f_const, f_nodal, u_dir, rhs);
   if (nbad) atomicAdd(bad, nbad);
 }
 
@@ -921,9 +719,7 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   const Geom& g = A->test->geom;
   const int64_t R = A->ngdofs;
   if (R == 0) return GD_OK;
-  const unsigned nb = (unsigned)((R + kRowsPerBlock - 1) / kRowsPerBlock);
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
-  (void)nb;
   // one warp per row; grid sized for a few waves of resident blocks
   const unsigned nbw = (unsigned)std::min<int64_t>((R + 7) / 8, 152 * 64);
   if (A->code_bytes == 1)
@@ -1044,7 +840,7 @@ extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nn
   if (ngdofs) *ngdofs = A->ngdofs;
   if (nnz_owned) *nnz_owned = A->nnz_own;
   if (nnz_total) *nnz_total = A->nnz_total;
-  // cube Q1: k_prescale + k_numeric_q1; other Q1: k_numeric_q1; Q_k: k_numeric_matrix + k_numeric_rhs
+  // cube Q1: k_prescale + k_numeric_q1; other Q1: k_numeric_q1; Q_k: k_numeric_qk_rows + k_numeric_rhs
   if (kernels) *kernels = A->fast_q1 ? (A->q1c_cube ? 2 : 1) : 2;
   return GD_OK;
 }

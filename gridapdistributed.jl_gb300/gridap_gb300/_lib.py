@@ -88,6 +88,14 @@ SIGNATURES = {
     "gd_fe_function_local": [P, C.c_int, P, C.c_int, DP],
     "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
+    "gd_batch_create": [P, P, C.c_int, PP],
+    "gd_batch_destroy": [P],
+    "gd_batch_assemble": [P],
+    "gd_batch_assemble_async": [P],
+    "gd_batch_counts": [P, I32P, I64P, I64P],
+    "gd_batch_tuning": [P, I32P, I32P, I32P, C.POINTER(C.c_float), I32P],
+    "gd_batch_solve": [P, C.c_double, C.c_int, P],
+    "gd_batch_solution": [P, C.c_int, P, C.c_int],
     "gd_learned_create": [P, C.c_int, C.c_uint64, PP],
     "gd_learned_levels": [P, I32P],
     "gd_learned_destroy": [P],

@@ -221,6 +221,32 @@ int gd_solve_noalloc(gd_asm* a, double rtol, int maxit, double* x, int where, gd
 int gd_fe_function_local(const gd_space* space, int part, const double* x_global, int where,
                          double* x_local);
 
+/* ---- batched assembly and solve of many problems ------------------------------
+ * No counterpart in the reference (one problem per assemble_matrix_and_vector call).
+ * A batch holds assemblers whose symbolic phase is done (any order 1..3, 2D or 3D,
+ * one shared context) with their coefficients.  gd_batch_assemble fills every
+ * problem's matrix and vector (what gd_assemble_numeric would, same values) in ONE
+ * persistent kernel launch with dynamic row-task scheduling; the first call times
+ * the candidate launch shapes, keeps the fastest and captures the launch in a CUDA
+ * graph that later calls replay.  gd_batch_solve runs Jacobi-PCG in FP64 on every
+ * problem at once (one launch per CG step for all unconverged problems, sixteen steps
+ * per CUDA graph replay). */
+typedef struct gd_batch gd_batch;
+int gd_batch_create(gd_asm* const* assemblers, const gd_coeffs* coeffs, int nprobs, gd_batch** out);
+int gd_batch_destroy(gd_batch* b);
+int gd_batch_assemble(gd_batch* b);
+/* Same, without the final stream synchronisation and coefficient check (timing loops). */
+int gd_batch_assemble_async(gd_batch* b);
+int gd_batch_counts(const gd_batch* b, int32_t* nprobs, int64_t* rows, int64_t* nnz_owned);
+/* Chosen launch shape (index, rows per task, CTAs per SM) and the measured ms of each
+ * candidate (nshapes of them); -1 before the first assembly. */
+int gd_batch_tuning(const gd_batch* b, int32_t* shape, int32_t* rows_per_task, int32_t* ctas_per_sm,
+                    float* ms_per_shape, int32_t* nshapes);
+/* stats: one entry per problem (may be NULL). */
+int gd_batch_solve(gd_batch* b, double rtol, int maxit, gd_solve_stats* stats);
+/* Solution of problem p (its ngdofs values, gid order) after gd_batch_solve. */
+int gd_batch_solution(const gd_batch* b, int p, double* x, int where);
+
 /* ---- learned preconditioner (3D Q1 on cube cells) ---------------------------------
  * No counterpart in the reference (whose `\` is a gathered LU).  An L-level (1..6,
  * default 3), 8-channel convolutional network on the node lattice, gated by the
