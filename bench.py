@@ -12,7 +12,10 @@ step time), whole job.  `e2e` is the same metric through the C-ABI call with hos
 buffers: kappa copied host->device and the assembled values + rhs copied
 device->host inside every timed step.  `roofline` uses the algorithmic bytes
 8*nnz + 8*n_free + 8*n_cells per assembly against the measured HBM copy bandwidth.
-`solve` reports Jacobi-PCG to 1e-8 relative residual on the assembled system.
+`solve` reports Jacobi-PCG (FP64) and the mixed-precision refinement to 1e-8 relative
+residual on the assembled system; `learned` the learned-preconditioner flexible CG
+against both on 96^3 lognormal diffusion (sigma 1.5); `batched` the 64-problem uneven
+batch (Q1-Q3, 16^3..96^3 cells) assembled one persistent launch per memory wave.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun with N>1 every rank runs its own replica of the workload on its own
@@ -51,6 +54,11 @@ def parse():
     ap.add_argument("--no-solve", action="store_true")
     ap.add_argument("--solve-maxit", type=int, default=20000)
     ap.add_argument("--cells", type=int, default=128, help="cells per direction (default: the 128^3 workload)")
+    ap.add_argument("--batched", default="sample", choices=["off", "sample", "full"],
+                    help="batched 64-problem workload: a bounded first wave (sample), every wave (full) or none")
+    ap.add_argument("--batched-budget-gb", type=float, default=140.0, help="device memory per wave (full)")
+    ap.add_argument("--batched-solve", action="store_true", help="also Jacobi-PCG every batched problem")
+    ap.add_argument("--no-learned", action="store_true")
     return ap.parse_args()
 
 
@@ -205,6 +213,148 @@ def run_reference(args, rank, world):
 
 
 # ------------------------------------------------------------------------------------
+# batched uneven workload (64 problems, Q1-Q3, 16^3..96^3 cells)
+# ------------------------------------------------------------------------------------
+def run_batched(args, be, stream, dev, mode):
+    """One persistent launch per wave of problems that fits the device-memory budget;
+    value = all assembled entries / the summed per-wave assembly time."""
+    import gc
+    import torch
+    import gridap_gb300 as G
+    from gridap_gb300.batch import BatchedAssembler
+    from gridap_gb300.synthetic import BATCHED3D_64, batched_draw, batched_kappa, batched_nnz_estimate
+    w = BATCHED3D_64
+    draw = batched_draw(w)
+    bytes_per_entry = 30.0   # values, column ids, stencil codes and symbolic scratch
+    budget = (16.0 if mode == "sample" else args.batched_budget_gb) * 1e9
+    waves, cur, cur_b = [], [], 0.0
+    for i, (n, k, ks) in enumerate(draw):
+        b = batched_nnz_estimate(n, k)[1] * bytes_per_entry
+        if cur and cur_b + b > budget:
+            waves.append(cur)
+            cur, cur_b = [], 0.0
+            if mode == "sample":
+                break
+        cur.append(i)
+        cur_b += b
+    if cur and (mode == "full" or not waves):
+        waves.append(cur)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    tot_nnz = tot_rows = tot_cells = 0
+    tot_ms = 0.0
+    wave_out = []
+    solve_out = []
+    for wi, idx in enumerate(waves):
+        built = []
+        t0 = time.perf_counter()
+        for i in idx:
+            n, k, ks = draw[i]
+            ranks = be.distribute(range(int(np.prod(w["parts"]))))
+            model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], (n, n, n))
+            V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, k), dirichlet_tags="boundary")
+            U = G.TrialFESpace(0.0, V)
+            dO = G.Measure(G.Triangulation(model), 2 * k)
+            assem = G.SparseMatrixAssembler(U, V, G.SubAssembledRows())
+            assem.symbolic()
+            built.append((model, V, U, assem, G.integral_grad_grad(batched_kappa(n, ks, w["sigma"]), dO),
+                          G.integral_source(w["f"], dO)))
+        t_setup = time.perf_counter() - t0
+        B = BatchedAssembler([(assem, a, l) for (_, _, _, assem, a, l) in built])
+        B.assemble()   # autotune + graph capture
+        cnt = B.counts()
+        for _ in range(max(args.warmup, 3)):
+            B.assemble(sync=False)
+        torch.cuda.synchronize()
+        steps = max(3, min(args.steps, 10))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            B.assemble(sync=False)
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        cells = sum(draw[i][0] ** 3 for i in idx)
+        tot_nnz += cnt["nnz_owned"]
+        tot_rows += cnt["rows"]
+        tot_cells += cells
+        tot_ms += ms
+        wave_out.append({"problems": len(idx), "nnz": cnt["nnz_owned"], "rows": cnt["rows"], "ms": ms,
+                         "setup_s": t_setup, "tuning": B.tuning()})
+        if args.batched_solve:
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            st = B.solve(rtol=1e-8, maxit=args.solve_maxit)
+            t_solve = time.perf_counter() - t0
+            solve_out.append({"wave": wi, "seconds": t_solve, "max_iterations": max(x.iterations for x in st),
+                              "all_converged": all(bool(x.converged) for x in st)})
+        B.close()
+        del B, built
+        gc.collect()
+        torch.cuda.synchronize()
+    peak, peak_kind = measured_peaks()
+    alg = 8 * tot_nnz + 8 * tot_rows + 8 * tot_cells
+    gbs = alg / (tot_ms * 1e-3) / 1e9 if tot_ms > 0 else 0.0
+    return {"workload": w["name"], "mode": mode, "problems": sum(len(x) for x in waves),
+            "problems_in_draw": len(draw), "nnz": tot_nnz, "rows": tot_rows, "ms": tot_ms,
+            "nnz_per_s": tot_nnz / (tot_ms * 1e-3) if tot_ms > 0 else None,
+            "roofline": {"bound": "hbm", "achieved": gbs, "peak": peak, "unit": "GB/s", "frac": gbs / peak,
+                         "peak_kind": peak_kind, "algorithmic_bytes": alg},
+            "launches_per_wave_step": 1, "waves": wave_out, "solve": solve_out or None,
+            "note": "each wave: one persistent kernel launch (CUDA graph replay) over all of its problems"}
+
+
+# ------------------------------------------------------------------------------------
+# learned preconditioner vs Jacobi (96^3 lognormal diffusion)
+# ------------------------------------------------------------------------------------
+def run_learned(args, be, dev):
+    import torch
+    import gridap_gb300 as G
+    from gridap_gb300.learned import LearnedPreconditioner
+    from gridap_gb300.synthetic import DIFFUSION3D_96, lognormal_kappa
+    w = DIFFUSION3D_96
+    path = PKG / "gridap_gb300" / "weights" / "diffusion3d_q1_l4.gdlp"
+    if not path.exists():
+        return None
+    cells = w["cells"]
+    ranks = be.distribute(range(int(np.prod(w["parts"]))))
+    model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], cells)
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 1), dirichlet_tags="boundary")
+    U = G.TrialFESpace(0.0, V)
+    dO = G.Measure(G.Triangulation(model), 2)
+    kap = lognormal_kappa(cells, w["sigma"], w["corr_len"], seed=w["seed"] + 1)
+    f = np.random.default_rng(w["seed"] + 100).standard_normal(int(np.prod([c + 1 for c in cells])))
+    op = G.AffineFEOperator(G.integral_grad_grad(kap, dO), G.integral_source(f, dO), U, V)
+    net = LearnedPreconditioner(op.matrix, seed=0, levels=LearnedPreconditioner.file_levels(path))
+    net.load(path)
+    out = {"workload": w["name"], "rtol": 1e-8, "weights": path.name, "levels": net.levels,
+           "params": net.num_params}
+    runs = {}
+    for name, fn in (("jacobi_pcg_fp64", lambda: op.matrix.solve(rtol=1e-8, method="jacobi_pcg")),
+                     ("mixed_ir_jacobi", lambda: op.matrix.solve(rtol=1e-8, method="mixed_ir")),
+                     ("learned_fcg", lambda: net.solve(rtol=1e-8))):
+        fn()   # warm
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        r = fn()
+        t = time.perf_counter() - t0
+        if name == "learned_fcg":
+            x, st, fb = r
+            runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                          "converged": bool(st.converged), "fallback_to_jacobi": fb}
+        else:
+            st = op.matrix.last_stats
+            runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                          "converged": bool(st.converged)}
+    out.update(runs)
+    tl = runs["learned_fcg"]["seconds"]
+    out["speedup_vs_jacobi_pcg_fp64"] = runs["jacobi_pcg_fp64"]["seconds"] / tl
+    out["speedup_vs_mixed_ir_jacobi"] = runs["mixed_ir_jacobi"]["seconds"] / tl
+    net.close()
+    return out
+
+
+# ------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------
 def run_gb300(args, rank, world, local):
@@ -340,6 +490,13 @@ def run_gb300(args, rank, world, local):
                            "rel_residual": st.rel_residual, "converged": bool(st.converged and rc == 0),
                            "ms_per_iteration": 1e3 * t_solve / max(st.iterations, 1)}
 
+    learned = None
+    if not args.no_learned:
+        learned = run_learned(args, be, dev)
+    batched = None
+    if args.batched != "off":
+        batched = run_batched(args, be, stream, dev, args.batched)
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         threads = int(np.prod(w["parts"]))
@@ -374,6 +531,8 @@ def run_gb300(args, rank, world, local):
             "symbolic_s": t_sym,
             "wall_s_timed_region": t_wall,
             "solve": solve,
+            "learned": learned,
+            "batched": batched,
             "cpu_baseline": cpu,
         }
         print(json.dumps(line), flush=True)

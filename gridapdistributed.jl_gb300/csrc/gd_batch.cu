@@ -6,7 +6,7 @@
 // number of consecutive owned rows of one problem) from an atomic counter, problems of
 // higher order (costlier rows) and more rows first, so uneven problems balance without
 // per-problem launches.  A task runs the same row bodies as the single-problem Q_k
-// kernels (gd_rows.cuh: one warp per matrix row, one thread per right-hand-side row), so
+// kernels (gd_rows.cuh: lane groups of a warp per matrix row, one thread per right-hand-side row), so
 // every problem's values equal what its own assembler would compute.  The launch shape
 // (rows per task, CTAs per SM) is chosen by timing candidates on the first call; the
 // counter reset and the launch are then captured in a CUDA graph and replayed.
@@ -58,34 +58,45 @@ struct BScal {
 };
 
 constexpr int kBatchThreads = 256;
+constexpr int kBatchMaxKhat = 64 * 64;    // doubles of the largest reference stiffness table (3D Q3)
+constexpr int kBatchMaxEtab = 8 * 343;    // entries of the largest entry table (3D Q3)
+constexpr size_t kBatchSmem = sizeof(double) * kBatchMaxKhat + sizeof(uint16_t) * kBatchMaxEtab;
 constexpr int kSolveRows = 128;   // rows per solve task
 constexpr int kSolveStepsPerGraph = 16;
 
 struct BatchShape {
   int rows, per_sm;
 };
-constexpr BatchShape kBatchShapes[] = {{32, 4}, {64, 4}, {128, 4}, {64, 2}, {128, 2}, {256, 2}, {32, 8}, {64, 8}};
+constexpr BatchShape kBatchShapes[] = {{32, 3}, {64, 3}, {128, 3}, {256, 3}, {64, 2}, {128, 2}, {256, 2}, {128, 4}};
 constexpr int kNumBatchShapes = 8;
 
 // ---- assembly -------------------------------------------------------------------------
 template <int DIM, int K, typename CodeT>
-__device__ __forceinline__ void batch_task(const BatchProb& P, int64_t r0, int64_t r1, int& nbad) {
+__device__ __forceinline__ void batch_task(const BatchProb& P, int64_t r0, int64_t r1, const double* sK,
+                                           const uint16_t* etab, double* skap, int* slx, int& nbad) {
+  constexpr int RPW = RowLanes<DIM, K>::RPW;
   const int warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  for (int64_t r = r0 + warp; r < r1; r += nw)
-    qk_matrix_row<DIM, K, CodeT>(P.g, r, P.rowptr, P.row_node, (const CodeT*)P.code, P.kappa, P.Khat, P.vals);
+  for (int64_t rb = r0 + warp * RPW; rb < r1; rb += nw * RPW)
+    qk_matrix_rows<DIM, K, CodeT>(P.g, rb, r1, P.rowptr, P.row_node, (const CodeT*)P.code, P.kappa, sK, etab,
+                                  P.vals, skap + 32 * warp, slx + 32 * warp);
   for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
     nbad += qk_rhs_row<DIM, K>(P.g, r, P.row_node, P.kappa, P.Khat, P.Mhat, P.Fhat, P.f_const, P.f_nodal, P.u_dir,
                                P.rhs);
 }
 
 // tstart[j] = first task of the j-th problem in schedule order ord[j]; tstart[nprobs] = total
-__global__ void __launch_bounds__(kBatchThreads)
+__global__ void __launch_bounds__(kBatchThreads, 3)
 k_batch_numeric(const BatchProb* __restrict__ probs, const int32_t* __restrict__ ord,
                 const int64_t* __restrict__ tstart, int nprobs, int rows_per_task, unsigned long long* next,
                 int32_t* bad) {
+  extern __shared__ double sK[];   // reference stiffness table of the current problem, then its entry table
   __shared__ long long s_task;
+  __shared__ int s_prob;
+  __shared__ double s_kap[kBatchThreads / 32 * 32];
+  __shared__ int s_lx[kBatchThreads / 32 * 32];
   int nbad = 0;
   const int64_t total = tstart[nprobs];
+  if (threadIdx.x == 0) s_prob = -1;
   while (true) {
     __syncthreads();   // every thread has read the previous task id
     if (threadIdx.x == 0) s_task = (long long)atomicAdd(next, 1ull);
@@ -98,16 +109,35 @@ k_batch_numeric(const BatchProb* __restrict__ probs, const int32_t* __restrict__
       if (tstart[mid] <= t) lo = mid;
       else hi = mid - 1;
     }
-    const BatchProb& P = probs[ord[lo]];
+    const int pid = ord[lo];
+    const BatchProb& P = probs[pid];
+    uint16_t* etab = reinterpret_cast<uint16_t*>(sK + kBatchMaxKhat);
+    if (pid != s_prob) {   // uniform across the block
+      __syncthreads();      // the previous problem's tables are no longer read
+      int nn = 1;
+      for (int d = 0; d < P.g.dim; ++d) nn *= P.k + 1;
+      for (int i = threadIdx.x; i < nn * nn; i += blockDim.x) sK[i] = P.Khat[i];
+      switch (P.g.dim * 10 + P.k) {
+        case 31: build_entry_tab<3, 1>(etab); break;
+        case 32: build_entry_tab<3, 2>(etab); break;
+        case 33: build_entry_tab<3, 3>(etab); break;
+        case 21: build_entry_tab<2, 1>(etab); break;
+        case 22: build_entry_tab<2, 2>(etab); break;
+        case 23: build_entry_tab<2, 3>(etab); break;
+        default: break;
+      }
+      __syncthreads();
+      if (threadIdx.x == 0) s_prob = pid;
+    }
     const int64_t r0 = (t - tstart[lo]) * rows_per_task;
     const int64_t r1 = r0 + rows_per_task < P.nrows ? r0 + rows_per_task : P.nrows;
     switch (P.g.dim * 10 + P.k) {
-      case 31: batch_task<3, 1, uint8_t>(P, r0, r1, nbad); break;
-      case 32: batch_task<3, 2, uint8_t>(P, r0, r1, nbad); break;
-      case 33: batch_task<3, 3, uint16_t>(P, r0, r1, nbad); break;
-      case 21: batch_task<2, 1, uint8_t>(P, r0, r1, nbad); break;
-      case 22: batch_task<2, 2, uint8_t>(P, r0, r1, nbad); break;
-      case 23: batch_task<2, 3, uint8_t>(P, r0, r1, nbad); break;
+      case 31: batch_task<3, 1, uint8_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
+      case 32: batch_task<3, 2, uint8_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
+      case 33: batch_task<3, 3, uint16_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
+      case 21: batch_task<2, 1, uint8_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
+      case 22: batch_task<2, 2, uint8_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
+      case 23: batch_task<2, 3, uint8_t>(P, r0, r1, sK, etab, s_kap, s_lx, nbad); break;
       default: break;
     }
   }
@@ -343,8 +373,9 @@ static int upload_tasks(gd_batch* B, int rows_per_task, cudaStream_t st) {
 static int launch_batch(gd_batch* B, int shape, cudaStream_t st) {
   const BatchShape s = kBatchShapes[shape];
   GD_CUDA_TRY(cudaMemsetAsync(B->counter.p, 0, sizeof(unsigned long long), st));
-  k_batch_numeric<<<sm_count() * s.per_sm, kBatchThreads, 0, st>>>(B->probs.p, B->d_ord.p, B->tstart.p,
-                                                                   (int)B->hp.size(), s.rows, B->counter.p, B->bad.p);
+  k_batch_numeric<<<sm_count() * s.per_sm, kBatchThreads, kBatchSmem, st>>>(B->probs.p, B->d_ord.p, B->tstart.p,
+                                                                          (int)B->hp.size(), s.rows, B->counter.p,
+                                                                          B->bad.p);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }

@@ -178,20 +178,28 @@ int reference_element(gd_asm* A, int degree) {
 }
 
 // ---- Q_k values and right-hand side (row bodies in gd_rows.cuh) ---------------------------
-// One warp per owned row; the reference stiffness table is staged in shared memory.
+// Lane groups of a warp take owned rows; the reference stiffness table is staged in
+// shared memory.
 template <int DIM, int K, typename CodeT>
 __global__ void __launch_bounds__(256)
 k_numeric_qk_rows(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
                   const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
                   double* __restrict__ vals) {
   using L = Lat<DIM, K>;
+  constexpr int RPW = RowLanes<DIM, K>::RPW;
   __shared__ double s_K[L::NN * L::NN];
+  __shared__ double s_kap[8][32];
+  __shared__ int s_lx[8][32];
+  __shared__ uint16_t s_tab[EntryTab<DIM, K>::SIZE];
   for (int i = threadIdx.x; i < L::NN * L::NN; i += blockDim.x) s_K[i] = Khat[i];
+  build_entry_tab<DIM, K>(s_tab);
   __syncthreads();
+  const int wl = threadIdx.x >> 5;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-  for (int64_t r = warp; r < nrows_own; r += nwarps)
-    qk_matrix_row<DIM, K, CodeT>(g, r, rowptr, row_node, code, kappa, s_K, vals);
+  for (int64_t rb = warp * RPW; rb < nrows_own; rb += nwarps * RPW)
+    qk_matrix_rows<DIM, K, CodeT>(g, rb, nrows_own, rowptr, row_node, code, kappa, s_K, s_tab, vals, s_kap[wl],
+                                  s_lx[wl]);
 }
 
 // one thread per owned row

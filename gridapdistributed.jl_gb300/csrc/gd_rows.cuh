@@ -12,25 +12,81 @@ struct Lat {
   static constexpr int W = 2 * K + 1;
 };
 
-// Matrix values of owned row r, computed by one warp (all 32 lanes call it).
-// The row's node X and the coefficients of the (up to 2^DIM) cells around it are decoded
-// once per warp; the lanes then walk the row's entries (coalesced stencil codes in,
-// coalesced values out).  Along each direction the node sits either on a cell boundary
-// (X % K == 0: cells "below" = slot 0 and "above" = slot 1) or inside one cell (slot 1);
-// entry (X, X+o) sums kappa_c * Khat[X in c][X+o in c] over the slots whose cell holds
-// both nodes: o_d < 0 -> slot 0, o_d > 0 -> slot 1, o_d = 0 -> both.  Kt is the
-// reference stiffness table (shared or global memory).
+// Lanes per matrix row: a row of a Q_k stencil has at most (2k+1)^DIM entries, so a
+// warp takes 4 rows of at most 32 entries (8 lanes each), 2 rows of at most 128 (16
+// lanes each) or one longer row; the per-row decoding below is then shared by 4, 2 or
+// 1 rows per warp instruction.
+// Entry table of a (DIM, K) stencil: for every stencil code (W-ary digits o_d + K) and
+// every set of directions in which the row's node sits on a cell boundary (3 bits), the
+// packed entry: bits 0-7 off(o) + 128, bits 8-10 slot bits forced to 1, bits 11-13
+// slot bits that take both values.  One shared-memory lookup then replaces the digit
+// decoding of every entry.
+template <int DIM, int K>
+struct EntryTab {
+  static constexpr int W = 2 * K + 1;
+  static constexpr int E = DIM == 3 ? W * W * W : W * W;
+  static constexpr int SIZE = 8 * E;
+};
+
+template <int DIM, int K>
+__device__ __forceinline__ void build_entry_tab(uint16_t* tab) {
+  using T = EntryTab<DIM, K>;
+  constexpr int KP1 = K + 1;
+  for (int i = threadIdx.x; i < T::SIZE; i += blockDim.x) {
+    const int onb = i / T::E;
+    int cv = i % T::E;
+    int off = 0, fixed = 0, both = 0, mul = 1;
+    for (int d = 0; d < DIM; ++d) {
+      const int od = cv % T::W - K;
+      cv /= T::W;
+      off += od * mul;
+      mul *= KP1;
+      if (od > 0 || !((onb >> d) & 1)) fixed |= 1 << d;
+      else if (od == 0) both |= 1 << d;
+    }
+    tab[i] = (uint16_t)((off + 128) | (fixed << 8) | (both << 11));
+  }
+}
+
+template <int DIM, int K>
+struct RowLanes {
+  static constexpr int W = 2 * K + 1;
+  static constexpr int E = DIM == 3 ? W * W * W : W * W;
+  static constexpr int G = E <= 32 ? 8 : (E <= 128 ? 16 : 32);
+  static constexpr int RPW = 32 / G;   // rows per warp
+};
+
+// Matrix values of owned rows rbase .. rbase+RPW-1 (those < rend), one lane group of G
+// lanes per row; all 32 lanes of the warp call it.
+// Along each direction the row's node X sits either on a cell boundary (X % K == 0:
+// cells "below" = slot bit 0 and "above" = slot bit 1) or inside one cell (bit 1).
+// Entry (X, X+o) sums kappa_c * Khat[X in c][X+o in c] over the slots whose cell holds
+// both nodes: per direction o_d < 0 -> bit 0, o_d > 0 -> bit 1, o_d = 0 -> both when X
+// is on a cell boundary, bit 1 inside a cell.  With lx(a) the local index of X in slot
+// a's cell, the local index of X+o there is lx(a) + off(o), off = sum o_d (K+1)^d, so an
+// entry is sum over its (usually one) slots of kap[a] * Khat[lx(a) (NN + 1) + off].
+// The first 2^DIM lanes of a group decode the slots (coefficient, lx, validity) into
+// the warp's shared-memory slot tables (skap: 32 doubles, slx: 32 ints); the group then
+// walks its row's entries (coalesced stencil codes in, coalesced values out), each
+// entry's offset and slots read from the entry table etab (build_entry_tab).  Kt is
+// the reference stiffness table (shared or global memory).
 template <int DIM, int K, typename CodeT>
-__device__ __forceinline__ void qk_matrix_row(const Geom& g, int64_t r, const int64_t* __restrict__ rowptr,
-                                              const int32_t* __restrict__ row_node, const CodeT* __restrict__ code,
-                                              const double* __restrict__ kappa, const double* Kt,
-                                              double* __restrict__ vals) {
+__device__ __forceinline__ void qk_matrix_rows(const Geom& g, int64_t rbase, int64_t rend,
+                                               const int64_t* __restrict__ rowptr,
+                                               const int32_t* __restrict__ row_node, const CodeT* __restrict__ code,
+                                               const double* __restrict__ kappa, const double* Kt,
+                                               const uint16_t* etab, double* __restrict__ vals, double* skap,
+                                               int* slx) {
   using L = Lat<DIM, K>;
+  using RL = RowLanes<DIM, K>;
   constexpr int NC = 1 << DIM;
-  const int lane = threadIdx.x & 31;
+  constexpr int G = RL::G;
+  const int lane = threadIdx.x & 31, sub = lane / G, gl = lane % G;
+  const int64_t r = rbase + sub;
+  const bool live = r < rend;
   const uint32_t N0 = (uint32_t)g.N[0], N1 = (uint32_t)g.N[1];
-  const uint32_t lin = (uint32_t)row_node[r];
-  int X[3], q[3], rm[3];
+  const uint32_t lin = live ? (uint32_t)row_node[r] : 0u;
+  int X[3], rm[3];
   X[0] = (int)(lin % N0);
   if (DIM == 3) {
     const uint32_t t = lin / N0;
@@ -40,61 +96,56 @@ __device__ __forceinline__ void qk_matrix_row(const Geom& g, int64_t r, const in
     X[1] = (int)(lin / N0);
     X[2] = 0;
   }
+  int onb = 0;   // bit d: X on a cell boundary along d
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    q[d] = X[d] / K;
     rm[d] = X[d] % K;
+    if (rm[d] == 0) onb |= 1 << d;
   }
-  // coefficient of slot a (lane a loads it, then broadcast)
-  double kv = 0.0;
   bool slot_ok = false;
-  if (lane < NC) {
+  if (live && gl < NC) {
     bool ok = true;
-    int64_t cl = 0, stride = 1;
+    int cl = 0, stride = 1;   // cell ids stay below 2^31 (checked when the space is created)
+    int lx = 0, mul = 1;
 #pragma unroll
     for (int d = 0; d < DIM; ++d) {
-      const int sd = (lane >> d) & 1;
-      const int c = sd ? q[d] : q[d] - 1;
+      const int sd = (gl >> d) & 1;
+      const int c = sd ? X[d] / K : X[d] / K - 1;
       if (!sd && rm[d] != 0) ok = false;
-      if (c < 0 || c >= g.n[d]) ok = false;
+      if (c < 0 || c >= (int)g.n[d]) ok = false;
       cl += stride * c;
-      stride *= g.n[d];
+      stride *= (int)g.n[d];
+      lx += mul * (sd ? rm[d] : K);
+      mul *= L::KP1;
     }
-    kv = ok ? __ldg(kappa + cl) : 0.0;
+    skap[sub * NC + gl] = ok ? __ldg(kappa + cl) : 0.0;
+    slx[sub * NC + gl] = lx * (L::NN + 1);
     slot_ok = ok;
   }
-  const uint32_t vmask = __ballot_sync(0xffffffffu, slot_ok);   // valid slots (integer test, not FP64)
-  double kap[NC];
-#pragma unroll
-  for (int a = 0; a < NC; ++a) kap[a] = __shfl_sync(0xffffffffu, kv, a);
-  const int64_t e0 = rowptr[r], e1 = rowptr[r + 1];
-  for (int64_t e = e0 + lane; e < e1; e += 32) {
-    int cv = (int)code[e];
-    int o[3] = {0, 0, 0};
-#pragma unroll
-    for (int d = 0; d < DIM; ++d) {
-      o[d] = cv % L::W - K;
-      cv /= L::W;
-    }
-    double v = 0.0;
-#pragma unroll
-    for (int a = 0; a < NC; ++a) {
-      bool ok = (vmask >> a) & 1u;
-      int lx = 0, ly = 0, mul = 1;
-#pragma unroll
-      for (int d = 0; d < DIM; ++d) {
-        const int sd = (a >> d) & 1;
-        if (sd == 0 && (rm[d] != 0 || o[d] > 0)) ok = false;
-        if (sd == 1 && rm[d] == 0 && o[d] < 0) ok = false;
-        const int lxd = sd ? rm[d] : K;
-        lx += mul * lxd;
-        ly += mul * (lxd + o[d]);
-        mul *= L::KP1;
+  const uint32_t vmask = (__ballot_sync(0xffffffffu, slot_ok) >> (sub * G)) & ((1u << NC) - 1);   // valid slots
+  __syncwarp();
+  if (live) {
+    const double* sk = skap + sub * NC;
+    const int* sl = slx + sub * NC;
+    const int64_t e0 = rowptr[r], e1 = rowptr[r + 1];
+    const uint16_t* et = etab + onb * EntryTab<DIM, K>::E;
+    for (int64_t e = e0 + gl; e < e1; e += G) {
+      const int info = et[(int)code[e]];
+      const int off = (info & 255) - 128;
+      const int fixed = (info >> 8) & 7;   // only the cell above
+      const int both = (info >> 11) & 7;   // both cells (node on a boundary, o_d = 0)
+      double v = 0.0;
+      int sb = both;
+      while (true) {
+        const int a = fixed | sb;
+        if ((vmask >> a) & 1u) v = fma(sk[a], Kt[sl[a] + off], v);
+        if (sb == 0) break;
+        sb = (sb - 1) & both;
       }
-      if (ok) v = fma(kap[a], Kt[lx * L::NN + ly], v);
+      vals[e] = v;
     }
-    vals[e] = v;
   }
+  __syncwarp();
 }
 
 // Right-hand side of owned row r (source term and Dirichlet lifting), one thread.

@@ -77,3 +77,36 @@ def gaussian_random_field_torch(cells, sigma=1.0, corr_len=0.1, seed=0, domain_l
 DIFFUSION3D_96 = dict(name="diffusion3d_q1_96^3_parts2x2x2_sigma1.5", dim=3, cells=(96, 96, 96), parts=(2, 2, 2),
                       domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=1, degree=2, sigma=1.5, corr_len=0.05,
                       seed=5000)
+
+
+# Batched uneven workload: 64 independent 3D diffusion problems, cells per direction
+# n ~ U{16..96}, order k ~ U{1,2,3}, kappa lognormal i.i.d. per cell (sigma 1), f = 1,
+# homogeneous Dirichlet, parts (2,2,1) per problem.  Draw: numpy PCG64(seed); problem i's
+# kappa uses PCG64(seed + 1 + i).
+BATCHED3D_64 = dict(name="batched64_3d_q1-q3_16-96cells_parts2x2x1", nprobs=64, cells=(16, 96), orders=(1, 2, 3),
+                    sigma=1.0, parts=(2, 2, 1), domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), f=1.0, seed=3000)
+
+
+def batched_draw(w=BATCHED3D_64):
+    """[(n, k, kappa_seed)] for the batch, in draw order."""
+    rng = np.random.Generator(np.random.PCG64(w["seed"]))
+    lo, hi = w["cells"]
+    out = []
+    for i in range(w["nprobs"]):
+        n = int(rng.integers(lo, hi + 1))
+        k = int(rng.integers(min(w["orders"]), max(w["orders"]) + 1))
+        out.append((n, k, w["seed"] + 1 + i))
+    return out
+
+
+def batched_kappa(n, seed, sigma=1.0):
+    rng = np.random.Generator(np.random.PCG64(seed))
+    return np.exp(sigma * rng.standard_normal(n ** 3))
+
+
+def batched_nnz_estimate(n, k):
+    """Free DOFs and stored owned-row entries of one problem (all-Dirichlet): a Q_k node
+    couples with 2k+1 nodes per direction at a cell vertex and k+1 inside a cell, so on
+    average k+2 per direction."""
+    dofs = (k * n - 1) ** 3
+    return dofs, dofs * (k + 2) ** 3
