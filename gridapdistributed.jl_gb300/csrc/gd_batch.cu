@@ -454,6 +454,7 @@ extern "C" int gd_batch_create(gd_asm* const* asms, const gd_coeffs* coeffs, int
     gd_asm* A = asms[p];
     if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_batch_create: every assembler needs its symbolic phase");
     if (A->test->geom.k < 1 || A->test->geom.k > 3) return fail(GD_ERR_UNSUPPORTED, "gd_batch_create: order 1..3");
+    if (A->bs != 1) return fail(GD_ERR_UNSUPPORTED, "gd_batch_create: scalar spaces only");
     const Geom& g = A->test->geom;
     const int W = 2 * g.k + 1;
     const int want = (W * W * (g.dim == 3 ? W : 1)) <= 256 ? 1 : 2;

@@ -181,6 +181,10 @@ struct MixedState {
   int64_t lat_epoch = -1;
 };
 constexpr int kLatVectors = 8;
+
+// host quadrature helpers (gd_numeric.cu)
+void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w);
+void lagrange01(int k, double x, double* v, double* dv);
 }  // namespace gd
 
 // ---------------------------------------------------------------------------------
@@ -278,6 +282,14 @@ struct gd_asm {
   double mf_ratio = 0.0;
   double mf_k2 = 0.0;
   const double* rhs_override = nullptr;   // solve with a caller-given right-hand side
+  // vector-valued spaces: bs = components per node; the CSR, row space and per-part
+  // counts are expanded to the vector DOFs (dof = bs * node dof + component)
+  int bs = 1;
+  gd::DBuf<int32_t> gcol_gstart, gcol_gsize;   // scalar ghost-column groups (symbolic only)
+  gd::DBuf<double> Kel;                        // elasticity reference matrix (E = 1)
+  int el_degree = -1;
+  double el_nu = -1.0;
+  gd::DBuf<double> E_dev;
   // solver workspace
   gd::DBuf<double> w;              // vectors
   gd::DBuf<double> dred;           // reduction partials

@@ -24,7 +24,7 @@
 namespace gd {
 
 // ---- 1D Gauss-Legendre rule on [0,1] (Newton on the Legendre recurrence) -------
-static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
+void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w) {
   x.assign(n, 0.0);
   w.assign(n, 0.0);
   const double pi = 3.14159265358979323846;
@@ -57,7 +57,7 @@ static void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>&
 }
 
 // Equispaced Lagrange basis of order k on [0,1]: values and derivatives at x.
-static void lagrange01(int k, double x, double* v, double* dv) {
+void lagrange01(int k, double x, double* v, double* dv) {
   for (int a = 0; a <= k; ++a) {
     double xa = (double)a / k, den = 1.0, val = 1.0, der = 0.0;
     for (int b = 0; b <= k; ++b) {
@@ -750,6 +750,8 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
 int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   if (!A || !c) return fail(GD_ERR_ARG, "gd_assemble_numeric: null argument");
   if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_assemble_numeric: run gd_assemble_symbolic first");
+  if (A->bs > 1)
+    return fail(GD_ERR_UNSUPPORTED, "gd_assemble_numeric: vector-valued space; use gd_assemble_elasticity");
   const Geom& g = A->test->geom;
   cudaStream_t st = A->test->model->ctx->stream;
   GD_TRY(reference_element(A, c->degree));

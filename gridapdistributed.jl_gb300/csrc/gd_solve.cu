@@ -228,6 +228,7 @@ __global__ void k_gather_local(int64_t n, const int64_t* __restrict__ lid_gid, c
 }
 
 static int grid_for(int64_t n, int per_block);
+int gather_local_vec(const gd_space* S, int part, const double* xg, double* xl, cudaStream_t st);
 
 // FP64 residual r = b - A x with per-block partials of r.r and b.b; returns the block count
 int residual_fp64(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, const double* x,
@@ -384,17 +385,20 @@ extern "C" int gd_fe_function_local(const gd_space* S, int part, const double* x
     return fail(GD_ERR_ARG, "gd_fe_function_local: bad argument");
   cudaStream_t st = S->model->ctx->stream;
   const DevPart& P = S->parts[part];
-  const int64_t n = P.nfree;
+  const int bs = S->ncomp;
+  const int64_t n = P.nfree * bs, ng = S->ngdofs * bs;
   DBuf<double> xg, xl;
   const double* dxg = x_global;
   if (where == GD_HOST) {
-    GD_TRY(dalloc(xg, std::max<int64_t>(S->ngdofs, 1)));
-    GD_CUDA_TRY(cudaMemcpyAsync(xg.p, x_global, sizeof(double) * S->ngdofs, cudaMemcpyHostToDevice, st));
+    GD_TRY(dalloc(xg, std::max<int64_t>(ng, 1)));
+    GD_CUDA_TRY(cudaMemcpyAsync(xg.p, x_global, sizeof(double) * ng, cudaMemcpyHostToDevice, st));
     dxg = xg.p;
     GD_TRY(dalloc(xl, std::max<int64_t>(n, 1)));
   }
   double* dxl = where == GD_HOST ? xl.p : x_local;
-  if (n > 0) {
+  if (bs > 1) {
+    GD_TRY(gather_local_vec(S, part, dxg, dxl, st));
+  } else if (n > 0) {
     k_gather_local<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, S->lid_gid.p + P.lid_off, dxg, dxl);
     GD_CUDA_TRY(cudaGetLastError());
   }

@@ -509,7 +509,8 @@ extern "C" int gd_space_create(gd_model* model, int order, int ncomp, const int3
                                gd_space** out) {
   if (!model || !out) return fail(GD_ERR_ARG, "gd_space_create: null argument");
   if (order < 1 || order > kMaxOrder) return fail(GD_ERR_UNSUPPORTED, "gd_space_create: order must be 1..3");
-  if (ncomp != 1) return fail(GD_ERR_UNSUPPORTED, "gd_space_create: only scalar spaces (ncomp = 1)");
+  if (ncomp != 1 && !(ncomp == model->geom.dim && order <= 2))
+    return fail(GD_ERR_UNSUPPORTED, "gd_space_create: ncomp must be 1, or the dimension for orders 1 and 2");
   gd_space* S = new gd_space();
   S->model = model;
   S->geom = model->geom;
@@ -547,9 +548,11 @@ extern "C" int gd_space_destroy(gd_space* S) {
   return GD_OK;
 }
 
+// The space keeps node-based arrays; a vector space (ncomp = bs > 1, orders 1 and 2)
+// exposes dof = bs * node dof + component for local ids, gids and owners alike.
 extern "C" int gd_space_num_free_dofs(const gd_space* S, int64_t* n) {
   if (!S || !n) return fail(GD_ERR_ARG, "gd_space_num_free_dofs: null argument");
-  *n = S->ngdofs;
+  *n = S->ngdofs * S->ncomp;
   return GD_OK;
 }
 
@@ -557,9 +560,9 @@ extern "C" int gd_space_local_sizes(const gd_space* S, int part, int64_t* nldofs
                                     int64_t* first_gdof) {
   if (!S || part < 0 || part >= S->geom.nparts) return fail(GD_ERR_ARG, "gd_space_local_sizes: bad part");
   const DevPart& P = S->parts[part];
-  if (nldofs) *nldofs = P.nfree;
-  if (nown) *nown = P.n_own;
-  if (first_gdof) *first_gdof = P.first_gdof;
+  if (nldofs) *nldofs = P.nfree * S->ncomp;
+  if (nown) *nown = P.n_own * S->ncomp;
+  if (first_gdof) *first_gdof = P.first_gdof * S->ncomp;
   return GD_OK;
 }
 
@@ -567,14 +570,26 @@ extern "C" int gd_space_get_gids(const gd_space* S, int part, int64_t* ldof_to_g
   if (!S || part < 0 || part >= S->geom.nparts) return fail(GD_ERR_ARG, "gd_space_get_gids: bad part");
   const DevPart& P = S->parts[part];
   cudaStream_t st = S->model->ctx->stream;
+  const int bs = S->ncomp;
+  std::vector<int64_t> gid(bs > 1 ? P.nfree : 0);
+  std::vector<int32_t> own(bs > 1 ? P.nfree : 0);
+  int64_t* dg = bs > 1 ? gid.data() : ldof_to_gdof;
+  int32_t* dow = bs > 1 ? own.data() : ldof_to_owner;
   if (ldof_to_gdof && P.nfree)
-    GD_CUDA_TRY(cudaMemcpyAsync(ldof_to_gdof, S->lid_gid.p + P.lid_off, sizeof(int64_t) * P.nfree, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaMemcpyAsync(dg, S->lid_gid.p + P.lid_off, sizeof(int64_t) * P.nfree, cudaMemcpyDeviceToHost, st));
   if (ldof_to_owner && P.nfree)
-    GD_CUDA_TRY(cudaMemcpyAsync(ldof_to_owner, S->lid_owner.p + P.lid_off, sizeof(int32_t) * P.nfree, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaMemcpyAsync(dow, S->lid_owner.p + P.lid_off, sizeof(int32_t) * P.nfree, cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (bs > 1)
+    for (int64_t i = 0; i < P.nfree; ++i)
+      for (int c = 0; c < bs; ++c) {
+        if (ldof_to_gdof) ldof_to_gdof[bs * i + c] = bs * gid[i] + c;
+        if (ldof_to_owner) ldof_to_owner[bs * i + c] = own[i];
+      }
   return GD_OK;
 }
 
+// lattice node of every local free dof (vector spaces: one entry per component)
 extern "C" int gd_space_dof_nodes(const gd_space* S, int part, int64_t* ldof_to_node) {
   if (!S || part < 0 || part >= S->geom.nparts || !ldof_to_node) return fail(GD_ERR_ARG, "gd_space_dof_nodes: bad argument");
   const DevPart& P = S->parts[part];
@@ -584,13 +599,14 @@ extern "C" int gd_space_dof_nodes(const gd_space* S, int part, int64_t* ldof_to_
     GD_CUDA_TRY(cudaMemcpyAsync(tmp.data(), S->lid_node.p + P.lid_off, sizeof(int32_t) * P.nfree, cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   const Geom& g = S->geom;
+  const int bs = S->ncomp;
   for (int64_t i = 0; i < P.nfree; ++i) {
     int64_t li = tmp[i], X[kMaxDim] = {0, 0, 0};
     for (int d = 0; d < g.dim; ++d) {
       X[d] = g.k * P.loc_lo[d] + li % P.nb[d];
       li /= P.nb[d];
     }
-    ldof_to_node[i] = lattice_lin(g, X);
+    for (int c = 0; c < bs; ++c) ldof_to_node[bs * i + c] = lattice_lin(g, X);
   }
   return GD_OK;
 }
@@ -603,6 +619,7 @@ extern "C" int gd_space_set_dirichlet(gd_space* S, const double* u, int where) {
     S->has_dirichlet_values = false;
     return GD_OK;
   }
+  if (S->ncomp > 1) return fail(GD_ERR_UNSUPPORTED, "gd_space_set_dirichlet: vector spaces take homogeneous values");
   int64_t n = 1;
   for (int d = 0; d < S->geom.dim; ++d) n *= S->geom.N[d];
   GD_TRY(dalloc(S->u_dir, n));

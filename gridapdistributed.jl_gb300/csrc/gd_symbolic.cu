@@ -627,6 +627,11 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   return GD_OK;
 }
 
+namespace gd {
+int gcol_groups(gd_asm* A, const unsigned long long* ckey, const int32_t* rank, int64_t ncand);   // gd_vector.cu
+int vector_expand(gd_asm* A);                                                                       // gd_vector.cu
+}  // namespace gd
+
 static int symbolic_impl(gd_asm* A) {
   gd_space* S = A->test;
   const Geom& g = S->geom;
@@ -721,6 +726,7 @@ static int symbolic_impl(gd_asm* A) {
       GD_TRY(launch_ok("k_assign_ghost_cols"));
     }
   }
+  if (S->ncomp > 1) GD_TRY(gcol_groups(A, ckey.p, rank.p, ncand));
   dfreeb(key);
   dfreeb(ckey);
   dfreeb(clid);
@@ -787,6 +793,7 @@ static int symbolic_impl(gd_asm* A) {
   GD_CUDA_TRY(cudaMemsetAsync(A->vals.p, 0, sizeof(double) * std::max<int64_t>(nnz, 1), st));
   GD_CUDA_TRY(cudaMemsetAsync(A->rhs.p, 0, sizeof(double) * std::max<int64_t>(R, 1), st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (S->ncomp > 1) GD_TRY(vector_expand(A));
   A->symbolic_done = true;
   return GD_OK;
 }
@@ -857,13 +864,15 @@ extern "C" int gd_matrix_export(const gd_asm* A, int part, int64_t* rowptr, int3
     if (P.n_gcol)
       GD_CUDA_TRY(cudaMemcpyAsync(gcl.data(), A->gcol_lid.p + P.gcol_off, sizeof(int32_t) * P.n_gcol, cudaMemcpyDeviceToHost, st));
     GD_CUDA_TRY(cudaStreamSynchronize(st));
+    // ghost row / column lids are vector lids (bs * node lid + component) for bs > 1
+    const int bs = A->bs;
     for (int64_t i = 0; i < P.n_grow; ++i) {
-      if (ghost_row_gids) ghost_row_gids[i] = gid[grl[i]];
-      if (ghost_row_owners) ghost_row_owners[i] = own[grl[i]];
+      if (ghost_row_gids) ghost_row_gids[i] = bs * gid[grl[i] / bs] + grl[i] % bs;
+      if (ghost_row_owners) ghost_row_owners[i] = own[grl[i] / bs];
     }
     for (int64_t i = 0; i < P.n_gcol; ++i) {
-      if (ghost_col_gids) ghost_col_gids[i] = gid[gcl[i]];
-      if (ghost_col_owners) ghost_col_owners[i] = own[gcl[i]];
+      if (ghost_col_gids) ghost_col_gids[i] = bs * gid[gcl[i] / bs] + gcl[i] % bs;
+      if (ghost_col_owners) ghost_col_owners[i] = own[gcl[i] / bs];
     }
   }
   GD_CUDA_TRY(cudaStreamSynchronize(st));

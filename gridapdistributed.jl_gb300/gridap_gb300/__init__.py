@@ -7,8 +7,8 @@ from . import _lib
 from .distributed import (AffineFEOperator, CartesianDiscreteModel, FEFunction, FESpace,
                           FullyAssembledRows, GB300Backend, Measure, PSparseMatrix, PVector,
                           ReferenceFE, SparseMatrixAssembler, SubAssembledRows, TestFESpace,
-                          Triangulation, TrialFESpace, assemble_matrix_and_vector,
-                          collect_cell_matrix_and_vector, integral_grad_grad, integral_source,
-                          lagrangian, solve, with_gb300)
+                          Triangulation, TrialFESpace, VectorValue, assemble_matrix_and_vector,
+                          collect_cell_matrix_and_vector, integral_elasticity, integral_grad_grad,
+                          integral_source, lagrangian, solve, with_gb300)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

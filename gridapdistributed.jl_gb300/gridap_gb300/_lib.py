@@ -39,6 +39,11 @@ class gd_coeffs(C.Structure):
                 ("degree", C.c_int), ("where", C.c_int)]
 
 
+class gd_elasticity(C.Structure):
+    _fields_ = [("E", C.c_void_p), ("nu", C.c_double), ("force", C.c_double * 3), ("degree", C.c_int),
+                ("where", C.c_int)]
+
+
 class gd_solve_stats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("rel_residual", C.c_double),
                 ("seconds", C.c_double)]
@@ -88,6 +93,7 @@ SIGNATURES = {
     "gd_fe_function_local": [P, C.c_int, P, C.c_int, DP],
     "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
+    "gd_assemble_elasticity": [P, P],
     "gd_batch_create": [P, P, C.c_int, PP],
     "gd_batch_destroy": [P],
     "gd_batch_assemble": [P],

@@ -145,10 +145,15 @@ class Measure:
     degree: int
 
 
+class VectorValue:
+    """Tag for ``ReferenceFE(lagrangian, VectorValue, k)``: a vector Lagrangian space
+    with as many components as the model's dimension (VectorValue{D,Float64})."""
+
+
 def ReferenceFE(name, T, order):
-    if name != lagrangian or T not in (float, np.float64):
-        raise NotImplementedError("only scalar Lagrangian Float64 reference FEs")
-    return ("lagrangian", float, int(order))
+    if name != lagrangian or T not in (float, np.float64, VectorValue):
+        raise NotImplementedError("only Lagrangian Float64 and VectorValue reference FEs")
+    return ("lagrangian", VectorValue if T is VectorValue else float, int(order))
 
 
 # --------------------------------------------------------------------------------------
@@ -225,9 +230,10 @@ class DistributedSingleFieldFESpace:
     def __init__(self, model: DistributedDiscreteModel, reffe, dirichlet_tags="boundary"):
         self.model = model
         self.order = reffe[2]
+        self.ncomp = model.dim if reffe[1] is VectorValue else 1
         self.sides = _sides_from_tags(model.dim, dirichlet_tags)
         h = C.c_void_p()
-        L.call("gd_space_create", model.handle, self.order, 1, L.ptr(self.sides, C.c_int32), C.byref(h))
+        L.call("gd_space_create", model.handle, self.order, self.ncomp, L.ptr(self.sides, C.c_int32), C.byref(h))
         self.handle = h
         self._gids = None
         self.dirichlet_values = None
@@ -327,8 +333,19 @@ class GradGradForm:
 
 
 @dataclass
+class ElasticityForm:
+    """a(u,v) = ∫( ε(v) ⊙ (σ∘ε(u)) )dΩ, σ(ε) = λ tr(ε) I + 2μ ε with Young's modulus E per
+    global cell (None = 1) and Poisson ratio nu (λ, μ from E and nu)."""
+
+    E: np.ndarray | None
+    nu: float
+    measure: Measure
+
+
+@dataclass
 class SourceForm:
-    """l(v) = ∫( v f )dΩ with f constant or nodal (dense over the lattice)."""
+    """l(v) = ∫( v f )dΩ with f constant or nodal (dense over the lattice); for a vector
+    space f is a constant vector (body force)."""
 
     f: object
     measure: Measure
@@ -336,6 +353,10 @@ class SourceForm:
 
 def integral_grad_grad(kappa=None, measure: Measure = None):
     return GradGradForm(None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64), measure)
+
+
+def integral_elasticity(E=None, nu=0.3, measure: Measure = None):
+    return ElasticityForm(None if E is None else np.ascontiguousarray(E, dtype=np.float64), float(nu), measure)
 
 
 def integral_source(f=0.0, measure: Measure = None):
@@ -359,8 +380,20 @@ class DistributedSparseMatrixAssembler:
             L.call("gd_assemble_symbolic", self.handle)
             self._symbolic = True
 
-    def numeric(self, a: GradGradForm, l: SourceForm):
+    def numeric(self, a, l: SourceForm):
         self.symbolic()
+        if isinstance(a, ElasticityForm):
+            c = L.gd_elasticity()
+            c.E = None if a.E is None else a.E.ctypes.data
+            c.nu = a.nu
+            f = l.f if l is not None else (0.0,) * self.V.model.dim
+            f = tuple(float(x) for x in (f if not np.isscalar(f) else (0.0,) * self.V.model.dim))
+            for i in range(3):
+                c.force[i] = f[i] if i < len(f) else 0.0
+            c.degree = int(a.measure.degree if a.measure is not None else 2 * self.V.order)
+            c.where = L.GD_HOST
+            L.call("gd_assemble_elasticity", self.handle, C.byref(c))
+            return
         keep = []
         c = L.gd_coeffs()
         c.kappa = None if a.kappa is None else a.kappa.ctypes.data

@@ -104,7 +104,11 @@ int gd_model_part_boxes(const gd_model* model, int part, int64_t* own_lo, int64_
  * cells, Gridap's conforming numbering) and generate_gids (FESpaces.jl:139-261).
  * dirichlet_sides[2*d] / [2*d+1] flag the planes x_d = min / max; a node on a
  * flagged plane is a Dirichlet node ("boundary" = all flags set).
- * Scalar spaces (ncomp = 1), order 1..3.                                          */
+ * Scalar spaces (ncomp = 1), order 1..3, or vector spaces (ncomp = dim, the
+ * ReferenceFE(lagrangian, VectorValue{dim,Float64}, k) of the reference), order 1..2,
+ * all components sharing the Dirichlet sides; their dofs are numbered
+ * ncomp * (node dof) + component, which is Gridap's component-major numbering of each
+ * face's own DOFs when every face owns one node.                                   */
 int gd_space_create(gd_model* model, int order, int ncomp, const int32_t* dirichlet_sides,
                     gd_space** out);
 int gd_space_destroy(gd_space* space);
@@ -148,6 +152,21 @@ typedef struct gd_coeffs {
 int gd_assemble_numeric(gd_asm* a, const gd_coeffs* c);
 /* Same, without the final stream synchronisation (for timing loops). */
 int gd_assemble_numeric_async(gd_asm* a, const gd_coeffs* c);
+
+/* Linear elasticity on a vector space (gd_space_create with ncomp = dim, orders 1-2):
+ * a(u,v) = int C(E) eps(u):eps(v), isotropic C with Young's modulus E per cell and
+ * Poisson ratio nu; l(v) = int v.force (constant body force).  Homogeneous Dirichlet
+ * values on the space's Dirichlet sides (all components clamped). */
+typedef struct gd_elasticity {
+  const double* E;       /* per global cell (lexicographic); NULL = 1 */
+  double nu;             /* Poisson ratio, -1 < nu < 0.5 */
+  double force[3];       /* body force (components beyond dim ignored) */
+  int degree;            /* quadrature degree (tensor Gauss) */
+  int where;             /* GD_HOST or GD_DEVICE for E */
+} gd_elasticity;
+/* assemble_matrix_and_vector! for the elasticity forms into the symbolic pattern of a
+ * vector-space assembler (dof = dim * node dof + component). */
+int gd_assemble_elasticity(gd_asm* a, const gd_elasticity* c);
 
 /* Record CUDA events around the phases of every numeric assembly (off by default). */
 int gd_assembler_set_profiling(gd_asm* a, int on);

@@ -527,6 +527,46 @@ def reference_matrices(dim, k, h, degree):
     return K, M, F
 
 
+def reference_elasticity(dim, k, h, degree, nu):
+    """Element matrix of ``int C eps(u):eps(v)`` for E = 1 on an axis-aligned cell of
+    sizes ``h``, in Gridap's vector cell-DOF order (component-major: entry ``c*nn + a``
+    is component c of node a).  With u = phi_j e_d and v = phi_i e_c:
+    C eps(u):eps(v) = lam d_c(phi_i) d_d(phi_j) + mu (delta_cd grad(phi_i).grad(phi_j)
+    + d_d(phi_i) d_c(phi_j)), lam = nu/((1+nu)(1-2nu)), mu = 1/(2(1+nu))."""
+    nq = quad_points_per_dir(degree)
+    xq, wq = gauss_legendre(nq)
+    V, D = lagrange_1d(k, xq)
+    lnodes = cell_local_nodes(dim, k)
+    nn = len(lnodes)
+    detJ = float(np.prod(h))
+    qidx = list(itertools.product(*[range(nq)] * dim))
+    grad = np.zeros((len(qidx), nn, dim))
+    W = np.zeros(len(qidx))
+    for iq, qi in enumerate(qidx):
+        qi = tuple(reversed(qi))
+        W[iq] = np.prod([wq[qi[d]] for d in range(dim)]) * detJ
+        for a, off in enumerate(lnodes):
+            vals = [V[qi[d], off[d]] for d in range(dim)]
+            for d in range(dim):
+                g = D[qi[d], off[d]] / h[d]
+                for e in range(dim):
+                    if e != d:
+                        g *= vals[e]
+                grad[iq, a, d] = g
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    G = np.einsum("q,qic,qjd->icjd", W, grad, grad)   # int d_c phi_i d_d phi_j
+    K = np.zeros((dim * nn, dim * nn))
+    lap = np.einsum("icjc->ij", G)
+    for c in range(dim):
+        for d in range(dim):
+            blk = lam * G[:, c, :, d] + mu * G[:, d, :, c]
+            if c == d:
+                blk = blk + mu * lap
+            K[c * nn:(c + 1) * nn, d * nn:(d + 1) * nn] = blk
+    return K
+
+
 # --------------------------------------------------------------------------------------
 # Problem description
 # --------------------------------------------------------------------------------------
@@ -534,7 +574,10 @@ def reference_matrices(dim, k, h, degree):
 
 @dataclass
 class Problem:
-    """A scalar diffusion problem ``-div(kappa grad u) = f`` on a Cartesian box."""
+    """A scalar diffusion problem ``-div(kappa grad u) = f`` on a Cartesian box, or
+    (``physics="elasticity"``) linear elasticity ``a(u,v) = int C(E) eps(u):eps(v)``,
+    ``l(v) = int v.force`` with a vector space of ``ncomp = dim`` components, E per cell
+    in ``kappa`` and Poisson ratio ``nu``."""
 
     np: tuple
     n: tuple
@@ -546,6 +589,13 @@ class Problem:
     f_const: float = 0.0            # constant source
     f_nodal: np.ndarray = None      # or nodal source values on the global lattice (b = M f)
     u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0
+    physics: str = "poisson"        # or "elasticity"
+    nu: float = 0.3                 # Poisson ratio (elasticity)
+    force: tuple = None             # body force (elasticity), default 0
+
+    @property
+    def ncomp(self):
+        return self.dim if self.physics == "elasticity" else 1
 
     def __post_init__(self):
         dim = len(self.n)
@@ -593,7 +643,7 @@ class FESpaceData:
 
 def build_fespace(pb: Problem) -> FESpaceData:
     P = make_partition(pb.np, pb.n)
-    spaces = [build_local_space(P, p, pb.order, 1, pb.dirichlet_sides) for p in range(P.nparts)]
+    spaces = [build_local_space(P, p, pb.order, pb.ncomp, pb.dirichlet_sides) for p in range(P.nparts)]
     dofs, first = generate_gids(P, spaces)
     return FESpaceData(P, spaces, dofs, first)
 
@@ -609,6 +659,15 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
     dim = pb.dim
     lnodes = np.array(cell_local_nodes(dim, pb.order))
     mats, vecs = [], []
+    if pb.physics == "elasticity":
+        assert pb.u_dir is None and pb.f_nodal is None, "elasticity: homogeneous Dirichlet, constant force"
+        Kel = reference_elasticity(dim, pb.order, pb.h, pb.degree, pb.nu)
+        force = pb.force if pb.force is not None else (0.0,) * dim
+        be = np.concatenate([force[c] * Fh for c in range(dim)])
+        for ic, g in enumerate(sp.cells):
+            mats.append(pb.kappa[g] * Kel)
+            vecs.append(be.copy())
+        return mats, vecs
     for ic, g in enumerate(sp.cells):
         kap = pb.kappa[g]
         Ke = kap * Kh
