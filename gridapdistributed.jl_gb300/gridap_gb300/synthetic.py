@@ -110,3 +110,11 @@ def batched_nnz_estimate(n, k):
     average k+2 per direction."""
     dofs = (k * n - 1) ** 3
     return dofs, dofs * (k + 2) ** 3
+
+
+# Linear elasticity workload: 64^3 hex cells on the unit cube, vector Q2, quadrature
+# degree 4, parts (2,2,2), E = exp(g) (sigma 0.5, correlation length 0.1), nu = 0.3,
+# body force (0,0,-1), clamped (all components) on x = 0.
+ELASTICITY3D_64 = dict(name="elasticity3d_vq2_64^3_parts2x2x2", cells=(64, 64, 64), parts=(2, 2, 2),
+                       domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=2, degree=4, sigma=0.5, corr_len=0.1,
+                       nu=0.3, force=(0.0, 0.0, -1.0), seed=4000)
