@@ -57,10 +57,12 @@ def parse():
     ap.add_argument("--batched", default="sample", choices=["off", "sample", "full"],
                     help="batched 64-problem workload: a bounded first wave (sample), every wave (full) or none")
     ap.add_argument("--batched-budget-gb", type=float, default=140.0, help="device memory per wave (full)")
+    ap.add_argument("--batched-sample-gb", type=float, default=16.0, help="device memory of the sample wave")
     ap.add_argument("--batched-solve", action="store_true", help="also Jacobi-PCG every batched problem")
     ap.add_argument("--no-learned", action="store_true")
     ap.add_argument("--no-elasticity", action="store_true")
     ap.add_argument("--elasticity-solve", action="store_true", help="also solve the elasticity system (seconds)")
+    ap.add_argument("--elasticity-cells", type=int, default=64, help="cells per direction of the elasticity workload")
     return ap.parse_args()
 
 
@@ -228,7 +230,7 @@ def run_batched(args, be, stream, dev, mode):
     w = BATCHED3D_64
     draw = batched_draw(w)
     bytes_per_entry = 30.0   # values, column ids, stencil codes and symbolic scratch
-    budget = (16.0 if mode == "sample" else args.batched_budget_gb) * 1e9
+    budget = (args.batched_sample_gb if mode == "sample" else args.batched_budget_gb) * 1e9
     waves, cur, cur_b = [], [], 0.0
     for i, (n, k, ks) in enumerate(draw):
         b = batched_nnz_estimate(n, k)[1] * bytes_per_entry
@@ -314,7 +316,10 @@ def run_elasticity(args, be, stream, dev):
     import gridap_gb300 as G
     from gridap_gb300 import _lib as L
     from gridap_gb300.synthetic import ELASTICITY3D_64, lognormal_kappa
-    w = ELASTICITY3D_64
+    w = dict(ELASTICITY3D_64)
+    if args.elasticity_cells != 64:
+        w["cells"] = (args.elasticity_cells,) * 3
+        w["name"] = f"elasticity3d_vq2_{args.elasticity_cells}^3_parts2x2x2"
     ranks = be.distribute(range(int(np.prod(w["parts"]))))
     model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], w["cells"])
     V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, G.VectorValue, w["order"]), dirichlet_tags="left")
