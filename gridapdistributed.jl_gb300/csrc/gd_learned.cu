@@ -164,38 +164,51 @@ __global__ void k_sum_partials(int nparts, int nw, const float* __restrict__ par
   out[w] += a;
 }
 
+// load modes and epilogues of the application convolutions (described at k_tconv)
+enum { LD_PLAIN = 0, LD_GATED = 1, LD_GATHER = 2 };
+enum { EP_GATE = 0, EP_PLAIN = 1, EP_OUT = 2, EP_OUTLAT = 3 };
+
+struct TConvArgsS {   // direct convolution: output channels co_n, input/gate/weights as in k_tconv
+  Dims d;
+  const float* in;
+  const float* in_gate;
+  const float* W;
+  int adjoint;
+  int co_n;
+  const float* out_gate;
+  float* out;
+};
+
 // ---- restriction / prolongation ----------------------------------------------------------
-// One thread per output voxel for all C channels; neighbour indices and weights are
-// formed once per voxel in 32-bit arithmetic (lattices stay below 2^31 nodes).
-// coarse[i] = scale * sum_{o in {-1,0,1}^3} w(o) fine[2i+o], w = prod(1/2 if o=0 else 1/4)
+// One thread per (output voxel, channel), channel-major so a warp covers consecutive
+// voxels of one channel; 32-bit index arithmetic (lattices stay below 2^31 / 8 nodes).
+// coarse[ch][i] = scale * sum_{o in {-1,0,1}^3} w(o) fine[ch][2i+o], w = prod(1/2 if o=0 else 1/4)
 __global__ void k_restrict(int C, Dims f, Dims c, const float* __restrict__ fine, float* __restrict__ coarse,
                            float scale) {
   const int nc = (int)c.size(), nf = (int)f.size();
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < C * nc; v += gridDim.x * blockDim.x) {
+    const int ch = v / nc, i = v - ch * nc;
     const int ix = i % c.n[0], iy = (i / c.n[0]) % c.n[1], iz = i / (c.n[0] * c.n[1]);
-    float acc[kC];
+    const float* src = fine + (size_t)ch * nf;
+    float acc = 0.f;
 #pragma unroll
-    for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
     for (int oz = -1; oz <= 1; ++oz) {
       const int fz = 2 * iz + oz;
       if (fz < 0 || fz >= f.n[2]) continue;
+#pragma unroll
       for (int oy = -1; oy <= 1; ++oy) {
         const int fy = 2 * iy + oy;
         if (fy < 0 || fy >= f.n[1]) continue;
+#pragma unroll
         for (int ox = -1; ox <= 1; ++ox) {
           const int fx = 2 * ix + ox;
           if (fx < 0 || fx >= f.n[0]) continue;
           const float w = (ox == 0 ? 0.5f : 0.25f) * (oy == 0 ? 0.5f : 0.25f) * (oz == 0 ? 0.5f : 0.25f);
-          const int u = fx + f.n[0] * (fy + f.n[1] * fz);
-#pragma unroll
-          for (int ch = 0; ch < kC; ++ch)
-            if (ch < C) acc[ch] = fmaf(w, __ldg(fine + (size_t)ch * nf + u), acc[ch]);
+          acc = fmaf(w, __ldg(src + fx + f.n[0] * (fy + f.n[1] * fz)), acc);
         }
       }
     }
-#pragma unroll
-    for (int ch = 0; ch < kC; ++ch)
-      if (ch < C) coarse[(size_t)ch * nc + i] = scale * acc[ch];
+    coarse[(size_t)ch * nc + i] = scale * acc;
   }
 }
 
@@ -220,41 +233,40 @@ __device__ inline Lin1 lin1(int j, int nc) {
   return r;
 }
 
-// fine[j] (+)= scale * sum_i w'(j - 2i) coarse[i] (P = 8 R^T, trilinear)
+__device__ __forceinline__ float prolong_at(const Dims& c, const Dims& f, const float* __restrict__ src, int j) {
+  const int jx = j % f.n[0], jy = (j / f.n[0]) % f.n[1], jz = j / (f.n[0] * f.n[1]);
+  const Lin1 X = lin1(jx, c.n[0]), Y = lin1(jy, c.n[1]), Z = lin1(jz, c.n[2]);
+  const float w = X.w * Y.w * Z.w;
+  float acc = 0.f;
+  for (int b = 0; b < Z.cnt; ++b)
+    for (int a = 0; a < Y.cnt; ++a)
+      for (int e = 0; e < X.cnt; ++e)
+        acc = fmaf(w, __ldg(src + (e ? X.i1 : X.i0) + c.n[0] * ((a ? Y.i1 : Y.i0) + c.n[1] * (b ? Z.i1 : Z.i0))),
+                   acc);
+  return acc;
+}
+
+// fine[ch][j] (+)= scale * sum_i w'(j - 2i) coarse[ch][i] (P = 8 R^T, trilinear)
 __global__ void k_prolong(int C, Dims c, Dims f, const float* __restrict__ coarse, float* __restrict__ fine,
                           float scale, int accumulate) {
   const int nc = (int)c.size(), nf = (int)f.size();
-  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
-    const int jx = j % f.n[0], jy = (j / f.n[0]) % f.n[1], jz = j / (f.n[0] * f.n[1]);
-    const Lin1 X = lin1(jx, c.n[0]), Y = lin1(jy, c.n[1]), Z = lin1(jz, c.n[2]);
-    float acc[kC];
-#pragma unroll
-    for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
-    for (int b = 0; b < Z.cnt; ++b)
-      for (int a = 0; a < Y.cnt; ++a)
-        for (int e = 0; e < X.cnt; ++e) {
-          const int u = (e ? X.i1 : X.i0) + c.n[0] * ((a ? Y.i1 : Y.i0) + c.n[1] * (b ? Z.i1 : Z.i0));
-          const float w = X.w * Y.w * Z.w;
-#pragma unroll
-          for (int ch = 0; ch < kC; ++ch)
-            if (ch < C) acc[ch] = fmaf(w, __ldg(coarse + (size_t)ch * nc + u), acc[ch]);
-        }
-#pragma unroll
-    for (int ch = 0; ch < kC; ++ch)
-      if (ch < C) {
-        if (accumulate) fine[(size_t)ch * nf + j] += scale * acc[ch];
-        else fine[(size_t)ch * nf + j] = scale * acc[ch];
-      }
+  for (int v = blockIdx.x * blockDim.x + threadIdx.x; v < C * nf; v += gridDim.x * blockDim.x) {
+    const int ch = v / nf, j = v - ch * nf;
+    const float val = scale * prolong_at(c, f, coarse + (size_t)ch * nc, j);
+    if (accumulate) fine[(size_t)ch * nf + j] += val;
+    else fine[(size_t)ch * nf + j] = val;
   }
 }
 
-// decoder step below the top level: out = (h + scale * P gx) * s, all kC channels
+// decoder step below the top level: out = (h + scale * P gx) * s, all kC channels; one
+// thread per fine voxel (the neighbour indices are formed once for the 8 channels)
 __global__ void k_prolong_gate(Dims c, Dims f, const float* __restrict__ gx, const float* __restrict__ h,
                                const float* __restrict__ s, float scale, float* __restrict__ out) {
   const int nc = (int)c.size(), nf = (int)f.size();
   for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x) {
     const int jx = j % f.n[0], jy = (j / f.n[0]) % f.n[1], jz = j / (f.n[0] * f.n[1]);
     const Lin1 X = lin1(jx, c.n[0]), Y = lin1(jy, c.n[1]), Z = lin1(jz, c.n[2]);
+    const float w = X.w * Y.w * Z.w;
     float acc[kC];
 #pragma unroll
     for (int ch = 0; ch < kC; ++ch) acc[ch] = 0.f;
@@ -262,13 +274,50 @@ __global__ void k_prolong_gate(Dims c, Dims f, const float* __restrict__ gx, con
       for (int a = 0; a < Y.cnt; ++a)
         for (int e = 0; e < X.cnt; ++e) {
           const int u = (e ? X.i1 : X.i0) + c.n[0] * ((a ? Y.i1 : Y.i0) + c.n[1] * (b ? Z.i1 : Z.i0));
-          const float w = X.w * Y.w * Z.w;
 #pragma unroll
           for (int ch = 0; ch < kC; ++ch) acc[ch] = fmaf(w, __ldg(gx + (size_t)ch * nc + u), acc[ch]);
         }
 #pragma unroll
-    for (int ch = 0; ch < kC; ++ch)
-      out[(size_t)ch * nf + j] = fmaf(scale, acc[ch], __ldg(h + (size_t)ch * nf + j)) * __ldg(s + (size_t)ch * nf + j);
+    for (int ch = 0; ch < kC; ++ch) {
+      const size_t o = (size_t)ch * nf + j;
+      out[o] = fmaf(scale, acc[ch], __ldg(h + o)) * __ldg(s + o);
+    }
+  }
+}
+
+// ---- direct convolution for the coarse levels ------------------------------------------------
+// One thread per (voxel, output channel), channel-major; inputs through the read-only
+// cache.  Coarse lattices are too small to fill the GPU with tiles of 512 voxels, and a
+// tiled CTA there runs long serial loops; here every thread does CI x 27 FMAs.
+template <int CI, int LD, int EP>
+__global__ void __launch_bounds__(kLT) k_conv_direct(TConvArgsS a) {
+  __shared__ float sw[kC * CI * kTaps];   // [co][ci][tap] in the orientation applied
+  for (int i = threadIdx.x; i < a.co_n * CI * kTaps; i += blockDim.x) {
+    const int tap = i % kTaps, ci = (i / kTaps) % CI, co = i / (kTaps * CI);
+    sw[i] = a.adjoint ? a.W[(ci * a.co_n + co) * kTaps + (kTaps - 1 - tap)] : a.W[(co * CI + ci) * kTaps + tap];
+  }
+  __syncthreads();
+  const int nx = a.d.n[0], ny = a.d.n[1], nz = a.d.n[2];
+  const int nv = nx * ny * nz;
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < a.co_n * nv; idx += gridDim.x * blockDim.x) {
+    const int co = idx / nv, v = idx - co * nv;
+    const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
+    const float* wco = sw + co * CI * kTaps;
+    float acc = 0.f;
+#pragma unroll
+    for (int tap = 0; tap < kTaps; ++tap) {
+      const int xx = x + tap % 3 - 1, yy = y + (tap / 3) % 3 - 1, zz = z + tap / 9 - 1;
+      if ((unsigned)xx >= (unsigned)nx || (unsigned)yy >= (unsigned)ny || (unsigned)zz >= (unsigned)nz) continue;
+      const int u = xx + nx * (yy + ny * zz);
+#pragma unroll
+      for (int ci = 0; ci < CI; ++ci) {
+        float val = __ldg(a.in + (size_t)ci * nv + u);
+        if (LD == LD_GATED) val *= __ldg(a.in_gate + (size_t)ci * nv + u);
+        acc = fmaf(wco[ci * kTaps + tap], val, acc);
+      }
+    }
+    if (EP == EP_GATE) acc *= __ldg(a.out_gate + (size_t)co * nv + v);
+    a.out[(size_t)co * nv + v] = acc;
   }
 }
 
@@ -284,8 +333,7 @@ __global__ void k_prolong_gate(Dims c, Dims f, const float* __restrict__ gx, con
 //                EP_PLAIN  out[co][v] = acc                         (decoder)
 //                EP_OUT    z[g] = dinv[g] r[g] + sqrt(dinv[g]) acc  (decoder, level 0; CO = 1)
 //                EP_OUTLAT z[v] = dinv[v] r[v] + dsq[v] acc         (same, vectors on the lattice)
-enum { LD_PLAIN = 0, LD_GATED = 1, LD_GATHER = 2 };
-enum { EP_GATE = 0, EP_PLAIN = 1, EP_OUT = 2, EP_OUTLAT = 3 };
+
 constexpr int kTX = 16, kTY = 8;
 
 struct TConvArgs {
@@ -303,13 +351,17 @@ struct TConvArgs {
   float* z;
 };
 
+// Halo rows are padded to a multiple of 4 floats (HXP) so a thread reads the XT + 2 = 6
+// inputs of a row as one float4 and one float2; single-output-channel weights are stored
+// [ci][dz][dy][4] (dx = 0..2, slot 3 zero) and read as one float4 per row.
 template <int CI, int CO, int XT, int TZ>
 struct TConvShape {
   static constexpr int HX = kTX + 2, HY = kTY + 2, HZ = TZ + 2;
-  static constexpr int HP = HX * HY * HZ;
+  static constexpr int HXP = (HX + 3) & ~3;
+  static constexpr int HP = HXP * HY * HZ;
   static constexpr int LX = kTX / XT;
   static constexpr int threads = LX * kTY * TZ;
-  static constexpr int nw = CI * kTaps * CO;
+  static constexpr int nw = CO == 1 ? CI * 9 * 4 : CI * kTaps * CO;
   static constexpr size_t smem = sizeof(float) * (size_t)(nw + CI * HP);
 };
 
@@ -325,30 +377,65 @@ __global__ void __launch_bounds__(TConvShape<CI, CO, XT, TZ>::threads) k_tconv(T
   const int bx = blockIdx.x % tiles_x, by = (blockIdx.x / tiles_x) % tiles_y, bz = blockIdx.x / (tiles_x * tiles_y);
   const int x0 = bx * kTX, y0 = by * kTY, z0 = bz * TZ;
   for (int i = threadIdx.x; i < S::nw; i += S::threads) {
-    const int co = i % CO, tap = (i / CO) % kTaps, ci = i / (kTaps * CO);
-    sw[i] = a.adjoint ? a.W[(ci * CO + co) * kTaps + (kTaps - 1 - tap)] : a.W[(co * CI + ci) * kTaps + tap];
-  }
-  for (int i = threadIdx.x; i < S::HP; i += S::threads) {
-    const int hx = i % S::HX, hy = (i / S::HX) % S::HY, hz = i / (S::HX * S::HY);
-    const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
-    const bool inb = gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz;
-    const int u = gx + nx * (gy + ny * gz);
-    if (LD == LD_GATHER) {
-      float v = 0.f;
-      if (inb) {
-        const int32_t g = __ldg(a.node_gid + u);
-        if (g >= 0) v = sqrtf(__ldg(a.dinv + g)) * __ldg(a.r + g);
-      }
-      sx[i] = v;
+    int co, tap, ci;
+    if (CO == 1) {   // [ci][dz][dy][4]
+      const int dx = i % 4, row = (i / 4) % 9;
+      ci = i / 36;
+      co = 0;
+      tap = dx < 3 ? row * 3 + dx : -1;
     } else {
+      co = i % CO;
+      tap = (i / CO) % kTaps;
+      ci = i / (kTaps * CO);
+    }
+    sw[i] = tap < 0 ? 0.f
+                    : (a.adjoint ? a.W[(ci * CO + co) * kTaps + (kTaps - 1 - tap)] : a.W[(co * CI + ci) * kTaps + tap]);
+  }
+  // halo: U elements per thread per step, all loads issued before any is used, so a CTA
+  // waits for a few load latencies instead of one per element (the gathered level-0 input
+  // is a node -> gid -> value chain)
+  constexpr int U = CI == 1 ? 8 : 2;
+  for (int i0 = threadIdx.x; i0 < S::HP; i0 += S::threads * U) {
+    int uu[U];
+    bool inb[U];
 #pragma unroll
-      for (int ci = 0; ci < CI; ++ci) {
-        float v = 0.f;
-        if (inb) {
-          v = __ldg(a.in + (size_t)ci * nv + u);
-          if (LD == LD_GATED) v *= __ldg(a.in_gate + (size_t)ci * nv + u);
+    for (int k = 0; k < U; ++k) {
+      const int i = i0 + k * S::threads;
+      const int hx = i % S::HXP, hy = (i / S::HXP) % S::HY, hz = i / (S::HXP * S::HY);
+      const int gx = x0 + hx - 1, gy = y0 + hy - 1, gz = z0 + hz - 1;
+      inb[k] = i < S::HP && hx < S::HX && gx >= 0 && gx < nx && gy >= 0 && gy < ny && gz >= 0 && gz < nz;
+      uu[k] = inb[k] ? gx + nx * (gy + ny * gz) : 0;
+    }
+    if (LD == LD_GATHER) {
+      int32_t gg[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) gg[k] = inb[k] ? __ldg(a.node_gid + uu[k]) : -1;
+      float dv[U], rv[U];
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        dv[k] = gg[k] >= 0 ? __ldg(a.dinv + gg[k]) : 0.f;
+        rv[k] = gg[k] >= 0 ? __ldg(a.r + gg[k]) : 0.f;
+      }
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const int i = i0 + k * S::threads;
+        if (i < S::HP) sx[i] = gg[k] >= 0 ? sqrtf(dv[k]) * rv[k] : 0.f;
+      }
+    } else {
+      float v[U][CI];
+#pragma unroll
+      for (int k = 0; k < U; ++k)
+#pragma unroll
+        for (int ci = 0; ci < CI; ++ci) {
+          v[k][ci] = inb[k] ? __ldg(a.in + (size_t)ci * nv + uu[k]) : 0.f;
+          if (LD == LD_GATED && inb[k]) v[k][ci] *= __ldg(a.in_gate + (size_t)ci * nv + uu[k]);
         }
-        sx[ci * S::HP + i] = v;
+#pragma unroll
+      for (int k = 0; k < U; ++k) {
+        const int i = i0 + k * S::threads;
+        if (i < S::HP)
+#pragma unroll
+          for (int ci = 0; ci < CI; ++ci) sx[ci * S::HP + i] = v[k][ci];
       }
     }
   }
@@ -365,15 +452,36 @@ __global__ void __launch_bounds__(TConvShape<CI, CO, XT, TZ>::threads) k_tconv(T
     for (int dz = 0; dz < 3; ++dz)
 #pragma unroll
       for (int dy = 0; dy < 3; ++dy) {
-        const float* row = sx + ci * S::HP + (tz + dz) * (S::HX * S::HY) + (ty + dy) * S::HX + tx * XT;
+        const float* row = sx + ci * S::HP + (tz + dz) * (S::HXP * S::HY) + (ty + dy) * S::HXP + tx * XT;
         float v[XT + 2];
+        if constexpr (XT == 4) {
+          const float4 a4 = *reinterpret_cast<const float4*>(row);
+          const float2 b2 = *reinterpret_cast<const float2*>(row + 4);
+          v[0] = a4.x;
+          v[1] = a4.y;
+          v[2] = a4.z;
+          v[3] = a4.w;
+          v[4] = b2.x;
+          v[5] = b2.y;
+        } else {
 #pragma unroll
-        for (int k = 0; k < XT + 2; ++k) v[k] = row[k];
+          for (int k = 0; k < XT + 2; ++k) v[k] = row[k];
+        }
+        float w1[4];
+        if constexpr (CO == 1) {
+          const float4 t = *reinterpret_cast<const float4*>(sw + (ci * 9 + dz * 3 + dy) * 4);
+          w1[0] = t.x;
+          w1[1] = t.y;
+          w1[2] = t.z;
+          w1[3] = t.w;
+        }
 #pragma unroll
         for (int dx = 0; dx < 3; ++dx) {
           const float* wp = sw + (ci * kTaps + dz * 9 + dy * 3 + dx) * CO;
           float w[CO];
-          if constexpr (CO % 4 == 0) {
+          if constexpr (CO == 1) {
+            w[0] = w1[dx];
+          } else if constexpr (CO % 4 == 0) {
 #pragma unroll
             for (int q = 0; q < CO / 4; ++q) {
               const float4 t = reinterpret_cast<const float4*>(wp)[q];
@@ -657,7 +765,7 @@ static int net_encode(gd_learned* N, int p, cudaStream_t st) {
   const float* P = N->params.p;
   for (int l = 0; l < N->levels; ++l) {
     if (l > 0)
-      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[p][l - 1].p, N->x[p][l].p,
+      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[p][l - 1].p, N->x[p][l].p,
                                                         1.f);
     GD_TRY(conv_launch(cin_of(l), kC, N->L[l], N->x[p][l].p, P + N->offW[l], nullptr, nullptr, N->a[p][l].p, 0, 0, st));
     k_mul<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->a[p][l].p, N->s[l].p, N->h[p][l].p);
@@ -677,7 +785,7 @@ static int net_decode(gd_learned* N, int p, cudaStream_t st) {
     GD_TRY(conv_launch(kC, cin_of(l), N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, out, 1, 0, st));
     if (l > 0) {
       k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[p][l - 1].p, N->u[l - 1].p);
-      k_prolong<<<nb_for(N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->u[l - 1].p,
+      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->u[l - 1].p,
                                                            0.125f, 1);
     }
   }
@@ -701,7 +809,7 @@ static int net_encoder_backward(gd_learned* N, int p, int q, cudaStream_t st) {
     if (l > 0) {
       GD_TRY(conv_launch(kC, kC, N->L[l], N->da[l].p, P + N->offW[l], nullptr, nullptr, N->gx[l].p, 1, 0, st));
       k_copyf<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC * N->nl[l - 1], N->h[q][l - 1].p, N->d[l - 1].p);
-      k_prolong<<<nb_for(N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->d[l - 1].p,
+      k_prolong<<<nb_for(kC * N->nl[l - 1]), kLT, 0, st>>>(kC, N->L[l], N->L[l - 1], N->gx[l].p, N->d[l - 1].p,
                                                            0.125f, 1);
     }
   }
@@ -756,6 +864,22 @@ static int net_loss(gd_learned* N, const float* z, const float* e, double* loss,
   return GD_OK;
 }
 
+// levels with fewer voxels than this use the direct convolution (one thread per voxel and
+// output channel) instead of the shared-memory tiles
+constexpr int64_t kDirectConvVoxels = 60000;
+// levels below this (but above the direct limit) use 2 voxels per thread: twice the
+// threads per tile, so a level of ~10^5 voxels still fills the SMs
+constexpr int64_t kWideTileVoxels = 400000;
+
+template <int LD, int EP>
+static int direct_launch(const Dims& d, const float* in, const float* in_gate, const float* W, int adjoint,
+                         const float* out_gate, float* out, cudaStream_t st) {
+  TConvArgsS a{d, in, in_gate, W, adjoint, kC, out_gate, out};
+  k_conv_direct<kC, LD, EP><<<nb_for(kC * d.size()), kLT, 0, st>>>(a);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
 template <int CI, int CO, int XT, int TZ, int LD, int EP>
 static int tconv_launch(const TConvArgs& a, cudaStream_t st) {
   using S = TConvShape<CI, CO, XT, TZ>;
@@ -791,9 +915,14 @@ static int net_apply_fast(gd_learned* N, const float* r, float* z, cudaStream_t 
       t.in = nullptr;
       GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATHER, EP_GATE>(t, st)));
     } else {
-      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
+      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
       t.in = N->x[0][l].p;
-      GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
+      if (N->nl[l] < kDirectConvVoxels)
+        GD_TRY((direct_launch<LD_PLAIN, EP_GATE>(t.d, t.in, nullptr, t.W, 0, t.out_gate, t.out, st)));
+      else if (N->nl[l] < kWideTileVoxels)
+        GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_GATE>(t, st)));
+      else
+        GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
     }
   }
   // decoder (adjoint convolutions)
@@ -816,8 +945,14 @@ static int net_apply_fast(gd_learned* N, const float* r, float* z, cudaStream_t 
       t.in_gate = nullptr;
     }
     if (l == 0) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 8, 8, LD_GATED, EP_OUT>(t, st)));
-      else GD_TRY((tconv_launch<kC, 1, 8, 8, LD_PLAIN, EP_OUT>(t, st)));
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUT>(t, st)));
+      else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUT>(t, st)));
+    } else if (N->nl[l] < kDirectConvVoxels) {
+      if (ld == LD_GATED) GD_TRY((direct_launch<LD_GATED, EP_PLAIN>(t.d, t.in, t.in_gate, t.W, 1, nullptr, t.out, st)));
+      else GD_TRY((direct_launch<LD_PLAIN, EP_PLAIN>(t.d, t.in, nullptr, t.W, 1, nullptr, t.out, st)));
+    } else if (N->nl[l] < kWideTileVoxels) {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 2, 4, LD_GATED, EP_PLAIN>(t, st)));
+      else GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_PLAIN>(t, st)));
     } else {
       if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
       else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
@@ -847,10 +982,15 @@ static int net_apply_lattice(gd_learned* N, const float* r, float* z, cudaStream
       t.in_gate = N->dsq.p;
       GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATED, EP_GATE>(t, st)));
     } else {
-      k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
+      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
       t.in = N->x[0][l].p;
       t.in_gate = nullptr;
-      GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
+      if (N->nl[l] < kDirectConvVoxels)
+        GD_TRY((direct_launch<LD_PLAIN, EP_GATE>(t.d, t.in, nullptr, t.W, 0, t.out_gate, t.out, st)));
+      else if (N->nl[l] < kWideTileVoxels)
+        GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_GATE>(t, st)));
+      else
+        GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
     }
   }
   for (int l = Lv - 1; l >= 0; --l) {
@@ -872,8 +1012,14 @@ static int net_apply_lattice(gd_learned* N, const float* r, float* z, cudaStream
       t.in_gate = nullptr;
     }
     if (l == 0) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 8, 8, LD_GATED, EP_OUTLAT>(t, st)));
-      else GD_TRY((tconv_launch<kC, 1, 8, 8, LD_PLAIN, EP_OUTLAT>(t, st)));
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUTLAT>(t, st)));
+      else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUTLAT>(t, st)));
+    } else if (N->nl[l] < kDirectConvVoxels) {
+      if (ld == LD_GATED) GD_TRY((direct_launch<LD_GATED, EP_PLAIN>(t.d, t.in, t.in_gate, t.W, 1, nullptr, t.out, st)));
+      else GD_TRY((direct_launch<LD_PLAIN, EP_PLAIN>(t.d, t.in, nullptr, t.W, 1, nullptr, t.out, st)));
+    } else if (N->nl[l] < kWideTileVoxels) {
+      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 2, 4, LD_GATED, EP_PLAIN>(t, st)));
+      else GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_PLAIN>(t, st)));
     } else {
       if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
       else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
