@@ -285,8 +285,31 @@ __device__ __forceinline__ bool bad_coefficient(double k) {
 // Cube cells: w_c = Kc[3] * kappa_c once per cell (validated here), so a 3D row needs
 // 12 adds for the face diagonals, 3 adds + 1 multiply for the diagonal, and nothing
 // for the corners (w itself) and the edge neighbours (exactly 0 on a cube).
+// Each thread streams 4 cells as two 16-byte loads issued together (one 8-byte load in
+// flight per thread would cap the kernel near 2.5 TB/s); kappa must be 16-byte aligned
+// (w always is), otherwise k_prescale_scalar runs.
 __global__ void k_prescale(int64_t ncells, const double* __restrict__ kappa, double scale, double* __restrict__ w,
                            int32_t* __restrict__ bad) {
+  int nbad = 0;
+  const int64_t n4 = ncells >> 2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(kappa) + 2 * i);
+    const double2 b = __ldg(reinterpret_cast<const double2*>(kappa) + 2 * i + 1);
+    nbad += bad_coefficient(a.x) + bad_coefficient(a.y) + bad_coefficient(b.x) + bad_coefficient(b.y);
+    reinterpret_cast<double2*>(w)[2 * i] = make_double2(scale * a.x, scale * a.y);
+    reinterpret_cast<double2*>(w)[2 * i + 1] = make_double2(scale * b.x, scale * b.y);
+  }
+  if (blockIdx.x == 0 && threadIdx.x < (ncells & 3)) {   // tail
+    const int64_t i = (n4 << 2) + threadIdx.x;
+    const double k = kappa[i];
+    nbad += bad_coefficient(k);
+    w[i] = scale * k;
+  }
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+__global__ void k_prescale_scalar(int64_t ncells, const double* __restrict__ kappa, double scale,
+                                  double* __restrict__ w, int32_t* __restrict__ bad) {
   int nbad = 0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < ncells; i += (int64_t)gridDim.x * blockDim.x) {
     const double k = kappa[i];
@@ -674,8 +697,13 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
   const double* coef = kappa;
   if (cube) {   // w = Kc[3] * kappa, validated on the way
     if (A->w_cells.n != (size_t)ncells) GD_TRY(dalloc(A->w_cells, ncells));
-    int blocks = (int)std::min<int64_t>((ncells + 255) / 256, 4096);
-    k_prescale<<<blocks, 256, 0, st>>>(ncells, kappa, q.Kc[3], A->w_cells.p, bad);
+    if (((uintptr_t)kappa & 15) == 0) {
+      const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((ncells / 4 + 255) / 256, 8192));
+      k_prescale<<<blocks, 256, 0, st>>>(ncells, kappa, q.Kc[3], A->w_cells.p, bad);
+    } else {
+      const int blocks = (int)std::min<int64_t>((ncells + 255) / 256, 4096);
+      k_prescale_scalar<<<blocks, 256, 0, st>>>(ncells, kappa, q.Kc[3], A->w_cells.p, bad);
+    }
     GD_CUDA_TRY(cudaGetLastError());
     coef = A->w_cells.p;
   }
