@@ -224,6 +224,8 @@ struct gd_space {
   bool has_dirichlet_values = false;
   // table: lexicographic cell-local node -> Gridap cell-local node index
   std::vector<int> lex_to_gridap;
+  // lattice node -> gid (-1: Dirichlet), built on first use by post-processing
+  gd::DBuf<int32_t> lat_gid;
 };
 
 struct gd_asm {

@@ -344,27 +344,40 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   int it = 0;
   bool conv = bnorm == 0.0;
   const int check_every = 8;
-  while (!conv && it < maxit) {
-    int nstep = std::min(check_every, maxit - it);
-    for (int s = 0; s < nstep; ++s) {
-      k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
-      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
-      k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, A->dinv.p, pa, pb);
-      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
-      k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
+  // When the recursive residual meets the tolerance but the true one (recomputed in FP64)
+  // does not -- rounding makes the two drift apart near tight tolerances -- CG restarts
+  // from the true residual, at most kMaxRestarts times.
+  constexpr int kMaxRestarts = 3;
+  for (int restart = 0;; ++restart) {
+    while (!conv && it < maxit) {
+      int nstep = std::min(check_every, maxit - it);
+      for (int s = 0; s < nstep; ++s) {
+        k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
+        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
+        k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, A->dinv.p, pa, pb);
+        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
+        k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
+      }
+      GD_CUDA_TRY(cudaGetLastError());
+      it += nstep;
+      GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+      GD_CUDA_TRY(cudaStreamSynchronize(st));
+      if (!std::isfinite(h.rr)) break;
+      if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
     }
+    // true FP64 residual (kept in r for a restart)
+    k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, dr, pa, pb);
+    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
     GD_CUDA_TRY(cudaGetLastError());
-    it += nstep;
     GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
     GD_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!std::isfinite(h.rr)) break;
-    if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
+    const double rel_true = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
+    if (!conv || rel_true <= rtol || !std::isfinite(rel_true) || it >= maxit || restart >= kMaxRestarts) break;
+    conv = false;
+    k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, A->dinv.p, dr, dz, dp, pa, pb);
+    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
+    GD_CUDA_TRY(cudaGetLastError());
   }
-  // true FP64 residual
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, nullptr, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
-  GD_CUDA_TRY(cudaGetLastError());
-  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaMemcpyAsync(x, dx, sizeof(double) * n,
                               where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));

@@ -544,6 +544,7 @@ extern "C" int gd_space_destroy(gd_space* S) {
   dfreeb(S->lid_ownidx);
   dfreeb(S->lid_gid);
   dfreeb(S->u_dir);
+  dfreeb(S->lat_gid);
   delete S;
   return GD_OK;
 }

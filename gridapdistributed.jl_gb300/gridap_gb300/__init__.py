@@ -9,6 +9,7 @@ from .distributed import (AffineFEOperator, CartesianDiscreteModel, FEFunction, 
                           ReferenceFE, SparseMatrixAssembler, SubAssembledRows, TestFESpace,
                           Triangulation, TrialFESpace, VectorValue, assemble_matrix_and_vector,
                           collect_cell_matrix_and_vector, integral_elasticity, integral_grad_grad,
-                          integral_source, lagrangian, solve, with_gb300)
+                          integral_source, l2_error, lagrangian, quadrature_points, solve,
+                          with_gb300)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -94,6 +94,7 @@ SIGNATURES = {
     "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_assemble_elasticity": [P, P],
+    "gd_l2_error": [P, P, P, C.c_int, C.c_int, DP],
     "gd_batch_create": [P, P, C.c_int, PP],
     "gd_batch_destroy": [P],
     "gd_batch_assemble": [P],

@@ -559,6 +559,43 @@ class FEFunction:
         return u
 
 
+def _gauss01(nq):
+    x, w = np.polynomial.legendre.leggauss(nq)
+    return 0.5 * (x + 1.0), 0.5 * w
+
+
+def quadrature_points(model: DistributedDiscreteModel, degree: int):
+    """Physical coordinates (ncells * nq^dim, dim) of the tensor Gauss points of every
+    global cell (cells lexicographic, points x fastest), nq = (degree + 2) // 2."""
+    dim = model.dim
+    nq = (int(degree) + 2) // 2
+    xq, _ = _gauss01(nq)
+    h = [(model.domain[2 * d + 1] - model.domain[2 * d]) / model.cells[d] for d in range(dim)]
+    cells = np.indices(tuple(reversed(model.cells))).reshape(dim, -1)[::-1]        # (dim, ncells), x fastest
+    q = np.indices((nq,) * dim).reshape(dim, -1)[::-1]                              # (dim, nqt), x fastest
+    out = np.empty((cells.shape[1], q.shape[1], dim))
+    for d in range(dim):
+        out[:, :, d] = model.domain[2 * d] + (cells[d][:, None] + xq[q[d]][None, :]) * h[d]
+    return out.reshape(-1, dim)
+
+
+def l2_error(uh: "FEFunction", u_exact, measure: Measure) -> float:
+    """``sqrt(sum(∫( abs2(u - uh) )dΩ))`` on the device; ``u_exact`` is a vectorised callable
+    of the coordinates (a tuple of components on vector spaces)."""
+    U = uh.U
+    xyz = quadrature_points(U.model, measure.degree)
+    vals = u_exact(*[xyz[:, d] for d in range(U.model.dim)])
+    if U.ncomp > 1:
+        vals = np.stack([np.broadcast_to(np.asarray(v, dtype=np.float64), (xyz.shape[0],)) for v in vals], axis=1)
+    else:
+        vals = np.broadcast_to(np.asarray(vals, dtype=np.float64), (xyz.shape[0],))
+    vals = np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)
+    err = C.c_double()
+    L.call("gd_l2_error", U.handle, L.vptr(uh.free_values), L.vptr(vals), int(measure.degree), L.GD_HOST,
+           C.byref(err))
+    return err.value
+
+
 def solve(op: AffineFEOperator, rtol=1e-12, maxit=100000):
     x = op.matrix.solve(rtol=rtol, maxit=maxit)
     return FEFunction(op.U, x)

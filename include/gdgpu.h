@@ -235,6 +235,13 @@ int gd_solve_rhs(gd_asm* a, int method, double rtol, int maxit, const double* b,
  * stream capture.  Every call shares the array and clears what must start at zero;
  * calls that overlap on the GPU race on it. */
 int gd_solve_noalloc(gd_asm* a, double rtol, int maxit, double* x, int where, gd_solve_stats* stats);
+/* sqrt(sum(int(abs2(u - u_h)) dOmega)) (test/PoissonTests.jl:43-45): u_h = FEFunction(U, x)
+ * with x the global free values (dim components interleaved on vector spaces) and the
+ * trial space's Dirichlet values; u_qp the exact solution at the tensor Gauss points
+ * ((degree+2)/2 per direction, on [0,1] mapped to each cell) of every global cell:
+ * index (cell * nq^dim + q) * ncomp + component, cells lexicographic, points x fastest.
+ * `where` applies to x and u_qp. */
+int gd_l2_error(gd_space* space, const double* x, const double* u_qp, int degree, int where, double* err);
 /* FEFunction(U, x) / consistent!: the local (owned+ghost) free values of one part
  * from a global vector (FESpaces.jl:354-371, Algebra.jl:270-293). */
 int gd_fe_function_local(const gd_space* space, int part, const double* x_global, int where,
