@@ -1,5 +1,9 @@
-// Post-processing on the device: the L2 error sqrt(sum(int(abs2(u - u_h)) dOmega)) of an
-// FE function, as the reference's tests compute it (test/PoissonTests.jl:43-45,
+// Boundary source terms and post-processing on the device.
+//
+// gd_add_boundary_source adds int(v g) dGamma over flagged boundary sides to the
+// assembled right-hand side (the Neumann term of test/PoissonTests.jl:20-41, g given at
+// the face Gauss points).  gd_l2_error is the L2 error sqrt(sum(int(abs2(u - u_h)) dOmega))
+// of an FE function, as the reference's tests compute it (test/PoissonTests.jl:43-45,
 // test/FESpacesTests.jl:36-40).  The exact solution comes sampled at the tensor Gauss
 // points of every cell (the caller evaluates it; a device cannot call back into the
 // host's function); u_h is evaluated from the cell's nodal values (free values by gid,
@@ -121,9 +125,138 @@ static int space_node_gid(gd_space* S, cudaStream_t st) {
   return GD_OK;
 }
 
+// ---- boundary source l(v) += int(v g) dGamma on flagged sides ------------------------------
+// One thread per owned row: the row's node X, on each flagged side it lies on, collects
+// sum_q w_q |J_face| phi_X(x_q) g(x_q) over the boundary faces around it (up to 2^(dim-1)),
+// phi_X restricted to the face being the product of the tangential 1D Lagrange factors.
+// g_qp: faces side by side (flagged sides in order x-, x+, y-, y+, z-, z+), lexicographic
+// over the face's cells in the remaining directions (lowest first), nq^(dim-1) points
+// per face (lowest remaining direction fastest).
+template <int DIM, int K>
+__global__ void k_boundary_rhs(Geom g, int64_t nrows_own, const int32_t* __restrict__ row_node, int side_mask,
+                               const int64_t* __restrict__ side_off, const double* __restrict__ g_qp, int nq,
+                               const double* __restrict__ tab, double* __restrict__ rhs) {
+  constexpr int KP1 = K + 1;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows_own) return;
+  int64_t lin = row_node[r];
+  int64_t X[3] = {0, 0, 0};
+  for (int d = 0; d < DIM; ++d) {
+    X[d] = lin % g.N[d];
+    lin /= g.N[d];
+  }
+  const double* V = tab;          // [nq][KP1]
+  const double* W = tab + nq * KP1;
+  double b = 0.0;
+  for (int s = 0; s < 2 * DIM; ++s) {
+    if (!((side_mask >> s) & 1)) continue;
+    const int d = s >> 1;
+    if (X[d] != ((s & 1) ? g.N[d] - 1 : 0)) continue;
+    int tang[2] = {0, 0}, nt = 0;
+    for (int t = 0; t < DIM; ++t)
+      if (t != d) tang[nt++] = t;
+    int64_t clo[2] = {0, 0}, chi[2] = {0, 0};
+    for (int j = 0; j < nt; ++j) {
+      const int t = tang[j];
+      const int64_t c = X[t] / K;
+      if (X[t] % K == 0) {
+        clo[j] = c - 1 < 0 ? 0 : c - 1;
+        chi[j] = c > g.n[t] - 1 ? g.n[t] - 1 : c;
+      } else {
+        clo[j] = chi[j] = c;
+      }
+    }
+    int nqf = 1;
+    for (int j = 0; j < nt; ++j) nqf *= nq;
+    for (int64_t c1 = clo[1]; c1 <= chi[1]; ++c1)
+      for (int64_t c0 = clo[0]; c0 <= chi[0]; ++c0) {
+        const int64_t cc[2] = {c0, c1};
+        const int64_t f = nt == 1 ? c0 : c0 + g.n[tang[0]] * c1;
+        int l[2] = {0, 0};
+        for (int j = 0; j < nt; ++j) l[j] = (int)(X[tang[j]] - K * cc[j]);
+        const double* gq = g_qp + (side_off[s] + f) * nqf;
+        for (int q = 0; q < nqf; ++q) {
+          double w = 1.0, phi = 1.0;
+          for (int j = 0, rest = q; j < nt; ++j) {
+            const int qj = rest % nq;
+            rest /= nq;
+            w *= W[qj] * g.h[tang[j]];
+            phi *= V[qj * KP1 + l[j]];
+          }
+          b = fma(w * phi, gq[q], b);
+        }
+      }
+  }
+  rhs[r] += b;
+}
+
 }  // namespace gd
 
 using namespace gd;
+
+extern "C" int gd_add_boundary_source(gd_asm* A, const int32_t* sides, const double* g_qp, int degree, int where) {
+  if (!A || !sides || !g_qp) return fail(GD_ERR_ARG, "gd_add_boundary_source: null argument");
+  if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_add_boundary_source: run the numeric assembly first");
+  if (A->bs != 1) return fail(GD_ERR_UNSUPPORTED, "gd_add_boundary_source: scalar spaces only");
+  const Geom& g = A->test->geom;
+  const int nq = (degree + 2) / 2;
+  if (nq < 1 || nq > kMaxQ) return fail(GD_ERR_ARG, "gd_add_boundary_source: quadrature degree out of range");
+  cudaStream_t st = A->test->model->ctx->stream;
+  int mask = 0;
+  std::vector<int64_t> off(2 * kMaxDim + 1, 0);
+  int64_t nfaces = 0;
+  int nqf = 1;
+  for (int d = 0; d + 1 < g.dim; ++d) nqf *= nq;
+  for (int s = 0; s < 2 * g.dim; ++s) {
+    off[s] = nfaces;
+    if (!sides[s]) continue;
+    mask |= 1 << s;
+    int64_t nf = 1;
+    for (int t = 0; t < g.dim; ++t)
+      if (t != s / 2) nf *= g.n[t];
+    nfaces += nf;
+  }
+  if (!mask) return GD_OK;
+  const double* dg = g_qp;
+  DBuf<double> hg, dtab;
+  DBuf<int64_t> doff;
+  if (where == GD_HOST) {
+    GD_TRY(dalloc(hg, nfaces * nqf));
+    GD_CUDA_TRY(cudaMemcpyAsync(hg.p, g_qp, sizeof(double) * nfaces * nqf, cudaMemcpyHostToDevice, st));
+    dg = hg.p;
+  }
+  const int kp1 = g.k + 1;
+  std::vector<double> xq, wq, tab(nq * kp1 + nq), dtmp(kp1);
+  gauss_legendre01(nq, xq, wq);
+  for (int q = 0; q < nq; ++q) {
+    lagrange01(g.k, xq[q], &tab[q * kp1], dtmp.data());
+    tab[nq * kp1 + q] = wq[q];
+  }
+  GD_TRY(dalloc(dtab, tab.size()));
+  GD_TRY(dalloc(doff, off.size()));
+  GD_CUDA_TRY(cudaMemcpyAsync(dtab.p, tab.data(), sizeof(double) * tab.size(), cudaMemcpyHostToDevice, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(doff.p, off.data(), sizeof(int64_t) * off.size(), cudaMemcpyHostToDevice, st));
+  const int64_t R = A->ngdofs;
+  if (R > 0) {
+    const unsigned nb = (unsigned)((R + 127) / 128);
+    const int sel = g.dim * 10 + g.k;
+#define BND_LAUNCH(D, K) \
+  k_boundary_rhs<D, K><<<nb, 128, 0, st>>>(g, R, A->row_node.p, mask, doff.p, dg, nq, dtab.p, A->rhs.p)
+    switch (sel) {
+      case 21: BND_LAUNCH(2, 1); break;
+      case 22: BND_LAUNCH(2, 2); break;
+      case 23: BND_LAUNCH(2, 3); break;
+      case 31: BND_LAUNCH(3, 1); break;
+      case 32: BND_LAUNCH(3, 2); break;
+      case 33: BND_LAUNCH(3, 3); break;
+      default: return fail(GD_ERR_UNSUPPORTED, "gd_add_boundary_source: unsupported dim/order");
+    }
+#undef BND_LAUNCH
+    GD_CUDA_TRY(cudaGetLastError());
+  }
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return GD_OK;
+}
 
 extern "C" int gd_l2_error(gd_space* S, const double* x, const double* u_qp, int degree, int where, double* err) {
   if (!S || !x || !u_qp || !err) return fail(GD_ERR_ARG, "gd_l2_error: null argument");

@@ -4,11 +4,12 @@
 ``include/gdgpu.h``; ``_lib`` is the ctypes binding of ``libgdgpu.so``.
 """
 from . import _lib
-from .distributed import (AffineFEOperator, CartesianDiscreteModel, FEFunction, FESpace,
+from .distributed import (AffineFEOperator, Boundary, CartesianDiscreteModel, FEFunction, FESpace,
                           FullyAssembledRows, GB300Backend, Measure, PSparseMatrix, PVector,
                           ReferenceFE, SparseMatrixAssembler, SubAssembledRows, TestFESpace,
                           Triangulation, TrialFESpace, VectorValue, assemble_matrix_and_vector,
-                          collect_cell_matrix_and_vector, integral_elasticity, integral_grad_grad,
+                          collect_cell_matrix_and_vector, integral_boundary_source, integral_elasticity,
+                          integral_grad_grad,
                           integral_source, l2_error, lagrangian, quadrature_points, solve,
                           with_gb300)
 

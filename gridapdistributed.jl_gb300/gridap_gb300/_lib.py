@@ -95,6 +95,7 @@ SIGNATURES = {
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_assemble_elasticity": [P, P],
     "gd_l2_error": [P, P, P, C.c_int, C.c_int, DP],
+    "gd_add_boundary_source": [P, I32P, P, C.c_int, C.c_int],
     "gd_batch_create": [P, P, C.c_int, PP],
     "gd_batch_destroy": [P],
     "gd_batch_assemble": [P],

@@ -140,6 +140,19 @@ class Triangulation:
 
 
 @dataclass
+class BoundaryTriangulation:
+    """``Boundary(model, tags=...)``: the boundary faces on the tagged sides of the box
+    ("left"/"right" = x min/max, "bottom"/"top" = y, "back"/"front" = z, or "boundary")."""
+
+    model: DistributedDiscreteModel
+    sides: np.ndarray
+
+
+def Boundary(model, tags="boundary"):
+    return BoundaryTriangulation(model, _sides_from_tags(model.dim, tags))
+
+
+@dataclass
 class Measure:
     trian: Triangulation
     degree: int
@@ -351,6 +364,58 @@ class SourceForm:
     measure: Measure
 
 
+@dataclass
+class BoundarySourceForm:
+    """l(v) = ∫( v g )dΓ on a BoundaryTriangulation; g is a vectorised callable of the
+    coordinates and the outward unit normal, g(x, y[, z], nx, ny[, nz])."""
+
+    g: object
+    measure: Measure
+
+
+class LinearFormSum(list):
+    """A sum of linear forms, e.g. ∫( v f )dΩ + ∫( v g )dΓn."""
+
+    def __add__(self, other):
+        return LinearFormSum(list(self) + [other])
+
+
+def _form_add(self, other):
+    return LinearFormSum([self, other])
+
+
+SourceForm.__add__ = _form_add
+BoundarySourceForm.__add__ = _form_add
+
+
+def integral_boundary_source(g, measure: Measure):
+    return BoundarySourceForm(g, measure)
+
+
+def boundary_quadrature_points(trian: BoundaryTriangulation, degree: int):
+    """Face Gauss points of the flagged sides, in the layout gd_add_boundary_source
+    expects: list of (side, coordinates (nfaces * nq^(dim-1), dim))."""
+    model = trian.model
+    dim = model.dim
+    nq = (int(degree) + 2) // 2
+    xq, _ = _gauss01(nq)
+    h = [(model.domain[2 * d + 1] - model.domain[2 * d]) / model.cells[d] for d in range(dim)]
+    out = []
+    for side in range(2 * dim):
+        if not trian.sides[side]:
+            continue
+        d = side // 2
+        tang = [t for t in range(dim) if t != d]
+        fc = np.indices(tuple(model.cells[t] for t in reversed(tang))).reshape(len(tang), -1)[::-1]
+        qq = np.indices((nq,) * len(tang)).reshape(len(tang), -1)[::-1]
+        pts = np.empty((fc.shape[1], qq.shape[1], dim))
+        pts[:, :, d] = model.domain[2 * d + (side & 1)]
+        for j, t in enumerate(tang):
+            pts[:, :, t] = model.domain[2 * t] + (fc[j][:, None] + xq[qq[j]][None, :]) * h[t]
+        out.append((side, pts.reshape(-1, dim)))
+    return out
+
+
 def integral_grad_grad(kappa=None, measure: Measure = None):
     return GradGradForm(None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64), measure)
 
@@ -380,8 +445,36 @@ class DistributedSparseMatrixAssembler:
             L.call("gd_assemble_symbolic", self.handle)
             self._symbolic = True
 
-    def numeric(self, a, l: SourceForm):
+    def numeric(self, a, l):
         self.symbolic()
+        bnd = []
+        if isinstance(l, (list, tuple)):
+            vol = [f for f in l if isinstance(f, SourceForm)]
+            bnd = [f for f in l if isinstance(f, BoundarySourceForm)]
+            if len(vol) > 1:
+                raise NotImplementedError("one volume source term")
+            l = vol[0] if vol else None
+        elif isinstance(l, BoundarySourceForm):
+            bnd, l = [l], None
+        self._numeric(a, l)
+        for bf in bnd:
+            self._boundary(bf)
+
+    def _boundary(self, bf):
+        trian = bf.measure.trian
+        dim = trian.model.dim
+        vals = []
+        for side, pts in boundary_quadrature_points(trian, bf.measure.degree):
+            normal = [0.0] * dim
+            normal[side // 2] = 1.0 if side & 1 else -1.0
+            v = bf.g(*[pts[:, d] for d in range(dim)], *[np.full(len(pts), c) for c in normal])
+            vals.append(np.broadcast_to(np.asarray(v, dtype=np.float64), (len(pts),)))
+        g = np.ascontiguousarray(np.concatenate(vals) if vals else np.zeros(1))
+        sides = np.ascontiguousarray(trian.sides, dtype=np.int32)
+        L.call("gd_add_boundary_source", self.handle, L.ptr(sides, C.c_int32), L.vptr(g), int(bf.measure.degree),
+               L.GD_HOST)
+
+    def _numeric(self, a, l):
         if isinstance(a, ElasticityForm):
             c = L.gd_elasticity()
             c.E = None if a.E is None else a.E.ctypes.data

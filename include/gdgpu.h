@@ -168,6 +168,15 @@ typedef struct gd_elasticity {
  * vector-space assembler (dof = dim * node dof + component). */
 int gd_assemble_elasticity(gd_asm* a, const gd_elasticity* c);
 
+/* l(v) += int(v g) dGamma over the boundary sides flagged in `sides` (2*dim flags in the
+ * order of dirichlet_sides; the Neumann term of test/PoissonTests.jl:20-41), added to
+ * the owned rows of the assembled rhs -- call after gd_assemble_numeric.  g_qp holds g at
+ * the face Gauss points ((degree+2)/2 per direction): faces side by side (flagged sides
+ * in order x-, x+, y-, y+, z-, z+), on a side lexicographic over the face's cells in the
+ * remaining directions (lowest first), points lowest remaining direction fastest.
+ * Scalar spaces. */
+int gd_add_boundary_source(gd_asm* a, const int32_t* sides, const double* g_qp, int degree, int where);
+
 /* Record CUDA events around the phases of every numeric assembly (off by default). */
 int gd_assembler_set_profiling(gd_asm* a, int on);
 /* Event-timed durations (ms) of the last profiled numeric assembly: clearing the

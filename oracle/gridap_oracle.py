@@ -589,6 +589,7 @@ class Problem:
     f_const: float = 0.0            # constant source
     f_nodal: np.ndarray = None      # or nodal source values on the global lattice (b = M f)
     u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0
+    neumann: dict = None            # {side: g(*xyz, *normal)}, side 2d (x_d = min) / 2d+1 (max): l += int(v g)dGamma
     physics: str = "poisson"        # or "elasticity"
     nu: float = 0.3                 # Poisson ratio (elasticity)
     force: tuple = None             # body force (elasticity), default 0
@@ -668,6 +669,7 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
             mats.append(pb.kappa[g] * Kel)
             vecs.append(be.copy())
         return mats, vecs
+    nbt = neumann_tables(pb) if pb.neumann else None
     for ic, g in enumerate(sp.cells):
         kap = pb.kappa[g]
         Ke = kap * Kh
@@ -681,9 +683,48 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
         if pb.u_dir is not None:
             ud = np.where(dofs < 0, pb.u_dir[pb.node_lin(X)], 0.0)
             be = be - Ke @ ud
+        if nbt is not None:
+            be = be + neumann_cell_load(pb, ci, lnodes, nbt)
         mats.append(Ke)
         vecs.append(be)
     return mats, vecs
+
+
+def neumann_tables(pb: Problem):
+    nq = quad_points_per_dir(pb.degree)
+    xq, wq = gauss_legendre(nq)
+    V, _ = lagrange_1d(pb.order, xq)
+    return nq, xq, wq, V
+
+
+def neumann_cell_load(pb: Problem, ci, lnodes, tabs):
+    """``int(v g)dGamma`` over the cell's faces on the Neumann sides (Gridap boundary
+    triangulation restricted to the cell; g evaluated at the face Gauss points)."""
+    nq, xq, wq, V = tabs
+    dim, k, h = pb.dim, pb.order, pb.h
+    be = np.zeros(len(lnodes))
+    for side, gfun in pb.neumann.items():
+        d, hi = side // 2, side % 2
+        if ci[d] != (pb.n[d] - 1 if hi else 0):
+            continue
+        tang = [t for t in range(dim) if t != d]
+        normal = [0.0] * dim
+        normal[d] = 1.0 if hi else -1.0
+        for qi in itertools.product(*[range(nq)] * len(tang)):
+            qi = tuple(reversed(qi))
+            w = 1.0
+            xyz = [0.0] * dim
+            xyz[d] = pb.domain[2 * d + hi]
+            for j, t in enumerate(tang):
+                w *= wq[qi[j]] * h[t]
+                xyz[t] = pb.domain[2 * t] + (ci[t] + xq[qi[j]]) * h[t]
+            gv = gfun(*xyz, *normal)
+            for a, off in enumerate(lnodes):
+                if off[d] != (k if hi else 0):
+                    continue   # the node's basis function vanishes on this face
+                phi = np.prod([V[qi[j], off[t]] for j, t in enumerate(tang)])
+                be[a] += w * phi * gv
+    return be
 
 
 def P_cell_coords(n, gid):
