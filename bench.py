@@ -388,7 +388,7 @@ def run_learned(args, be, dev):
     from gridap_gb300.learned import LearnedPreconditioner
     from gridap_gb300.synthetic import DIFFUSION3D_96, lognormal_kappa
     w = DIFFUSION3D_96
-    path = PKG / "gridap_gb300" / "weights" / "diffusion3d_q1_l4.gdlp"
+    path = PKG / "gridap_gb300" / "weights" / "diffusion3d_q1.gdlp"
     if not path.exists():
         return None
     cells = w["cells"]
@@ -400,9 +400,10 @@ def run_learned(args, be, dev):
     kap = lognormal_kappa(cells, w["sigma"], w["corr_len"], seed=w["seed"] + 1)
     f = np.random.default_rng(w["seed"] + 100).standard_normal(int(np.prod([c + 1 for c in cells])))
     op = G.AffineFEOperator(G.integral_grad_grad(kap, dO), G.integral_source(f, dO), U, V)
-    net = LearnedPreconditioner(op.matrix, seed=0, levels=LearnedPreconditioner.file_levels(path))
+    levels, cs = LearnedPreconditioner.file_spec(path)
+    net = LearnedPreconditioner(op.matrix, seed=0, levels=levels, coarse_start=cs)
     net.load(path)
-    out = {"workload": w["name"], "rtol": 1e-8, "weights": path.name, "levels": net.levels,
+    out = {"workload": w["name"], "rtol": 1e-8, "weights": path.name, "levels": net.levels, "coarse_start": cs,
            "params": net.num_params}
     runs = {}
     for name, fn in (("jacobi_pcg_fp64", lambda: op.matrix.solve(rtol=1e-8, method="jacobi_pcg")),

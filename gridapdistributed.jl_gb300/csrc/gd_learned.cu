@@ -11,7 +11,9 @@
 //   S x_0 = (h_0, ..., h_{L-1})
 // and S^T is its exact adjoint (the decoder shares the encoder's weights: a U-net with
 // tied weights), so the learned term is positive semi-definite and plain (or flexible)
-// CG applies.  R is full-weighting restriction (coarse node i <-> fine node 2i), P = 8 R^T
+// CG applies.  With the coarse-start option the network runs on the once-restricted
+// lattice, z = D^-1 r + D^-1/2 R^T S^T S R D^-1/2 r (still SPD): the fine-scale error is
+// left to the Jacobi term and the costliest level of the application disappears.  R is full-weighting restriction (coarse node i <-> fine node 2i), P = 8 R^T
 // trilinear prolongation, conv3 a 3x3x3 convolution with zero padding.  Training
 // minimises the relative A-norm error ||z - e||_A^2 / ||e||_A^2 over (residual, error)
 // pairs generated by the solver, with hand-written backward kernels and Adam.  All in
@@ -283,6 +285,44 @@ __global__ void k_prolong_gate(Dims c, Dims f, const float* __restrict__ gx, con
       out[o] = fmaf(scale, acc[ch], __ldg(h + o)) * __ldg(s + o);
     }
   }
+}
+
+// coarse-start input on the lattice: coarse[i] = sum_o w(o) dsq[2i+o] r[2i+o]
+__global__ void k_scale_restrict(Dims f, Dims c, const float* __restrict__ r, const float* __restrict__ dsq,
+                                 float* __restrict__ coarse) {
+  const int nc = (int)c.size();
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nc; i += gridDim.x * blockDim.x) {
+    const int ix = i % c.n[0], iy = (i / c.n[0]) % c.n[1], iz = i / (c.n[0] * c.n[1]);
+    float acc = 0.f;
+#pragma unroll
+    for (int oz = -1; oz <= 1; ++oz) {
+      const int fz = 2 * iz + oz;
+      if (fz < 0 || fz >= f.n[2]) continue;
+#pragma unroll
+      for (int oy = -1; oy <= 1; ++oy) {
+        const int fy = 2 * iy + oy;
+        if (fy < 0 || fy >= f.n[1]) continue;
+#pragma unroll
+        for (int ox = -1; ox <= 1; ++ox) {
+          const int fx = 2 * ix + ox;
+          if (fx < 0 || fx >= f.n[0]) continue;
+          const float w = (ox == 0 ? 0.5f : 0.25f) * (oy == 0 ? 0.5f : 0.25f) * (oz == 0 ? 0.5f : 0.25f);
+          const int u = fx + f.n[0] * (fy + f.n[1] * fz);
+          acc = fmaf(w, __ldg(dsq + u) * __ldg(r + u), acc);
+        }
+      }
+    }
+    coarse[i] = acc;
+  }
+}
+
+// coarse-start output on the lattice: z[j] = dinv[j] r[j] + dsq[j] (P zc)[j] / 8
+__global__ void k_prolong_out_lattice(Dims c, Dims f, const float* __restrict__ zc, const float* __restrict__ r,
+                                      const float* __restrict__ dinv, const float* __restrict__ dsq,
+                                      float* __restrict__ z) {
+  const int nf = (int)f.size();
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < nf; j += gridDim.x * blockDim.x)
+    z[j] = fmaf(__ldg(dsq + j), 0.125f * prolong_at(c, f, zc, j), __ldg(dinv + j) * __ldg(r + j));
 }
 
 // ---- direct convolution for the coarse levels ------------------------------------------------
@@ -682,6 +722,11 @@ struct gd_learned {
   DBuf<float> x[2][kMaxLevels], a[2][kMaxLevels], h[2][kMaxLevels];
   DBuf<float> u[kMaxLevels], gx[kMaxLevels], d[kMaxLevels], da[kMaxLevels], gp[kMaxLevels];
   DBuf<float> zl;
+  // coarse start: the network's level 0 is the once-restricted lattice
+  int cs = 0;
+  Dims LF{};          // node lattice
+  int64_t nlf = 0;
+  DBuf<float> xf, zf;   // node-lattice scratch (restriction input, prolongation output)
   DBuf<float> part;
   DBuf<double> dred;
   DBuf<float> zv, ev, dv, yv;
@@ -743,7 +788,12 @@ static int net_prepare(gd_learned* N, cudaStream_t st) {
   GD_CUDA_TRY(cudaMemcpyAsync(dn.p, hn, sizeof(hn), cudaMemcpyHostToDevice, st));
   const float* P = N->params.p;
   const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
-  k_node_logk<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->L[0], dn.p, A->w_cells.p, 1.0 / A->mf_k2, N->f[0].p);
+  if (N->cs) {
+    k_node_logk<<<nb_for(N->nlf), kLT, 0, st>>>(N->LF, dn.p, A->w_cells.p, 1.0 / A->mf_k2, N->xf.p);
+    k_restrict<<<nb_for(N->nl[0]), kLT, 0, st>>>(1, N->LF, N->L[0], N->xf.p, N->f[0].p, 1.f);
+  } else {
+    k_node_logk<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->L[0], dn.p, A->w_cells.p, 1.0 / A->mf_k2, N->f[0].p);
+  }
   for (int l = 1; l < N->levels; ++l)
     k_restrict<<<nb_for(N->nl[l]), kLT, 0, st>>>(1, N->L[l - 1], N->L[l], N->f[l - 1].p, N->f[l].p, 1.f);
   GD_CUDA_TRY(cudaGetLastError());
@@ -751,7 +801,7 @@ static int net_prepare(gd_learned* N, cudaStream_t st) {
     GD_TRY(conv_launch(1, 8, N->L[l], N->f[l].p, P + N->offG[l], nullptr, P + N->offB[l], N->s[l].p, 0, 0, st));
     k_sigmoid<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC * N->nl[l], N->s[l].p);
   }
-  k_dsqrt_lattice<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, dinv, N->dsq.p);
+  k_dsqrt_lattice<<<nb_for(N->nlf), kLT, 0, st>>>(N->nlf, A->mx.node_gid.p, dinv, N->dsq.p);
   GD_CUDA_TRY(cudaGetLastError());
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   dfreeb(dn);
@@ -818,13 +868,28 @@ static int net_encoder_backward(gd_learned* N, int p, int q, cudaStream_t st) {
 }
 
 // z = D^-1 r + D^-1/2 S^T S D^-1/2 r  (r, z in gid order); keeps the path-0 encoder cache
+// network input of path p from a gid-order vector v: x_0 = (R) D^-1/2 v
+static int net_input(gd_learned* N, int p, const float* v, cudaStream_t st) {
+  gd_asm* A = N->A;
+  float* fine = N->cs ? N->xf.p : N->x[p][0].p;
+  k_to_lattice_scaled<<<nb_for(N->nlf), kLT, 0, st>>>(N->nlf, A->mx.node_gid.p, v, N->dsq.p, fine);
+  if (N->cs) k_restrict<<<nb_for(N->nl[0]), kLT, 0, st>>>(1, N->LF, N->L[0], N->xf.p, N->x[p][0].p, 1.f);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
 static int net_forward(gd_learned* N, const float* r, float* z, cudaStream_t st) {
   gd_asm* A = N->A;
   const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
-  k_to_lattice_scaled<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, r, N->dsq.p, N->x[0][0].p);
+  GD_TRY(net_input(N, 0, r, st));
   GD_TRY(net_encode(N, 0, st));
   GD_TRY(net_decode(N, 0, st));
-  k_learned_out<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, dinv, r, N->dsq.p, N->zl.p, z);
+  const float* zo = N->zl.p;
+  if (N->cs) {   // R^T = P / 8
+    k_prolong<<<nb_for(N->nlf), kLT, 0, st>>>(1, N->L[0], N->LF, N->zl.p, N->zf.p, 0.125f, 0);
+    zo = N->zf.p;
+  }
+  k_learned_out<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, dinv, r, N->dsq.p, zo, z);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
@@ -832,8 +897,9 @@ static int net_forward(gd_learned* N, const float* r, float* z, cudaStream_t st)
 // parameter gradient of <gz, z(r)> (gz = dL/dz in gid order), accumulated into grads
 static int net_backward(gd_learned* N, const float* gz, cudaStream_t st) {
   gd_asm* A = N->A;
-  // path 1 input: D^-1/2 gz on the lattice
-  k_to_lattice_scaled<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->nl[0], A->mx.node_gid.p, gz, N->dsq.p, N->x[1][0].p);
+  // path 1 input: (R) D^-1/2 gz
+  (void)A;
+  GD_TRY(net_input(N, 1, gz, st));
   GD_TRY(net_encode(N, 1, st));
   // d<g, S^T S x> = <S g, dS x> + <S x, dS g>
   GD_TRY(net_encoder_backward(N, 0, 1, st));
@@ -871,11 +937,11 @@ constexpr int64_t kDirectConvVoxels = 60000;
 // threads per tile, so a level of ~10^5 voxels still fills the SMs
 constexpr int64_t kWideTileVoxels = 400000;
 
-template <int LD, int EP>
-static int direct_launch(const Dims& d, const float* in, const float* in_gate, const float* W, int adjoint,
+template <int CI, int LD, int EP>
+static int direct_launch(const Dims& d, const float* in, const float* in_gate, const float* W, int adjoint, int co_n,
                          const float* out_gate, float* out, cudaStream_t st) {
-  TConvArgsS a{d, in, in_gate, W, adjoint, kC, out_gate, out};
-  k_conv_direct<kC, LD, EP><<<nb_for(kC * d.size()), kLT, 0, st>>>(a);
+  TConvArgsS a{d, in, in_gate, W, adjoint, co_n, out_gate, out};
+  k_conv_direct<CI, LD, EP><<<nb_for(co_n * d.size()), kLT, 0, st>>>(a);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
@@ -892,140 +958,135 @@ static int tconv_launch(const TConvArgs& a, cudaStream_t st) {
   return GD_OK;
 }
 
-// z = D^-1 r + D^-1/2 S^T S D^-1/2 r for the solver (no training caches): tiled
-// convolutions with the gates, the gather of r and the output fused in; 4L - 1 launches.
-static int net_apply_fast(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+// encoder convolution of level l with gates: out = conv(in; W_l) * s_l (CI input channels,
+// 8 outputs); direct for coarse levels, tiles otherwise
+template <int CI>
+static int enc_conv(gd_learned* N, int l, const float* in, cudaStream_t st) {
+  TConvArgs t{};
+  t.d = N->L[l];
+  t.in = in;
+  t.W = N->params.p + N->offW[l];
+  t.adjoint = 0;
+  t.out_gate = N->s[l].p;
+  t.out = N->h[0][l].p;
+  if (N->nl[l] < kDirectConvVoxels)
+    return direct_launch<CI, LD_PLAIN, EP_GATE>(t.d, in, nullptr, t.W, 0, kC, t.out_gate, t.out, st);
+  if (CI == kC && N->nl[l] < kWideTileVoxels) return tconv_launch<CI, kC, 2, 4, LD_PLAIN, EP_GATE>(t, st);
+  return tconv_launch<CI, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st);
+}
+
+// decoder (adjoint) convolution of level l into CO outputs: in (8 channels, times the gates
+// when LD == LD_GATED)
+template <int CO, int LD>
+static int dec_conv(gd_learned* N, int l, const float* in, const float* in_gate, float* out, cudaStream_t st) {
+  TConvArgs t{};
+  t.d = N->L[l];
+  t.in = in;
+  t.in_gate = in_gate;
+  t.W = N->params.p + N->offW[l];
+  t.adjoint = 1;
+  t.out = out;
+  if (N->nl[l] < kDirectConvVoxels)
+    return direct_launch<kC, LD, EP_PLAIN>(t.d, in, in_gate, t.W, 1, CO, nullptr, out, st);
+  if (CO == kC && N->nl[l] < kWideTileVoxels) return tconv_launch<kC, CO, 2, 4, LD, EP_PLAIN>(t, st);
+  return tconv_launch<kC, CO, 4, 4, LD, EP_PLAIN>(t, st);
+}
+
+// z = D^-1 r + D^-1/2 (R^T) S^T S (R) D^-1/2 r for the solver (no training caches).
+// `lattice`: r and z on the node lattice (0 on Dirichlet nodes), else in gid order.  On
+// the full lattice the gather/scale of r and the output are fused into the level-0
+// convolutions; with the coarse start they are fused into the restriction and the
+// final prolongation instead.
+static int net_apply(gd_learned* N, const float* r, float* z, bool lattice, cudaStream_t st) {
   gd_asm* A = N->A;
   const float* P = N->params.p;
-  const float* dinv = A->mx.f32.p + 5 * A->ngdofs;
   const int Lv = N->levels;
-  TConvArgs t{};
-  t.node_gid = A->mx.node_gid.p;
-  t.r = r;
-  t.dinv = dinv;
-  t.z = z;
+  const float* dinv = lattice ? lattice_dinv(A) : A->mx.f32.p + 5 * A->ngdofs;
   // encoder
   for (int l = 0; l < Lv; ++l) {
-    t.d = N->L[l];
-    t.W = P + N->offW[l];
-    t.adjoint = 0;
-    t.out_gate = N->s[l].p;
-    t.out = N->h[0][l].p;
-    if (l == 0) {
-      t.in = nullptr;
-      GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATHER, EP_GATE>(t, st)));
-    } else {
+    if (l > 0) {
       k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
-      t.in = N->x[0][l].p;
-      if (N->nl[l] < kDirectConvVoxels)
-        GD_TRY((direct_launch<LD_PLAIN, EP_GATE>(t.d, t.in, nullptr, t.W, 0, t.out_gate, t.out, st)));
-      else if (N->nl[l] < kWideTileVoxels)
-        GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_GATE>(t, st)));
-      else
-        GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
+      GD_TRY((enc_conv<kC>(N, l, N->x[0][l].p, st)));
+    } else if (N->cs) {
+      if (lattice) {
+        k_scale_restrict<<<nb_for(N->nl[0]), kLT, 0, st>>>(N->LF, N->L[0], r, N->dsq.p, N->x[0][0].p);
+      } else {
+        k_to_lattice_scaled<<<nb_for(N->nlf), kLT, 0, st>>>(N->nlf, A->mx.node_gid.p, r, N->dsq.p, N->xf.p);
+        k_restrict<<<nb_for(N->nl[0]), kLT, 0, st>>>(1, N->LF, N->L[0], N->xf.p, N->x[0][0].p, 1.f);
+      }
+      GD_CUDA_TRY(cudaGetLastError());
+      GD_TRY((enc_conv<1>(N, 0, N->x[0][0].p, st)));
+    } else {
+      TConvArgs t{};
+      t.d = N->L[0];
+      t.W = P + N->offW[0];
+      t.out_gate = N->s[0].p;
+      t.out = N->h[0][0].p;
+      t.r = r;
+      t.dinv = dinv;
+      t.node_gid = A->mx.node_gid.p;
+      if (lattice) {
+        t.in = r;
+        t.in_gate = N->dsq.p;
+        GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATED, EP_GATE>(t, st)));
+      } else {
+        GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATHER, EP_GATE>(t, st)));
+      }
     }
   }
   // decoder (adjoint convolutions)
   for (int l = Lv - 1; l >= 0; --l) {
-    t.d = N->L[l];
-    t.W = P + N->offW[l];
-    t.adjoint = 1;
-    t.out_gate = nullptr;
-    t.out = N->gx[l].p;
-    int ld = LD_PLAIN;
-    if (l == Lv - 1) {
-      t.in = N->h[0][l].p;
-      t.in_gate = N->s[l].p;
-      ld = LD_GATED;
-    } else {
+    const bool top = l == Lv - 1;
+    const float* in = top ? N->h[0][l].p : N->da[l].p;
+    const float* gate = top ? N->s[l].p : nullptr;
+    if (!top) {
       k_prolong_gate<<<nb_for(N->nl[l]), kLT, 0, st>>>(N->L[l + 1], N->L[l], N->gx[l + 1].p, N->h[0][l].p,
                                                        N->s[l].p, 0.125f, N->da[l].p);
       GD_CUDA_TRY(cudaGetLastError());
-      t.in = N->da[l].p;
-      t.in_gate = nullptr;
     }
-    if (l == 0) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUT>(t, st)));
-      else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUT>(t, st)));
-    } else if (N->nl[l] < kDirectConvVoxels) {
-      if (ld == LD_GATED) GD_TRY((direct_launch<LD_GATED, EP_PLAIN>(t.d, t.in, t.in_gate, t.W, 1, nullptr, t.out, st)));
-      else GD_TRY((direct_launch<LD_PLAIN, EP_PLAIN>(t.d, t.in, nullptr, t.W, 1, nullptr, t.out, st)));
-    } else if (N->nl[l] < kWideTileVoxels) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 2, 4, LD_GATED, EP_PLAIN>(t, st)));
-      else GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_PLAIN>(t, st)));
+    if (l > 0) {
+      if (top) GD_TRY((dec_conv<kC, LD_GATED>(N, l, in, gate, N->gx[l].p, st)));
+      else GD_TRY((dec_conv<kC, LD_PLAIN>(N, l, in, gate, N->gx[l].p, st)));
+    } else if (N->cs) {
+      if (top) GD_TRY((dec_conv<1, LD_GATED>(N, 0, in, gate, N->zl.p, st)));
+      else GD_TRY((dec_conv<1, LD_PLAIN>(N, 0, in, gate, N->zl.p, st)));
+      if (lattice) {
+        k_prolong_out_lattice<<<nb_for(N->nlf), kLT, 0, st>>>(N->L[0], N->LF, N->zl.p, r, dinv, N->dsq.p, z);
+      } else {
+        k_prolong<<<nb_for(N->nlf), kLT, 0, st>>>(1, N->L[0], N->LF, N->zl.p, N->zf.p, 0.125f, 0);
+        k_learned_out<<<nb_for(A->ngdofs), kLT, 0, st>>>(A->ngdofs, A->row_node.p, dinv, r, N->dsq.p, N->zf.p, z);
+      }
+      GD_CUDA_TRY(cudaGetLastError());
     } else {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
-      else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
+      TConvArgs t{};
+      t.d = N->L[0];
+      t.in = in;
+      t.in_gate = gate;
+      t.W = P + N->offW[0];
+      t.adjoint = 1;
+      t.r = r;
+      t.dinv = dinv;
+      t.dsq = N->dsq.p;
+      t.node_gid = A->mx.node_gid.p;
+      t.z = z;
+      if (lattice) {
+        if (top) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUTLAT>(t, st)));
+        else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUTLAT>(t, st)));
+      } else {
+        if (top) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUT>(t, st)));
+        else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUT>(t, st)));
+      }
     }
   }
   return GD_OK;
 }
 
-// the same map with r and z on the node lattice (0 on Dirichlet nodes)
+static int net_apply_fast(gd_learned* N, const float* r, float* z, cudaStream_t st) {
+  return net_apply(N, r, z, false, st);
+}
+
 static int net_apply_lattice(gd_learned* N, const float* r, float* z, cudaStream_t st) {
-  gd_asm* A = N->A;
-  const float* P = N->params.p;
-  const int Lv = N->levels;
-  TConvArgs t{};
-  t.r = r;
-  t.dinv = lattice_dinv(A);
-  t.dsq = N->dsq.p;
-  t.z = z;
-  for (int l = 0; l < Lv; ++l) {
-    t.d = N->L[l];
-    t.W = P + N->offW[l];
-    t.adjoint = 0;
-    t.out_gate = N->s[l].p;
-    t.out = N->h[0][l].p;
-    if (l == 0) {
-      t.in = r;
-      t.in_gate = N->dsq.p;
-      GD_TRY((tconv_launch<1, kC, 4, 4, LD_GATED, EP_GATE>(t, st)));
-    } else {
-      k_restrict<<<nb_for(kC * N->nl[l]), kLT, 0, st>>>(kC, N->L[l - 1], N->L[l], N->h[0][l - 1].p, N->x[0][l].p, 1.f);
-      t.in = N->x[0][l].p;
-      t.in_gate = nullptr;
-      if (N->nl[l] < kDirectConvVoxels)
-        GD_TRY((direct_launch<LD_PLAIN, EP_GATE>(t.d, t.in, nullptr, t.W, 0, t.out_gate, t.out, st)));
-      else if (N->nl[l] < kWideTileVoxels)
-        GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_GATE>(t, st)));
-      else
-        GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_GATE>(t, st)));
-    }
-  }
-  for (int l = Lv - 1; l >= 0; --l) {
-    t.d = N->L[l];
-    t.W = P + N->offW[l];
-    t.adjoint = 1;
-    t.out_gate = nullptr;
-    t.out = N->gx[l].p;
-    int ld = LD_PLAIN;
-    if (l == Lv - 1) {
-      t.in = N->h[0][l].p;
-      t.in_gate = N->s[l].p;
-      ld = LD_GATED;
-    } else {
-      k_prolong_gate<<<nb_for(N->nl[l]), kLT, 0, st>>>(N->L[l + 1], N->L[l], N->gx[l + 1].p, N->h[0][l].p,
-                                                       N->s[l].p, 0.125f, N->da[l].p);
-      GD_CUDA_TRY(cudaGetLastError());
-      t.in = N->da[l].p;
-      t.in_gate = nullptr;
-    }
-    if (l == 0) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, 1, 4, 4, LD_GATED, EP_OUTLAT>(t, st)));
-      else GD_TRY((tconv_launch<kC, 1, 4, 4, LD_PLAIN, EP_OUTLAT>(t, st)));
-    } else if (N->nl[l] < kDirectConvVoxels) {
-      if (ld == LD_GATED) GD_TRY((direct_launch<LD_GATED, EP_PLAIN>(t.d, t.in, t.in_gate, t.W, 1, nullptr, t.out, st)));
-      else GD_TRY((direct_launch<LD_PLAIN, EP_PLAIN>(t.d, t.in, nullptr, t.W, 1, nullptr, t.out, st)));
-    } else if (N->nl[l] < kWideTileVoxels) {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 2, 4, LD_GATED, EP_PLAIN>(t, st)));
-      else GD_TRY((tconv_launch<kC, kC, 2, 4, LD_PLAIN, EP_PLAIN>(t, st)));
-    } else {
-      if (ld == LD_GATED) GD_TRY((tconv_launch<kC, kC, 4, 4, LD_GATED, EP_PLAIN>(t, st)));
-      else GD_TRY((tconv_launch<kC, kC, 4, 4, LD_PLAIN, EP_PLAIN>(t, st)));
-    }
-  }
-  return GD_OK;
+  return net_apply(N, r, z, true, st);
 }
 
 static int apply_as_precond(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st) {
@@ -1043,9 +1104,10 @@ static int apply_as_precond_lattice(void* ctx, gd_asm* A, const float* r, float*
 // ---------------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------------
-extern "C" int gd_learned_create(gd_asm* A, int levels, uint64_t seed, gd_learned** out) {
+extern "C" int gd_learned_create(gd_asm* A, int levels, int flags, uint64_t seed, gd_learned** out) {
   if (!A || !out) return fail(GD_ERR_ARG, "gd_learned_create: null argument");
   if (levels < 1 || levels > kMaxLevels) return fail(GD_ERR_ARG, "gd_learned_create: levels must be 1..6");
+  if (flags & ~GD_LEARNED_COARSE_START) return fail(GD_ERR_ARG, "gd_learned_create: unknown flags");
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_learned_create: assemble the system first");
   if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3))
     return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells");
@@ -1055,7 +1117,10 @@ extern "C" int gd_learned_create(gd_asm* A, int levels, uint64_t seed, gd_learne
   gd_learned* N = new gd_learned();
   N->A = A;
   N->levels = levels;
-  for (int d = 0; d < 3; ++d) N->L[0].n[d] = (int)g.N[d];
+  N->cs = (flags & GD_LEARNED_COARSE_START) ? 1 : 0;
+  for (int d = 0; d < 3; ++d) N->LF.n[d] = (int)g.N[d];
+  N->nlf = N->LF.size();
+  N->L[0] = N->cs ? coarse_dims(N->LF) : N->LF;
   for (int l = 1; l < levels; ++l) N->L[l] = coarse_dims(N->L[l - 1]);
   for (int l = 0; l < levels; ++l) N->nl[l] = N->L[l].size();
   int off = 0;
@@ -1084,8 +1149,12 @@ extern "C" int gd_learned_create(gd_asm* A, int levels, uint64_t seed, gd_learne
   ALLOC(N->grads, N->nparams);
   ALLOC(N->adam_m, N->nparams);
   ALLOC(N->adam_v, N->nparams);
-  ALLOC(N->dsq, N->nl[0]);
+  ALLOC(N->dsq, N->nlf);
   ALLOC(N->zl, N->nl[0]);
+  if (N->cs) {
+    ALLOC(N->xf, N->nlf);
+    ALLOC(N->zf, N->nlf);
+  }
   for (int l = 0; l < levels; ++l) {
     ALLOC(N->f[l], N->nl[l]);
     ALLOC(N->s[l], kC * N->nl[l]);
@@ -1140,6 +1209,8 @@ extern "C" int gd_learned_destroy(gd_learned* N) {
   dfreeb(N->adam_v);
   dfreeb(N->dsq);
   dfreeb(N->zl);
+  dfreeb(N->xf);
+  dfreeb(N->zf);
   for (int l = 0; l < kMaxLevels; ++l) {
     dfreeb(N->f[l]);
     dfreeb(N->s[l]);
@@ -1173,6 +1244,12 @@ extern "C" int gd_learned_num_params(const gd_learned* N, int64_t* n) {
 extern "C" int gd_learned_levels(const gd_learned* N, int32_t* levels) {
   if (!N || !levels) return fail(GD_ERR_ARG, "gd_learned_levels: null argument");
   *levels = N->levels;
+  return GD_OK;
+}
+
+extern "C" int gd_learned_flags(const gd_learned* N, int32_t* flags) {
+  if (!N || !flags) return fail(GD_ERR_ARG, "gd_learned_flags: null argument");
+  *flags = N->cs ? GD_LEARNED_COARSE_START : 0;
   return GD_OK;
 }
 

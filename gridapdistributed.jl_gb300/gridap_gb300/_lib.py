@@ -104,8 +104,9 @@ SIGNATURES = {
     "gd_batch_tuning": [P, I32P, I32P, I32P, C.POINTER(C.c_float), I32P],
     "gd_batch_solve": [P, C.c_double, C.c_int, P],
     "gd_batch_solution": [P, C.c_int, P, C.c_int],
-    "gd_learned_create": [P, C.c_int, C.c_uint64, PP],
+    "gd_learned_create": [P, C.c_int, C.c_int, C.c_uint64, PP],
     "gd_learned_levels": [P, I32P],
+    "gd_learned_flags": [P, I32P],
     "gd_learned_destroy": [P],
     "gd_learned_num_params": [P, I64P],
     "gd_learned_get_params": [P, C.POINTER(C.c_float)],

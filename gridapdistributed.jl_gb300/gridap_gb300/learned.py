@@ -22,7 +22,10 @@ import numpy as np
 from . import _lib as L
 
 MAGIC = b"GDLP"
-FORMAT_VERSION = 2   # header: magic, version, levels, parameter count, CRC32 of the float32 payload
+# header: magic, version, levels, flags, parameter count, CRC32 of the float32 payload
+# (version 2 files have no flags word: flags 0)
+FORMAT_VERSION = 3
+COARSE_START = 1   # gd_learned flag: network on the once-restricted lattice
 
 
 def _torch():
@@ -32,14 +35,17 @@ def _torch():
 
 class LearnedPreconditioner:
     """The L-level (default 3), 8-channel network bound to one assembler (one problem
-    size), applied as z = D^-1 r + D^-1/2 S^T S D^-1/2 r (symmetric positive definite)."""
+    size), applied as z = D^-1 r + D^-1/2 S^T S D^-1/2 r (symmetric positive definite);
+    with coarse_start the network runs on the once-restricted lattice,
+    z = D^-1 r + D^-1/2 R^T S^T S R D^-1/2 r."""
 
-    def __init__(self, matrix, seed: int = 0, levels: int = 3):
+    def __init__(self, matrix, seed: int = 0, levels: int = 3, coarse_start: bool = False):
         self.matrix = matrix
         self.assem = matrix.assem
         self.levels = int(levels)
+        self.flags = COARSE_START if coarse_start else 0
         h = C.c_void_p()
-        L.call("gd_learned_create", self.assem.handle, self.levels, C.c_uint64(seed), C.byref(h))
+        L.call("gd_learned_create", self.assem.handle, self.levels, self.flags, C.c_uint64(seed), C.byref(h))
         self.handle = h
         n = C.c_int64()
         L.call("gd_learned_num_params", self.handle, C.byref(n))
@@ -58,35 +64,43 @@ class LearnedPreconditioner:
         L.call("gd_learned_set_params", self.handle, p.ctypes.data_as(C.POINTER(C.c_float)))
 
     def save(self, path):
-        """Versioned little-endian file: magic, format version, levels, parameter count,
-        CRC32, float32 params.  The parameters do not depend on the mesh size."""
+        """Versioned little-endian file: magic, format version, levels, flags, parameter
+        count, CRC32, float32 params.  The parameters do not depend on the mesh size."""
         p = self.get_params()
         blob = p.tobytes()
-        Path(path).write_bytes(MAGIC + struct.pack("<IIII", FORMAT_VERSION, self.levels, p.size, zlib.crc32(blob))
-                               + blob)
+        Path(path).write_bytes(MAGIC + struct.pack("<IIIII", FORMAT_VERSION, self.levels, self.flags, p.size,
+                                                   zlib.crc32(blob)) + blob)
 
     @staticmethod
-    def file_levels(path) -> int:
-        """Number of levels stored in a parameter file (for constructing a matching net)."""
-        data = Path(path).read_bytes()[:20]
-        if data[:4] != MAGIC:
-            raise ValueError(f"{path}: not a learned-preconditioner file")
-        version, levels = struct.unpack("<II", data[4:12])
-        if version != FORMAT_VERSION:
-            raise ValueError(f"{path}: format version {version}, expected {FORMAT_VERSION}")
-        return levels
-
-    def load(self, path):
-        data = Path(path).read_bytes()
+    def _header(data, path):
         if data[:4] != MAGIC:
             raise ValueError(f"{path}: not a learned-preconditioner file")
         version, = struct.unpack("<I", data[4:8])
+        if version == 2:
+            levels, count, crc = struct.unpack("<III", data[8:20])
+            return levels, 0, count, crc, 20
         if version != FORMAT_VERSION:
             raise ValueError(f"{path}: format version {version}, expected {FORMAT_VERSION}")
-        levels, count, crc = struct.unpack("<III", data[8:20])
-        if levels != self.levels:
-            raise ValueError(f"{path}: {levels}-level network, this one has {self.levels}")
-        blob = data[20:]
+        levels, flags, count, crc = struct.unpack("<IIII", data[8:24])
+        return levels, flags, count, crc, 24
+
+    @staticmethod
+    def file_spec(path):
+        """(levels, coarse_start) stored in a parameter file, to construct a matching net."""
+        levels, flags, _, _, _ = LearnedPreconditioner._header(Path(path).read_bytes()[:24], path)
+        return levels, bool(flags & COARSE_START)
+
+    @staticmethod
+    def file_levels(path) -> int:
+        return LearnedPreconditioner.file_spec(path)[0]
+
+    def load(self, path):
+        data = Path(path).read_bytes()
+        levels, flags, count, crc, start = self._header(data, path)
+        if levels != self.levels or flags != self.flags:
+            raise ValueError(f"{path}: network ({levels} levels, flags {flags}) differs from this one "
+                             f"({self.levels} levels, flags {self.flags})")
+        blob = data[start:]
         if count != self.num_params or len(blob) != 4 * count or zlib.crc32(blob) != crc:
             raise ValueError(f"{path}: parameter count or checksum mismatch")
         self.set_params(np.frombuffer(blob, dtype=np.float32))

@@ -31,6 +31,7 @@ def main(argv=None):
     ap.add_argument("--epochs", type=int, default=8)
     ap.add_argument("--lr", type=float, default=2e-3)
     ap.add_argument("--levels", type=int, default=3)
+    ap.add_argument("--coarse-start", action="store_true", help="network on the once-restricted lattice")
     ap.add_argument("--eval-fields", type=int, default=3)
     ap.add_argument("--init", default=None, help="start from a saved parameter file")
     ap.add_argument("--out", default="learned.gdlp")
@@ -55,8 +56,8 @@ def main(argv=None):
     kap0 = field(1)
     f0 = rng.standard_normal(nnodes)
     op = G.AffineFEOperator(G.integral_grad_grad(kap0, dO), G.integral_source(f0, dO), U, V)
-    levels = LearnedPreconditioner.file_levels(a.init) if a.init else a.levels
-    net = LearnedPreconditioner(op.matrix, seed=3, levels=levels)
+    levels, cs = LearnedPreconditioner.file_spec(a.init) if a.init else (a.levels, a.coarse_start)
+    net = LearnedPreconditioner(op.matrix, seed=3, levels=levels, coarse_start=cs)
     if a.init:
         net.load(a.init)
 
@@ -111,7 +112,7 @@ def main(argv=None):
         evals.append({"jacobi_s": tj, "jacobi_iters": itj, "learned_s": tl, "learned_iters": st.iterations,
                       "learned_rel_residual": st.rel_residual, "fallback": fb, "speedup": tj / tl,
                       "max_rel_diff": float(np.abs(xl - xj).max() / np.abs(xj).max())})
-    print(json.dumps({"levels": levels, "params": net.num_params, "pairs": sum(len(d[1]) for d in data), "fields": len(data), "t_pairs_s": t_pairs,
+    print(json.dumps({"levels": levels, "coarse_start": cs, "params": net.num_params, "pairs": sum(len(d[1]) for d in data), "fields": len(data), "t_pairs_s": t_pairs,
                       "t_train_s": t_train, "loss_per_epoch": hist, "eval": evals}), flush=True)
     net.close()
     be.close()

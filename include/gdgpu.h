@@ -290,8 +290,12 @@ int gd_batch_solution(const gd_batch* b, int p, double* x, int where);
  * preconditioner of the mixed-precision flexible CG.
  * Vectors r, e, z are FP32 device arrays over the owned DOFs in gid order. */
 typedef struct gd_learned gd_learned;
-int gd_learned_create(gd_asm* a, int levels, uint64_t seed, gd_learned** out);
+/* flags: GD_LEARNED_COARSE_START runs the network on the once-restricted lattice,
+ * z = D^-1 r + D^-1/2 R^T S^T S R D^-1/2 r (R full-weighting restriction). */
+enum { GD_LEARNED_COARSE_START = 1 };
+int gd_learned_create(gd_asm* a, int levels, int flags, uint64_t seed, gd_learned** out);
 int gd_learned_levels(const gd_learned* net, int32_t* levels);
+int gd_learned_flags(const gd_learned* net, int32_t* flags);
 int gd_learned_destroy(gd_learned* net);
 int gd_learned_num_params(const gd_learned* net, int64_t* n);
 int gd_learned_get_params(const gd_learned* net, float* host_params);

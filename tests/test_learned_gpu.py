@@ -53,11 +53,13 @@ def global_matrix(op):
     return sps.csr_matrix((np.concatenate(vals), (np.concatenate(rows), np.concatenate(cols))), shape=(n, n))
 
 
-def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, levels):
+def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, levels, coarse_start=False):
     """The same network in float64 PyTorch on the CPU; returns z (gid order).
 
     S^T S x is taken as the gradient of 0.5 |S x|^2 (autograd), an independent route to
-    the decoder that the device computes as the explicit adjoint of the encoder."""
+    the decoder that the device computes as the explicit adjoint of the encoder; with
+    coarse_start the restriction R sits inside the autograd graph, so R^T is its exact
+    adjoint (the device uses P / 8)."""
     N = [c + 1 for c in cells]
     nlat = int(np.prod(N))
     off = 0
@@ -84,20 +86,23 @@ def torch_net(params, kappa_cells, cells, r_gid, node_of_gid, dinv, levels):
         c = x.shape[1]
         return F.conv3d(x, Rw.repeat(c, 1, 1, 1, 1), stride=2, padding=1, groups=c)
 
+    if coarse_start:
+        f = [R(f[0])]
     for _ in range(1, levels):
         f.append(R(f[-1]))
     s = [torch.sigmoid(F.conv3d(f[l], G[l], bias=Bs[l], padding=1)) for l in range(levels)]
     dsq = torch.sqrt(dinv)
-    x0 = torch.zeros(nlat, dtype=torch.float64)
-    x0[node_of_gid] = dsq * r_gid
-    x0 = x0.reshape(1, 1, N[2], N[1], N[0]).requires_grad_(True)
+    xf = torch.zeros(nlat, dtype=torch.float64)
+    xf[node_of_gid] = dsq * r_gid
+    xf = xf.reshape(1, 1, N[2], N[1], N[0]).requires_grad_(True)
+    x0 = R(xf) if coarse_start else xf
     hs, x = [], x0
     for l in range(levels):
         if l > 0:
             x = R(hs[-1])
         hs.append(F.conv3d(x, W[l], padding=1) * s[l])
     q = 0.5 * sum((h * h).sum() for h in hs)
-    y, = torch.autograd.grad(q, x0, create_graph=True)
+    y, = torch.autograd.grad(q, xf, create_graph=True)
     return dinv * r_gid + dsq * y.reshape(-1)[node_of_gid]
 
 
@@ -108,14 +113,14 @@ def small_system(be, seed=41):
     return pb, V, op, A
 
 
-@pytest.mark.parametrize("levels", [1, 3, 4])
-def test_network_gradient_matches_pytorch(levels):
+@pytest.mark.parametrize("levels,cs", [(1, False), (3, False), (4, False), (1, True), (3, True)])
+def test_network_gradient_matches_pytorch(levels, cs):
     import gridap_gb300 as G
     from gridap_gb300.learned import LearnedPreconditioner
     be = G.GB300Backend(0)
     try:
         pb, V, op, A = small_system(be)
-        net = LearnedPreconditioner(op.matrix, seed=7, levels=levels)
+        net = LearnedPreconditioner(op.matrix, seed=7, levels=levels, coarse_start=cs)
         assert net.num_params == C8 * TAPS + (levels - 1) * C8 * C8 * TAPS + levels * (C8 * TAPS + C8)
         n = V.num_free_dofs()
         rng = np.random.default_rng(5)
@@ -130,7 +135,8 @@ def test_network_gradient_matches_pytorch(levels):
         params = torch.tensor(net.get_params().astype(np.float64), requires_grad=True)
         total = 0.0
         for b in range(2):
-            z = torch_net(params, pb.kappa, pb.n, torch.tensor(r[b], dtype=torch.float64), node_of_gid, dinv, levels)
+            z = torch_net(params, pb.kappa, pb.n, torch.tensor(r[b], dtype=torch.float64), node_of_gid, dinv, levels,
+                          cs)
             if b == 0:
                 assert np.abs(z.detach().numpy() - z_gpu).max() <= 1e-4 * np.abs(z_gpu).max()
             ev = torch.tensor(e[b], dtype=torch.float64)
@@ -147,7 +153,8 @@ def test_network_gradient_matches_pytorch(levels):
         be.close()
 
 
-def test_network_is_symmetric_positive_definite():
+@pytest.mark.parametrize("cs", [False, True])
+def test_network_is_symmetric_positive_definite(cs):
     """<r1, M r2> = <M r1, r2> and <r, M r> > 0 for the device network, also with
     parameters far from the initial ones."""
     import gridap_gb300 as G
@@ -155,7 +162,7 @@ def test_network_is_symmetric_positive_definite():
     be = G.GB300Backend(0)
     try:
         pb, V, op, A = small_system(be, seed=43)
-        net = LearnedPreconditioner(op.matrix, seed=11, levels=3)
+        net = LearnedPreconditioner(op.matrix, seed=11, levels=3, coarse_start=cs)
         rng = np.random.default_rng(9)
         net.set_params(rng.standard_normal(net.num_params).astype(np.float32) * 0.5)
         n = V.num_free_dofs()
@@ -172,8 +179,8 @@ def test_network_is_symmetric_positive_definite():
         be.close()
 
 
-@pytest.mark.parametrize("levels", [1, 2, 3, 4])
-def test_tiled_application_matches_training_kernels(levels):
+@pytest.mark.parametrize("levels,cs", [(1, False), (2, False), (3, False), (4, False), (1, True), (3, True)])
+def test_tiled_application_matches_training_kernels(levels, cs):
     """The solver's tiled application (fused gather, gates and output) against the
     training kernels on a lattice with partial tiles in every direction, with
     parameters large enough that the learned term dominates D^-1 r."""
@@ -185,7 +192,7 @@ def test_tiled_application_matches_training_kernels(levels):
     try:
         pb = make_problem(3, (24, 16, 20), (2, 2, 1), 1, seed=47, domain=(0.0, 1.5, 0.0, 1.0, 0.0, 1.25))
         model, V, op = build(be, pb)
-        net = LearnedPreconditioner(op.matrix, seed=13, levels=levels)
+        net = LearnedPreconditioner(op.matrix, seed=13, levels=levels, coarse_start=cs)
         rng = np.random.default_rng(21)
         net.set_params(rng.standard_normal(net.num_params).astype(np.float32) * 0.3)
         n = V.num_free_dofs()
