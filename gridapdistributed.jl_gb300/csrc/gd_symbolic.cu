@@ -621,6 +621,7 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->mx.zold);
   dfreeb(A->mx.lat);
   dfreeb(A->mx.latred);
+  dfreeb(A->mx.plat);
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;

@@ -63,7 +63,8 @@ CASES = [
 
 
 def case_id(c):
-    return f"{c['dim']}d_n{'x'.join(map(str, c['n']))}_p{''.join(map(str, c['parts']))}_q{c['order']}"
+    cube = "_cube" if "domain" in c else ""
+    return f"{c['dim']}d_n{'x'.join(map(str, c['n']))}_p{''.join(map(str, c['parts']))}_q{c['order']}{cube}"
 
 
 @pytest.mark.parametrize("strategy", ["sub", "full"])
@@ -112,7 +113,15 @@ def test_solve_matches_gathered_lu(backend, case):
 @pytest.mark.parametrize("case", [CASES[6], CASES[7], CASES[13],
                                   dict(dim=3, n=(12, 10, 8), parts=(2, 2, 2), order=1, seed=30),
                                   dict(dim=3, n=(9, 8, 7), parts=(2, 2, 1), order=1, seed=31,
-                                       sides=(1, 0, 1, 1, 0, 1))], ids=case_id)
+                                       sides=(1, 0, 1, 1, 0, 1)),
+                                  # cube cells (the lattice inner iteration): rows of 12 nodes (no
+                                  # padding), of 10 (warps start mid-row), of 141 (rows across warps)
+                                  dict(dim=3, n=(11, 7, 6), parts=(1, 2, 1), order=1, seed=32,
+                                       sides=(0, 1, 1, 0, 1, 1), domain=(0, 1.375, 0, 0.875, 0, 0.75)),
+                                  dict(dim=3, n=(9, 8, 7), parts=(2, 2, 1), order=1, seed=34,
+                                       sides=(1, 0, 1, 1, 0, 1), domain=(0, 1.125, 0, 1.0, 0, 0.875)),
+                                  dict(dim=3, n=(140, 4, 3), parts=(2, 1, 1), order=1, seed=33,
+                                       domain=(0, 17.5, 0, 0.5, 0, 0.375))], ids=case_id)
 def test_mixed_solver_matches_gathered_lu(backend, case):
     """FP64 refinement around FP32 CG (matrix-free on cube Q1, FP32 CSR otherwise)."""
     pb = make_problem(**case)
