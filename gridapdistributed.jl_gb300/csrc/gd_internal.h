@@ -178,7 +178,7 @@ struct MixedState {
   // lattice-order inner iteration (3D cube Q1): x r z0 z1 p0 p1 q dinv, node-lattice sized
   DBuf<float> lat;
   DBuf<double> latred;    // block partials, arrival counter and CG scalars
-  // persistent Jacobi-CG on the padded lattice: x r z p0 p1 q dinv w
+  // persistent Jacobi-CG on the padded lattice: x r z p q dinv w
   DBuf<float> plat;
   int64_t plat_epoch = -1;
   int64_t lat_epoch = -1;

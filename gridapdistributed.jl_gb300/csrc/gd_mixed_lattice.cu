@@ -577,11 +577,11 @@ __global__ void k_pad_setup(PadGeom pg, const float* __restrict__ dinvl, const f
   }
 }
 
-// r = r64[gid] * inv, x = 0, p = 0, z = D^-1 r on the padded lattice; sums r.z, r.r; beta = 0
+// r = r64[gid] * inv, x = p = q = 0, z = D^-1 r on the padded lattice; sums r.z, r.r; beta = 0
 __global__ void __launch_bounds__(kLatThreads)
 k_pad_start(PadGeom pg, const int32_t* __restrict__ node_gid, const double* __restrict__ r64, double inv,
             const float* __restrict__ dpad, float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
-            float* __restrict__ p, LatRed* R) {
+            float* __restrict__ p, float* __restrict__ q, LatRed* R) {
   const int N0 = pg.N[0], N1 = pg.N[1], N2 = pg.N[2];
   float a = 0.f, b = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < pg.L; i += gridDim.x * blockDim.x) {
@@ -597,6 +597,7 @@ k_pad_start(PadGeom pg, const int32_t* __restrict__ node_gid, const double* __re
     z[i] = zi;
     x[i] = 0.f;
     p[i] = 0.f;
+    q[i] = 0.f;
     a = fmaf(ri, zi, a);
     b = fmaf(ri, ri, b);
   }
@@ -623,18 +624,19 @@ __global__ void k_pad_accumulate(PadGeom pg, const int32_t* __restrict__ node_gi
   }
 }
 
-// The apply phase on the padded lattice: pn = z + beta po, q = A pn (21-point stencil,
-// the same coefficients as k_lat_apply), returns the thread's pn.q partial.  The block
-// owns the groups c0 .. c1-1 (group = 4 nodes of one row, rows in lattice order); lane l
-// of a warp takes group wb + l, so a warp's groups are consecutive and the
-// x-halo values X0 - 1 and X0 + 4 of a row come from the neighbouring lanes by shuffle
-// (lanes 0 and 31 load their outer halo themselves, in one instruction), and are 0 at the
-// ends of a row.  Per neighbour row and vector that is one float4 load instead of six
-// scalar loads at a 16-byte lane stride.  Loads of z and po are plain (coherent after a
-// grid barrier); the cell coefficients go through the read-only path.
+// The apply phase on the padded lattice.  With p_new = z + beta p, A p_new = A z + beta q
+// (q = A p from the previous step), so the stencil reads only z at the neighbours and p
+// and q are updated in place from the thread's own values:
+//   q <- A z + beta q,  p <- z + beta p,  returns the thread's p.q partial
+// (the 21-point stencil of k_lat_apply).  The block owns the groups c0 .. c1-1 (group =
+// 4 nodes of one row, rows in lattice order); lane l of a warp takes group wb + l, so a
+// warp's groups are consecutive and the x-halo values X0 - 1 and X0 + 4 of a row come
+// from the neighbouring lanes by shuffle (lanes 0 and 31 load their outer halo
+// themselves), and are 0 at the ends of a row.  Per neighbour row that is one float4
+// load instead of six scalar loads at a 16-byte lane stride.  Loads of z are plain
+// (coherent after a grid barrier); the cell coefficients go through the read-only path.
 __device__ __forceinline__ float pad_apply(const PadGeom& pg, const float* __restrict__ wpad, float ratio,
-                                           float beta, const float* z, const float* po, float* pn, float* q, int c0,
-                                           int c1) {
+                                           float beta, const float* z, float* p, float* q, int c0, int c1) {
   const unsigned full = 0xffffffffu;
   const int lane = threadIdx.x & 31;
   const int N0 = pg.N[0], N1 = pg.N[1], N2 = pg.N[2], P0 = pg.P0, R1 = pg.R1;
@@ -651,6 +653,9 @@ __device__ __forceinline__ float pad_apply(const PadGeom& pg, const float* __res
     const bool hl = X0 > 0, hr = X0 + 4 < P0;   // the row continues left / right of the group
     const bool fetch = (lane == 0 && hl) || (lane == 31 && hr);
     const int eo = lane == 0 ? -1 : 4;
+    const int ob = ((X2 + 1) * R1 + X1 + 1) * P0 + X0;
+    const float4 pold = *reinterpret_cast<const float4*>(p + ob);
+    const float4 qold = *reinterpret_cast<const float4*>(q + ob);
     // w[cz][cy][k]: cell (X0 - 1 + k, X1 - 1 + cy, X2 - 1 + cz)
     float w[2][2][5];
 #pragma unroll
@@ -677,15 +682,14 @@ __device__ __forceinline__ float pad_apply(const PadGeom& pg, const float* __res
         const int nyz = (o1 != 0) + (o2 != 0);
         const int nb = ((X2 + 1 + o2) * R1 + X1 + 1 + o1) * P0 + X0;
         const float4 z4 = *reinterpret_cast<const float4*>(z + nb);
-        const float4 p4 = *reinterpret_cast<const float4*>(po + nb);
         float v[6];
-        v[1] = fmaf(beta, p4.x, z4.x);
-        v[2] = fmaf(beta, p4.y, z4.y);
-        v[3] = fmaf(beta, p4.z, z4.z);
-        v[4] = fmaf(beta, p4.w, z4.w);
+        v[1] = z4.x;
+        v[2] = z4.y;
+        v[3] = z4.z;
+        v[4] = z4.w;
         v[0] = v[5] = 0.f;
         if (nyz != 0) {   // the centre row needs the own nodes only
-          const float ev = fetch ? fmaf(beta, po[nb + eo], z[nb + eo]) : 0.f;
+          const float ev = fetch ? z[nb + eo] : 0.f;
           float l = __shfl_up_sync(full, v[4], 1);
           float rt = __shfl_down_sync(full, v[1], 1);
           if (lane == 0) l = ev;
@@ -723,16 +727,18 @@ __device__ __forceinline__ float pad_apply(const PadGeom& pg, const float* __res
     if (valid) {
       const bool ydir = (pg.ds[2] && X1 == 0) || (pg.ds[3] && X1 == N1 - 1) || (pg.ds[4] && X2 == 0) ||
                         (pg.ds[5] && X2 == N2 - 1);
-      float qv[4];
+      const float po[4] = {pold.x, pold.y, pold.z, pold.w}, qo[4] = {qold.x, qold.y, qold.z, qold.w};
+      float pv[4], qv[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int X = X0 + j;
         const bool dir = ydir || (pg.ds[0] && X == 0) || (pg.ds[1] && X == N0 - 1);
-        qv[j] = dir ? 0.f : acc[j];   // 0 past the row end too (all coefficients there are 0)
-        dot = fmaf(own[j], qv[j], dot);
+        // A z is 0 on Dirichlet nodes and past the row end (all coefficients there are 0)
+        qv[j] = fmaf(beta, qo[j], dir ? 0.f : acc[j]);
+        pv[j] = fmaf(beta, po[j], own[j]);
+        dot = fmaf(pv[j], qv[j], dot);
       }
-      const int ob = ((X2 + 1) * R1 + X1 + 1) * P0 + X0;
-      *reinterpret_cast<float4*>(pn + ob) = make_float4(own[0], own[1], own[2], own[3]);
+      *reinterpret_cast<float4*>(p + ob) = make_float4(pv[0], pv[1], pv[2], pv[3]);
       *reinterpret_cast<float4*>(q + ob) = make_float4(qv[0], qv[1], qv[2], qv[3]);
     }
   }
@@ -777,13 +783,13 @@ __device__ __forceinline__ void pad_update(const PadGeom& pg, float alpha, float
 }
 
 // Jacobi-CG on the padded lattice from the state k_pad_start left (R->sc: rz, rr,
-// beta = 0; p0 = 0) until r.r <= tol2, r.r is not finite, or max_it steps; p ping-pongs
-// between p0 and p1.  Two fused barrier/all-reduces per step (p.q; r.z and r.r), so every
-// block holds the same alpha, beta and r.r and takes the same exit.  Block 0 writes the
-// step count and the final scalars.
+// beta = 0; p = q = 0) until r.r <= tol2, r.r is not finite, or max_it steps.  Two fused
+// barrier/all-reduces per step (p.q; r.z and r.r), so every block holds the same alpha,
+// beta and r.r and takes the same exit.  Block 0 writes the step count and the final
+// scalars.
 __global__ void __launch_bounds__(kLatThreads, kPadBlocksPerSM)
-k_pad_cg(PadGeom pg, const float* __restrict__ wpad, float ratio, float* x, float* r, float* z, float* p0, float* p1,
-         float* q, const float* __restrict__ dpad, LatRed* R, int max_it, double tol2) {
+k_pad_cg(PadGeom pg, const float* __restrict__ wpad, float ratio, float* x, float* r, float* z, float* p, float* q,
+         const float* __restrict__ dpad, LatRed* R, int max_it, double tol2) {
   const unsigned nb = gridDim.x;
   // equal contiguous chunks of groups, a multiple of 32 each (whole warps)
   const int ngroups = (pg.P0 >> 2) * pg.N[1] * pg.N[2];
@@ -792,22 +798,17 @@ k_pad_cg(PadGeom pg, const float* __restrict__ wpad, float ratio, float* x, floa
   // CG scalars in FP32 (the vectors are FP32; the grid sums are FP32 in a fixed order)
   float rz = (float)R->sc.rz, rr = (float)R->sc.rr, beta = (float)R->sc.beta, alpha = 0.f;
   const float tol2f = (float)tol2;
-  float* po = p0;
-  float* pn = p1;
   int it = 0;
   unsigned epoch = 0;   // grid barriers passed in this launch
   while (it < max_it && rr > tol2f && isfinite(rr)) {
     {
-      const float f[1] = {pad_apply(pg, wpad, ratio, beta, z, po, pn, q, c0, c1)};
+      const float f[1] = {pad_apply(pg, wpad, ratio, beta, z, p, q, c0, c1)};
       float pq[1];
       if (!lat_allreduce<1, 0>(R, f, nb, ++epoch, pq)) break;
       alpha = pq[0] != 0.f ? rz / pq[0] : 0.f;
     }
-    float* t = po;
-    po = pn;
-    pn = t;
     float f[2] = {0.f, 0.f};
-    pad_update(pg, alpha, x, r, z, po, q, dpad, c0, c1, f[0], f[1]);
+    pad_update(pg, alpha, x, r, z, p, q, dpad, c0, c1, f[0], f[1]);
     float s2[2];
     if (!lat_allreduce<2, 1>(R, f, nb, ++epoch, s2)) break;
     beta = rz != 0.f ? s2[0] / rz : 0.f;
@@ -953,12 +954,12 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
   const PadGeom pg = pad_fits(g) ? pad_geom(g) : PadGeom{};
   const int64_t pls = ((int64_t)pg.L + 63) & ~(int64_t)63;   // padded vector stride (256-byte aligned)
   const int gc = ext || !pad_fits(g) ? 0 : lat_coop_grid((int64_t)(pg.P0 / 4) * pg.N[1] * pg.N[2]);
-  if (gc > 0 && (M.plat.n != (size_t)(8 * pls) || M.plat_epoch != M.numeric_epoch)) {
-    if (M.plat.n != (size_t)(8 * pls)) {
-      GD_TRY(dalloc(M.plat, 8 * pls));
-      GD_CUDA_TRY(cudaMemsetAsync(M.plat.p, 0, sizeof(float) * 8 * pls, st));
+  if (gc > 0 && (M.plat.n != (size_t)(7 * pls) || M.plat_epoch != M.numeric_epoch)) {
+    if (M.plat.n != (size_t)(7 * pls)) {
+      GD_TRY(dalloc(M.plat, 7 * pls));
+      GD_CUDA_TRY(cudaMemsetAsync(M.plat.p, 0, sizeof(float) * 7 * pls, st));
     }
-    k_pad_setup<<<lat_grid(pg.L), kLatThreads, 0, st>>>(pg, dinvl, M.wf.p, M.plat.p + 6 * pls, M.plat.p + 7 * pls);
+    k_pad_setup<<<lat_grid(pg.L), kLatThreads, 0, st>>>(pg, dinvl, M.wf.p, M.plat.p + 5 * pls, M.plat.p + 6 * pls);
     GD_CUDA_TRY(cudaGetLastError());
     M.plat_epoch = M.numeric_epoch;
   }
@@ -999,20 +1000,19 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
       float* px = M.plat.p;
       float* pr = px + pls;
       float* pz = px + 2 * pls;
-      float* pp0 = px + 3 * pls;
-      float* pp1 = px + 4 * pls;
-      float* pq = px + 5 * pls;
-      const float* dpad = px + 6 * pls;
-      const float* wpad = px + 7 * pls;
-      k_pad_start<<<lat_grid(pg.L), kLatThreads, 0, st>>>(pg, M.node_gid.p, r64, 1.0 / rnorm, dpad, px, pr, pz, pp0,
-                                                           R);
+      float* pp = px + 3 * pls;
+      float* pq = px + 4 * pls;
+      const float* dpad = px + 5 * pls;
+      const float* wpad = px + 6 * pls;
+      k_pad_start<<<lat_grid(pg.L), kLatThreads, 0, st>>>(pg, M.node_gid.p, r64, 1.0 / rnorm, dpad, px, pr, pz, pp,
+                                                           pq, R);
       GD_CUDA_TRY(cudaGetLastError());
       GD_CUDA_TRY(cudaMemsetAsync(&R->sync, 0, sizeof(LatSync), st));
       PadGeom pga = pg;
       float rat = M.ratio;
       int mi = inner_max;
       double t2 = tol_in * tol_in;
-      void* args[] = {&pga, &wpad, &rat, &px, &pr, &pz, &pp0, &pp1, &pq, &dpad, &R, &mi, &t2};
+      void* args[] = {&pga, &wpad, &rat, &px, &pr, &pz, &pp, &pq, &dpad, &R, &mi, &t2};
       GD_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_pad_cg, dim3(gc), dim3(kLatThreads), args, 0, st));
       LatSync hs{};
       GD_CUDA_TRY(cudaMemcpyAsync(&hs, &R->sync, sizeof(hs), cudaMemcpyDeviceToHost, st));
