@@ -557,12 +557,15 @@ def run_gb300(args, rank, world, local):
         for name, code in (("jacobi_pcg_fp64", L.GD_SOLVE_JACOBI_PCG), ("mixed_ir_jacobi", L.GD_SOLVE_MIXED_IR)):
             x = torch.empty(ngdofs, dtype=torch.float64, device=dev)
             st = L.gd_solve_stats()
+            # one untimed solve first: the method's one-time device buffers and tables
+            L.load().gd_solve(assem.handle, code, 1e-8, args.solve_maxit, C.c_void_p(x.data_ptr()),
+                              L.GD_DEVICE, C.byref(st))
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             rc = L.load().gd_solve(assem.handle, code, 1e-8, args.solve_maxit, C.c_void_p(x.data_ptr()),
                                    L.GD_DEVICE, C.byref(st))
             t_solve = time.perf_counter() - t0
-            solve[name] = {"rtol": 1e-8, "seconds": t_solve, "iterations": st.iterations,
+            solve[name] = {"rtol": 1e-8, "seconds": t_solve, "timing": "second solve (warm)", "iterations": st.iterations,
                            "rel_residual": st.rel_residual, "converged": bool(st.converged and rc == 0),
                            "ms_per_iteration": 1e3 * t_solve / max(st.iterations, 1)}
 

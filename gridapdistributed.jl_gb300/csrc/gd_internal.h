@@ -181,6 +181,10 @@ struct MixedState {
   // persistent Jacobi-CG on the padded lattice: x r z p q dinv w
   DBuf<float> plat;
   int64_t plat_epoch = -1;
+  // captured batch of flexible-CG steps (lattice path, external preconditioner) and the
+  // preconditioner key, buffers and sizes it was captured with
+  cudaGraphExec_t fcg_graph = nullptr;
+  uint64_t fcg_key[5] = {0, 0, 0, 0, 0};
   int64_t lat_epoch = -1;
 };
 constexpr int kLatVectors = 8;

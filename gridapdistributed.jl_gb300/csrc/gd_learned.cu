@@ -18,6 +18,7 @@
 // minimises the relative A-norm error ||z - e||_A^2 / ||e||_A^2 over (residual, error)
 // pairs generated by the solver, with hand-written backward kernels and Adam.  All in
 // FP32; every reduction is two-stage in a fixed order (deterministic).
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <string>
@@ -326,9 +327,12 @@ __global__ void k_prolong_out_lattice(Dims c, Dims f, const float* __restrict__ 
 }
 
 // ---- direct convolution for the coarse levels ------------------------------------------------
-// One thread per (voxel, output channel), channel-major; inputs through the read-only
-// cache.  Coarse lattices are too small to fill the GPU with tiles of 512 voxels, and a
-// tiled CTA there runs long serial loops; here every thread does CI x 27 FMAs.
+// CI lanes per (voxel, output channel), one input channel each: a lane runs the 27 taps
+// of its channel (independent loads, all in flight) and the CI lanes add their sums with
+// a shuffle tree, so an output costs 27 dependent-free loads of latency instead of
+// CI x 27 serial ones.  Coarse lattices are too small to fill the GPU with tiles of 512
+// voxels, and a tiled CTA there runs long serial loops.  Outputs are channel-major; the
+// weights are staged in shared memory per block.
 template <int CI, int LD, int EP>
 __global__ void __launch_bounds__(kLT) k_conv_direct(TConvArgsS a) {
   __shared__ float sw[kC * CI * kTaps];   // [co][ci][tap] in the orientation applied
@@ -339,25 +343,31 @@ __global__ void __launch_bounds__(kLT) k_conv_direct(TConvArgsS a) {
   __syncthreads();
   const int nx = a.d.n[0], ny = a.d.n[1], nz = a.d.n[2];
   const int nv = nx * ny * nz;
-  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < a.co_n * nv; idx += gridDim.x * blockDim.x) {
-    const int co = idx / nv, v = idx - co * nv;
+  const int total = a.co_n * nv * CI;   // a multiple of CI; the stride is too, so a lane group is all in or all out
+  const unsigned gmask = CI >= 32 ? 0xffffffffu : (((1u << CI) - 1u) << ((threadIdx.x & 31) & ~(CI - 1)));
+  for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
+    const int ci = idx % CI, ov = idx / CI;
+    const int co = ov / nv, v = ov - co * nv;
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-    const float* wco = sw + co * CI * kTaps;
+    const float* wci = sw + (co * CI + ci) * kTaps;
+    const float* in = a.in + (size_t)ci * nv;
+    const float* ing = LD == LD_GATED ? a.in_gate + (size_t)ci * nv : nullptr;
     float acc = 0.f;
 #pragma unroll
     for (int tap = 0; tap < kTaps; ++tap) {
       const int xx = x + tap % 3 - 1, yy = y + (tap / 3) % 3 - 1, zz = z + tap / 9 - 1;
-      if ((unsigned)xx >= (unsigned)nx || (unsigned)yy >= (unsigned)ny || (unsigned)zz >= (unsigned)nz) continue;
-      const int u = xx + nx * (yy + ny * zz);
-#pragma unroll
-      for (int ci = 0; ci < CI; ++ci) {
-        float val = __ldg(a.in + (size_t)ci * nv + u);
-        if (LD == LD_GATED) val *= __ldg(a.in_gate + (size_t)ci * nv + u);
-        acc = fmaf(wco[ci * kTaps + tap], val, acc);
-      }
+      const bool in_range = (unsigned)xx < (unsigned)nx && (unsigned)yy < (unsigned)ny && (unsigned)zz < (unsigned)nz;
+      const int u = in_range ? xx + nx * (yy + ny * zz) : v;
+      float val = in_range ? __ldg(in + u) : 0.f;
+      if (LD == LD_GATED) val *= in_range ? __ldg(ing + u) : 0.f;
+      acc = fmaf(wci[tap], val, acc);
     }
-    if (EP == EP_GATE) acc *= __ldg(a.out_gate + (size_t)co * nv + v);
-    a.out[(size_t)co * nv + v] = acc;
+#pragma unroll
+    for (int o = CI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o, CI);
+    if (ci == 0) {
+      if (EP == EP_GATE) acc *= __ldg(a.out_gate + (size_t)co * nv + v);
+      a.out[(size_t)co * nv + v] = acc;
+    }
   }
 }
 
@@ -732,6 +742,7 @@ struct gd_learned {
   DBuf<float> zv, ev, dv, yv;
   bool prepared = false;
   int64_t prepared_epoch = -1;
+  uint64_t serial = 0;   // unique per object (key of the solver's captured graphs)
 };
 
 namespace gd {
@@ -941,7 +952,7 @@ template <int CI, int LD, int EP>
 static int direct_launch(const Dims& d, const float* in, const float* in_gate, const float* W, int adjoint, int co_n,
                          const float* out_gate, float* out, cudaStream_t st) {
   TConvArgsS a{d, in, in_gate, W, adjoint, co_n, out_gate, out};
-  k_conv_direct<CI, LD, EP><<<nb_for(co_n * d.size()), kLT, 0, st>>>(a);
+  k_conv_direct<CI, LD, EP><<<nb_for((int64_t)co_n * d.size() * CI), kLT, 0, st>>>(a);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
@@ -1114,7 +1125,9 @@ extern "C" int gd_learned_create(gd_asm* A, int levels, int flags, uint64_t seed
   const Geom& g = A->test->geom;
   if ((double)g.N[0] * g.N[1] * g.N[2] * kC >= 2147483647.0)
     return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: node lattice too large (8 channels must index in 32 bits)");
+  static std::atomic<uint64_t> next_serial{1};
   gd_learned* N = new gd_learned();
+  N->serial = next_serial.fetch_add(1);
   N->A = A;
   N->levels = levels;
   N->cs = (flags & GD_LEARNED_COARSE_START) ? 1 : 0;
@@ -1338,7 +1351,7 @@ extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_solve_learned: assemble the system first");
   cudaStream_t st = A->test->model->ctx->stream;
   GD_TRY(net_prepare(N, st));
-  MixedPrecond pc{N, apply_as_precond, apply_as_precond_lattice};
+  MixedPrecond pc{N, apply_as_precond, apply_as_precond_lattice, N->serial};
   if (fallback_used) *fallback_used = 0;
   gd_solve_stats s1{};
   int rc = mixed_solve(A, rtol, maxit, x, where, &s1, &pc);

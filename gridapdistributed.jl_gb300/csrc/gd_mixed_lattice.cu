@@ -1040,8 +1040,7 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
     double check_res = 1.0;
     int check_it = 0;
     LatScalars h{};
-    while (it < inner_max) {
-      const int nstep = std::min(batch, inner_max - it);
+    auto enqueue = [&](int nstep) -> int {
       for (int s = 0; s < nstep; ++s) {
         k_lat_apply<<<gb, kLatThreads, 0, st>>>(lg, nlat, M.wf.p, M.ratio, zb[zc], pb[pc], pb[pc ^ 1], q, R);
         pc ^= 1;
@@ -1055,6 +1054,39 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
         }
       }
       GD_CUDA_TRY(cudaGetLastError());
+      return GD_OK;
+    };
+    while (it < inner_max) {
+      const int nstep = std::min(batch, inner_max - it);
+      // A full batch is an even number of steps, so z and p return to the same buffers:
+      // one captured graph of a batch replays every full batch of every outer step.  The
+      // first batch of a solve runs uncaptured (the preconditioner's first-use setup).
+      const uint64_t key[5] = {ext ? precond->graph_key : 0, (uint64_t)(uintptr_t)M.lat.p,
+                               (uint64_t)(uintptr_t)R, (uint64_t)nlat, (uint64_t)gb};
+      const bool graphable = ext && precond->graph_key != 0 && nstep == batch;
+      const bool have = M.fcg_graph && std::equal(key, key + 5, M.fcg_key);
+      if (graphable && !have && (it > 0 || total_inner > 0)) {
+        if (M.fcg_graph) cudaGraphExecDestroy(M.fcg_graph);
+        M.fcg_graph = nullptr;
+        cudaGraph_t g = nullptr;
+        if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
+          const int rc = enqueue(nstep);
+          const cudaError_t ce = cudaStreamEndCapture(st, &g);
+          if (rc == GD_OK && ce == cudaSuccess && g &&
+              cudaGraphInstantiate(&M.fcg_graph, g, 0) == cudaSuccess) {
+            std::copy(key, key + 5, M.fcg_key);
+          } else {
+            M.fcg_graph = nullptr;
+          }
+          if (g) cudaGraphDestroy(g);
+        }
+        cudaGetLastError();   // a failed capture leaves the uncaptured path below
+      }
+      if (graphable && M.fcg_graph && std::equal(key, key + 5, M.fcg_key)) {
+        GD_CUDA_TRY(cudaGraphLaunch(M.fcg_graph, st));
+      } else {
+        GD_TRY(enqueue(nstep));
+      }
       it += nstep;
       GD_CUDA_TRY(cudaMemcpyAsync(&h, &R->sc, sizeof(h), cudaMemcpyDeviceToHost, st));
       GD_CUDA_TRY(cudaStreamSynchronize(st));

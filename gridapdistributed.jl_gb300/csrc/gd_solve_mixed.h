@@ -12,6 +12,9 @@ struct MixedPrecond {
   void* ctx;
   int (*apply)(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st);
   int (*apply_lattice)(void* ctx, gd_asm* A, const float* r, float* z, cudaStream_t st);
+  // non-zero: apply_lattice launches only stream work on buffers that stay allocated for
+  // the preconditioner's lifetime, so a captured graph of it stays valid; unique per object
+  uint64_t graph_key;
 };
 
 int residual_fp64(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, const double* x,
