@@ -327,14 +327,18 @@ __global__ void k_prolong_out_lattice(Dims c, Dims f, const float* __restrict__ 
 }
 
 // ---- direct convolution for the coarse levels ------------------------------------------------
-// CI lanes per (voxel, output channel), one input channel each: a lane runs the 27 taps
-// of its channel (independent loads, all in flight) and the CI lanes add their sums with
-// a shuffle tree, so an output costs 27 dependent-free loads of latency instead of
-// CI x 27 serial ones.  Coarse lattices are too small to fill the GPU with tiles of 512
-// voxels, and a tiled CTA there runs long serial loops.  Outputs are channel-major; the
-// weights are staged in shared memory per block.
-template <int CI, int LD, int EP>
+// SPLIT lanes per (voxel, output channel), CI / SPLIT input channels each: a lane runs
+// the 27 taps of its channels and the SPLIT lanes add their sums with a shuffle tree.
+// SPLIT = CI (one channel per lane) cuts the serial load chain of an output from
+// CI x 27 to 27 and fills the GPU on the smallest levels; SPLIT = 1 keeps a warp on 32
+// consecutive voxels of one channel plane (coalesced) for the larger coarse levels.
+// Coarse lattices are too small to fill the GPU with tiles of 512 voxels, and a tiled
+// CTA there runs long serial loops.  Outputs are channel-major; the weights are staged
+// in shared memory per block.
+template <int CI, int SPLIT, int LD, int EP>
 __global__ void __launch_bounds__(kLT) k_conv_direct(TConvArgsS a) {
+  static_assert(CI % SPLIT == 0 && (SPLIT & (SPLIT - 1)) == 0 && SPLIT <= 32, "lane split");
+  constexpr int CPL = CI / SPLIT;   // input channels per lane
   __shared__ float sw[kC * CI * kTaps];   // [co][ci][tap] in the orientation applied
   for (int i = threadIdx.x; i < a.co_n * CI * kTaps; i += blockDim.x) {
     const int tap = i % kTaps, ci = (i / kTaps) % CI, co = i / (kTaps * CI);
@@ -343,28 +347,29 @@ __global__ void __launch_bounds__(kLT) k_conv_direct(TConvArgsS a) {
   __syncthreads();
   const int nx = a.d.n[0], ny = a.d.n[1], nz = a.d.n[2];
   const int nv = nx * ny * nz;
-  const int total = a.co_n * nv * CI;   // a multiple of CI; the stride is too, so a lane group is all in or all out
-  const unsigned gmask = CI >= 32 ? 0xffffffffu : (((1u << CI) - 1u) << ((threadIdx.x & 31) & ~(CI - 1)));
+  const int total = a.co_n * nv * SPLIT;   // a multiple of SPLIT; the stride is too, so a lane group is all in or all out
+  const unsigned gmask = SPLIT >= 32 ? 0xffffffffu : (((1u << SPLIT) - 1u) << ((threadIdx.x & 31) & ~(SPLIT - 1)));
   for (int idx = blockIdx.x * blockDim.x + threadIdx.x; idx < total; idx += gridDim.x * blockDim.x) {
-    const int ci = idx % CI, ov = idx / CI;
+    const int sub = idx % SPLIT, ov = idx / SPLIT;
     const int co = ov / nv, v = ov - co * nv;
     const int x = v % nx, y = (v / nx) % ny, z = v / (nx * ny);
-    const float* wci = sw + (co * CI + ci) * kTaps;
-    const float* in = a.in + (size_t)ci * nv;
-    const float* ing = LD == LD_GATED ? a.in_gate + (size_t)ci * nv : nullptr;
     float acc = 0.f;
 #pragma unroll
     for (int tap = 0; tap < kTaps; ++tap) {
       const int xx = x + tap % 3 - 1, yy = y + (tap / 3) % 3 - 1, zz = z + tap / 9 - 1;
-      const bool in_range = (unsigned)xx < (unsigned)nx && (unsigned)yy < (unsigned)ny && (unsigned)zz < (unsigned)nz;
-      const int u = in_range ? xx + nx * (yy + ny * zz) : v;
-      float val = in_range ? __ldg(in + u) : 0.f;
-      if (LD == LD_GATED) val *= in_range ? __ldg(ing + u) : 0.f;
-      acc = fmaf(wci[tap], val, acc);
+      if ((unsigned)xx >= (unsigned)nx || (unsigned)yy >= (unsigned)ny || (unsigned)zz >= (unsigned)nz) continue;
+      const int u = xx + nx * (yy + ny * zz);
+#pragma unroll
+      for (int cj = 0; cj < CPL; ++cj) {
+        const int ci = sub * CPL + cj;
+        float val = __ldg(a.in + (size_t)ci * nv + u);
+        if (LD == LD_GATED) val *= __ldg(a.in_gate + (size_t)ci * nv + u);
+        acc = fmaf(sw[(co * CI + ci) * kTaps + tap], val, acc);
+      }
     }
 #pragma unroll
-    for (int o = CI / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o, CI);
-    if (ci == 0) {
+    for (int o = SPLIT / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(gmask, acc, o, SPLIT);
+    if (sub == 0) {
       if (EP == EP_GATE) acc *= __ldg(a.out_gate + (size_t)co * nv + v);
       a.out[(size_t)co * nv + v] = acc;
     }
@@ -948,11 +953,17 @@ constexpr int64_t kDirectConvVoxels = 60000;
 // threads per tile, so a level of ~10^5 voxels still fills the SMs
 constexpr int64_t kWideTileVoxels = 400000;
 
+// levels with fewer voxels than this split the input channels of an output across lanes
+constexpr int64_t kSplitConvVoxels = 8192;
+
 template <int CI, int LD, int EP>
 static int direct_launch(const Dims& d, const float* in, const float* in_gate, const float* W, int adjoint, int co_n,
                          const float* out_gate, float* out, cudaStream_t st) {
   TConvArgsS a{d, in, in_gate, W, adjoint, co_n, out_gate, out};
-  k_conv_direct<CI, LD, EP><<<nb_for((int64_t)co_n * d.size() * CI), kLT, 0, st>>>(a);
+  if (d.size() < kSplitConvVoxels)
+    k_conv_direct<CI, CI, LD, EP><<<nb_for((int64_t)co_n * d.size() * CI), kLT, 0, st>>>(a);
+  else
+    k_conv_direct<CI, 1, LD, EP><<<nb_for((int64_t)co_n * d.size()), kLT, 0, st>>>(a);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
