@@ -158,6 +158,13 @@ void dfreeb(DBuf<T>& b) {
 // Exclusive scan of int32 flags/counts into int64 (out has n+1 entries; out[n] = total).
 int exclusive_scan_i32(const int32_t* in, int64_t* out, int64_t n, cudaStream_t s);
 
+// Generic Q_k rows with an arbitrary reference table (gd_numeric.cu): values of the owned
+// rows, and f_const * (int v) minus the Dirichlet lifting with the table.
+int launch_rows_table(gd_asm* A, const double* kappa, const double* table, double* vals, cudaStream_t st);
+int launch_rhs_table(gd_asm* A, const double* kappa, const double* table, double f_const, double* rhs, int32_t* bad,
+                     cudaStream_t st);
+int reference_element(gd_asm* A, int degree);
+
 }  // namespace gd
 
 namespace gd {

@@ -775,6 +775,63 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   return GD_OK;
 }
 
+// Values of the owned rows with an arbitrary reference element table (a linear
+// combination of the stiffness and mass tables), kappa per cell: the generic row
+// kernel over the assembler's pattern, into `vals` (multi-field blocks).
+template <int DIM, int K>
+static int launch_rows_table_t(gd_asm* A, const double* kappa, const double* table, double* vals, cudaStream_t st) {
+  const Geom& g = A->test->geom;
+  const int64_t R = A->ngdofs;
+  if (R == 0) return GD_OK;
+  const unsigned nbw = (unsigned)std::min<int64_t>((R + 7) / 8, 152 * 64);
+  if (A->code_bytes == 1)
+    k_numeric_qk_rows<DIM, K, uint8_t><<<nbw, 256, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, A->code.p, kappa, table,
+                                                            vals);
+  else
+    k_numeric_qk_rows<DIM, K, uint16_t><<<nbw, 256, 0, st>>>(g, R, A->rowptr.p, A->row_node.p,
+                                                             (const uint16_t*)A->code.p, kappa, table, vals);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+// Right-hand side of the owned rows: f_const * (int v) minus the Dirichlet lifting with
+// `table` (kappa per cell), into `rhs`.
+template <int DIM, int K>
+static int launch_rhs_table_t(gd_asm* A, const double* kappa, const double* table, double f_const, double* rhs,
+                              int32_t* bad, cudaStream_t st) {
+  const Geom& g = A->test->geom;
+  const int64_t R = A->ngdofs;
+  if (R == 0) return GD_OK;
+  const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
+  k_numeric_rhs<DIM, K><<<(unsigned)((R + 127) / 128), 128, 0, st>>>(g, R, A->row_node.p, kappa, table, A->Mhat.p,
+                                                                     A->Fhat.p, f_const, nullptr, udir, rhs, bad);
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+int launch_rows_table(gd_asm* A, const double* kappa, const double* table, double* vals, cudaStream_t st) {
+  const Geom& g = A->test->geom;
+  if (g.dim == 2 && g.k == 1) return launch_rows_table_t<2, 1>(A, kappa, table, vals, st);
+  if (g.dim == 2 && g.k == 2) return launch_rows_table_t<2, 2>(A, kappa, table, vals, st);
+  if (g.dim == 2 && g.k == 3) return launch_rows_table_t<2, 3>(A, kappa, table, vals, st);
+  if (g.dim == 3 && g.k == 1) return launch_rows_table_t<3, 1>(A, kappa, table, vals, st);
+  if (g.dim == 3 && g.k == 2) return launch_rows_table_t<3, 2>(A, kappa, table, vals, st);
+  if (g.dim == 3 && g.k == 3) return launch_rows_table_t<3, 3>(A, kappa, table, vals, st);
+  return fail(GD_ERR_UNSUPPORTED, "numeric: unsupported dim/order");
+}
+
+int launch_rhs_table(gd_asm* A, const double* kappa, const double* table, double f_const, double* rhs, int32_t* bad,
+                     cudaStream_t st) {
+  const Geom& g = A->test->geom;
+  if (g.dim == 2 && g.k == 1) return launch_rhs_table_t<2, 1>(A, kappa, table, f_const, rhs, bad, st);
+  if (g.dim == 2 && g.k == 2) return launch_rhs_table_t<2, 2>(A, kappa, table, f_const, rhs, bad, st);
+  if (g.dim == 2 && g.k == 3) return launch_rhs_table_t<2, 3>(A, kappa, table, f_const, rhs, bad, st);
+  if (g.dim == 3 && g.k == 1) return launch_rhs_table_t<3, 1>(A, kappa, table, f_const, rhs, bad, st);
+  if (g.dim == 3 && g.k == 2) return launch_rhs_table_t<3, 2>(A, kappa, table, f_const, rhs, bad, st);
+  if (g.dim == 3 && g.k == 3) return launch_rhs_table_t<3, 3>(A, kappa, table, f_const, rhs, bad, st);
+  return fail(GD_ERR_UNSUPPORTED, "numeric: unsupported dim/order");
+}
+
 int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   if (!A || !c) return fail(GD_ERR_ARG, "gd_assemble_numeric: null argument");
   if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_assemble_numeric: run gd_assemble_symbolic first");

@@ -12,5 +12,8 @@ from .distributed import (AffineFEOperator, Boundary, CartesianDiscreteModel, FE
                           integral_grad_grad,
                           integral_source, l2_error, lagrangian, quadrature_points, solve,
                           with_gb300)
+from .multifield import (BlockMultiFieldStyle, BlockPMatrix, BlockPVector, ConsecutiveMultiFieldStyle,
+                         MultiFieldFESpace, integral_multifield, integral_multifield_source,
+                         restrict_to_field)
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -116,6 +116,18 @@ SIGNATURES = {
     "gd_learned_gradient": [P, P, P, C.c_int, DP, C.POINTER(C.c_float)],
     "gd_learned_train_step": [P, P, P, C.c_int, C.c_float, DP],
     "gd_solve_learned": [P, P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats), I32P],
+    "gd_mfield_create": [P, C.c_int, PP],
+    "gd_mfield_destroy": [P],
+    "gd_mfield_assemble": [P, DP, DP, DP, C.POINTER(gd_coeffs)],
+    "gd_mfield_block_export": [P, C.c_int, C.c_int, C.c_int, DP, DP],
+    "gd_mfield_gids": [P, C.c_int, I32P, C.c_int, I64P, I32P],
+    "gd_mfmat_create": [P, C.c_int, I32P, C.c_int, I32P, PP],
+    "gd_mfmat_destroy": [P],
+    "gd_mfmat_refresh": [P],
+    "gd_mfmat_counts": [P, I64P, I64P],
+    "gd_mfmat_sizes": [P, C.c_int, I64P, I64P, I64P, I64P],
+    "gd_mfmat_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, DP],
+    "gd_mfmat_spmv": [P, P, P, C.c_int],
 }
 _RESTYPES = {"gd_last_error": C.c_char_p, "gd_version": C.c_char_p}
 

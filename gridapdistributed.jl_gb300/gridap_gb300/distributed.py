@@ -429,6 +429,11 @@ def integral_source(f=0.0, measure: Measure = None):
 
 
 def SparseMatrixAssembler(U, V, strategy=None):
+    from .multifield import DistributedMultiFieldFESpace, MultiFieldAssembler
+    if isinstance(U, DistributedMultiFieldFESpace) or isinstance(V, DistributedMultiFieldFESpace):
+        if not isinstance(strategy, FullyAssembledRows):
+            raise NotImplementedError("multi-field assembly is built for FullyAssembledRows")
+        return MultiFieldAssembler(U, V, strategy)
     return DistributedSparseMatrixAssembler(U, V, strategy or SubAssembledRows())
 
 
@@ -624,9 +629,13 @@ def assemble_matrix_and_vector(assem: DistributedSparseMatrixAssembler, data):
 
 class AffineFEOperator:
     def __init__(self, a, l, U, V, assem=None):
+        from .multifield import MultiFieldAssembler, assemble_multifield
         self.U, self.V = U, V
         self.assem = assem if assem is not None else SparseMatrixAssembler(U, V)
-        self.matrix, self.vector = assemble_matrix_and_vector(self.assem, (a, l))
+        if isinstance(self.assem, MultiFieldAssembler):
+            self.matrix, self.vector = assemble_multifield(self.assem, a, l)
+        else:
+            self.matrix, self.vector = assemble_matrix_and_vector(self.assem, (a, l))
 
 
 class FEFunction:

@@ -315,6 +315,46 @@ int gd_learned_train_step(gd_learned* net, const float* r, const float* e, int b
 int gd_solve_learned(gd_asm* a, gd_learned* net, double rtol, int maxit, double* x, int where,
                      gd_solve_stats* stats, int32_t* fallback_used);
 
+/* ---- Multi-field systems (src/MultiField.jl, test/BlockSparseMatrixAssemblersTests.jl) ----
+ * n fields (n <= 8) that share the test/trial spaces of one FullyAssembledRows
+ * assembler (after gd_assemble_symbolic).  The bilinear form is
+ *   sum_ij int( stiff[i*n+j] grad(u_j).grad(v_i) + mass[i*n+j] u_j v_i ) kappa dOmega
+ * (kappa per cell as in gd_coeffs, NULL = 1; f_nodal must be NULL), the linear form
+ * sum_i int( src[i] v_i ) dOmega minus the Dirichlet lifting of every field with the
+ * trial space's values.  Blocks with stiff = mass = 0 are not touched (no entries).
+ * Replaces the assembly behind MultiFieldFESpace + SparseMatrixAssembler(X, Y,
+ * FullyAssembledRows()) + AffineFEOperator (MultiField.jl:283-560). */
+typedef struct gd_mfield gd_mfield;
+typedef struct gd_mfmat gd_mfmat;
+int gd_mfield_create(gd_asm* a, int nfields, gd_mfield** out);
+int gd_mfield_destroy(gd_mfield* m);
+int gd_mfield_assemble(gd_mfield* m, const double* stiff, const double* mass, const double* src,
+                       const gd_coeffs* c);
+/* Block (i, j) values over the owned rows of `part` in the scalar pattern of
+ * gd_matrix_export, and field i's right-hand side over the part's owned rows. */
+int gd_mfield_block_export(const gd_mfield* m, int i, int j, int part, double* vals, double* rhs);
+/* gids / owners of the multi-field space of `fields` (generate_multi_field_gids,
+ * MultiField.jl:356-420) for one part; local ids field-major (position * nfree + lid). */
+int gd_mfield_gids(const gd_mfield* m, int nfields, const int* fields, int part, int64_t* lid_to_gid,
+                   int32_t* lid_to_owner);
+/* The matrix of row fields rf and column fields cf: block (R, C) of a
+ * BlockMultiFieldStyle system, or the ConsecutiveMultiFieldStyle matrix for R = C = all
+ * fields (MultiField.jl:468-560).  Rows in the row group's gid order; per part the
+ * columns are the column group's owned dofs, then the touched ghost columns.  Destroy
+ * the matrices before their gd_mfield. */
+int gd_mfmat_create(gd_mfield* m, int nr, const int* rf, int nc, const int* cf, gd_mfmat** out);
+int gd_mfmat_destroy(gd_mfmat* x);
+/* values and right-hand side from the latest gd_mfield_assemble (same touched blocks) */
+int gd_mfmat_refresh(gd_mfmat* x);
+int gd_mfmat_counts(const gd_mfmat* x, int64_t* nrows, int64_t* nnz);
+int gd_mfmat_sizes(const gd_mfmat* x, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
+                   int64_t* n_ghost_cols);
+int gd_mfmat_export(const gd_mfmat* x, int part, int64_t* rowptr, int32_t* colidx, double* vals,
+                    int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs);
+/* y = A x (mul!, BlockPartitionedArrays.jl:330-350 per block): x over the column group's
+ * global numbering, y over the row group's. */
+int gd_mfmat_spmv(const gd_mfmat* x, const double* xin, double* y, int where);
+
 #ifdef __cplusplus
 }
 #endif

@@ -593,6 +593,8 @@ class Problem:
     physics: str = "poisson"        # or "elasticity"
     nu: float = 0.3                 # Poisson ratio (elasticity)
     force: tuple = None             # body force (elasticity), default 0
+    stiff: float = 1.0              # a(u,v) = int kappa (stiff grad(u).grad(v) + mass u v)
+    mass: float = 0.0
 
     @property
     def ncomp(self):
@@ -672,7 +674,7 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
     nbt = neumann_tables(pb) if pb.neumann else None
     for ic, g in enumerate(sp.cells):
         kap = pb.kappa[g]
-        Ke = kap * Kh
+        Ke = kap * Kh if (pb.stiff == 1.0 and pb.mass == 0.0) else kap * (pb.stiff * Kh + pb.mass * Mh)
         ci = np.array(P_cell_coords(pb.n, int(g)))
         X = pb.order * ci[None, :] + lnodes
         if pb.f_nodal is not None:
@@ -1003,3 +1005,124 @@ def l2_error(pb: Problem, u_nodal, u_exact):
             w = np.prod([wq[qi[d]] for d in range(dim)]) * np.prod(h)
             err += w * (u_exact(*xyz) - phi @ ue) ** 2
     return math.sqrt(err)
+
+
+# --------------------------------------------------------------------------------------
+# Multi-field systems over one scalar space (src/MultiField.jl)
+# --------------------------------------------------------------------------------------
+
+
+def multifield_gids(fe: FESpaceData, nfields: int):
+    """``generate_multi_field_gids`` (src/MultiField.jl:356-420) for ``nfields`` copies of
+    the space: local ids are field-major (f * nfree + lid, Gridap's MultiFieldFESpace);
+    each part numbers its owned dofs field by field (each field's owned dofs in its own
+    owned order) from the exclusive scan of the parts' owned counts; ghosts receive the
+    owner's number through each field's own ghost exchange (propagate_to_ghost_multifield!,
+    :422-451)."""
+    dofs = fe.dofs
+    nparts = len(dofs)
+    noids = [nfields * d.n_own for d in dofs]
+    firstgid = np.concatenate([[0], np.cumsum(noids)[:-1]]).astype(np.int64)
+    lid_gid, lid_part = [], []
+    for p, d in enumerate(dofs):
+        nfree = len(d.ldof_to_gdof)
+        g = np.full(nfields * nfree, -1, dtype=np.int64)
+        o = np.zeros(nfields * nfree, dtype=np.int32)
+        gid = firstgid[p]
+        own = np.nonzero(d.own_mask)[0]          # own_to_local: owned lids in order
+        for f in range(nfields):
+            for flid in own:
+                g[f * nfree + flid] = gid
+                gid += 1
+            o[f * nfree:(f + 1) * nfree] = d.ldof_to_owner
+        lid_gid.append(g)
+        lid_part.append(o)
+    # ghost values from the owners, field by field (the single-field exchange)
+    gid_to_lid = [{int(x): i for i, x in enumerate(d.ldof_to_gdof)} for d in dofs]
+    for p, d in enumerate(dofs):
+        nfree = len(d.ldof_to_gdof)
+        for f in range(nfields):
+            for flid in d.ghost_lids:
+                q = int(d.ldof_to_owner[flid])
+                qlid = gid_to_lid[q][int(d.ldof_to_gdof[flid])]
+                qn = len(dofs[q].ldof_to_gdof)
+                lid_gid[p][f * nfree + flid] = lid_gid[q][f * qn + qlid]
+    ngids = int(sum(noids))
+    out = [DofIndices(p, ngids, lid_gid[p], lid_part[p]) for p in range(nparts)]
+    for d in out:
+        assert (d.ldof_to_gdof >= 0).all()
+    return out
+
+
+def assemble_multifield(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf):
+    """The FullyAssembledRows matrix and right-hand side of the multi-field form
+    ``sum_ij int kappa (stiff[i][j] grad(u_j).grad(v_i) + mass[i][j] u_j v_i)``,
+    ``sum_i int src[i] v_i`` (minus the Dirichlet lifting of every field) restricted to
+    the row fields ``rf`` and column fields ``cf`` (a block of BlockMultiFieldStyle, or
+    the ConsecutiveMultiFieldStyle matrix for rf = cf = all fields): one LocalMatrix per
+    part, the local compression of FESpaces.jl:808-816 / Algebra.jl:549-579, 1245-1257 over
+    the multi-field index sets.  Blocks with stiff = mass = 0 add no entries."""
+    P, spaces, dofs = fe.P, fe.spaces, fe.dofs
+    stiff = np.asarray(stiff, dtype=np.float64)
+    mass = np.asarray(mass, dtype=np.float64)
+    nf = stiff.shape[0]
+    Kh, Mh, Fh = reference_matrices(pb.dim, pb.order, pb.h, pb.degree)
+    T = [[stiff[i, j] * Kh + mass[i, j] * Mh for j in range(nf)] for i in range(nf)]
+    touched = (stiff != 0.0) | (mass != 0.0)
+    S = [sum(T[i][j] for j in range(nf)) for i in range(nf)]
+    rg = multifield_gids(fe, len(rf))
+    cg = multifield_gids(fe, len(cf))
+    lnodes = np.array(cell_local_nodes(pb.dim, pb.order))
+    out = []
+    for p in range(P.nparts):
+        sp, di = spaces[p], dofs[p]
+        nfree = sp.nfree
+        own_dof = di.ldof_to_owner == p
+        I, J, V = [], [], []
+        b = np.zeros(len(rf) * nfree)
+        for ic, g in enumerate(sp.cells):
+            kap = pb.kappa[g]
+            cd = sp.cell_dofs[ic]
+            nd = len(cd)
+            ci = np.array(P_cell_coords(pb.n, int(g)))
+            X = pb.order * ci[None, :] + lnodes
+            for ii, i in enumerate(rf):
+                for jj, j in enumerate(cf):
+                    if not touched[i, j]:
+                        continue
+                    Ke = kap * T[i][j]
+                    for c in range(nd):          # add_entries!: column-major
+                        gj = cd[c]
+                        if gj < 0:
+                            continue
+                        for a in range(nd):
+                            gi = cd[a]
+                            if gi < 0 or not own_dof[gi]:
+                                continue
+                            I.append(ii * nfree + gi); J.append(jj * nfree + gj); V.append(Ke[a, c])
+                be = src[i] * Fh
+                if pb.u_dir is not None:
+                    ud = np.where(cd < 0, pb.u_dir[pb.node_lin(X)], 0.0)
+                    be = be - kap * (S[i] @ ud)
+                for a in range(nd):
+                    gi = cd[a]
+                    if gi >= 0 and own_dof[gi]:
+                        b[ii * nfree + gi] += be[a]
+        I = np.array(I, dtype=np.int64); J = np.array(J, dtype=np.int64); V = np.array(V, dtype=np.float64)
+        rdi, cdi = rg[p], cg[p]
+        rown = rdi.own_to_global
+        cown = cdi.own_to_global
+        gl = np.unique(J[~cdi.own_mask[J]]) if len(J) else np.zeros(0, dtype=np.int64)
+        cg_g = cdi.ldof_to_gdof[gl]; cg_o = cdi.ldof_to_owner[gl]
+        row_map = {int(x): k for k, x in enumerate(rown)}
+        col_map = {int(x): k for k, x in enumerate(cown)}
+        for k, x in enumerate(cg_g):
+            col_map[int(x)] = len(cown) + k
+        Ig = rdi.ldof_to_gdof[I]; Jg = cdi.ldof_to_gdof[J]
+        Il = np.array([row_map[int(x)] for x in Ig], dtype=np.int64)
+        Jl = np.array([col_map[int(x)] for x in Jg], dtype=np.int64)
+        rowptr, colidx, vals = _compress(len(rown), Il, Jl, V, len(cown) + len(cg_g))
+        out.append(LocalMatrix(p, len(rown), len(cown) + len(cg_g), rowptr, colidx, vals, rown,
+                               np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32),
+                               cown, cg_g, cg_o.astype(np.int32), b[rdi.own_mask]))
+    return out
