@@ -164,6 +164,10 @@ int launch_rows_table(gd_asm* A, const double* kappa, const double* table, doubl
 int launch_rhs_table(gd_asm* A, const double* kappa, const double* table, double f_const, double* rhs, int32_t* bad,
                      cudaStream_t st);
 int reference_element(gd_asm* A, int degree);
+// FP64 Jacobi-PCG on the owned rows of a CSR with global column ids (gd_solve.cu)
+int jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals, const double* rhs,
+                   DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
+                   double* x, int where, gd_solve_stats* stats);
 
 }  // namespace gd
 
@@ -198,6 +202,8 @@ constexpr int kLatVectors = 8;
 
 // host quadrature helpers (gd_numeric.cu)
 void gauss_legendre01(int n, std::vector<double>& x, std::vector<double>& w);
+// Gridap's local node order of one Q_k cell: lattice offsets of each local dof (gd_space.cu)
+void cell_dof_positions(int dim, int k, std::vector<int>& pos);
 void lagrange01(int k, double x, double* v, double* dv);
 }  // namespace gd
 

@@ -304,31 +304,37 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   }
   if (method != GD_SOLVE_JACOBI_PCG) return fail(GD_ERR_UNSUPPORTED, "gd_solve: unknown method");
   if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve: bad argument");
-  cudaStream_t st = A->test->model->ctx->stream;
-  const int64_t n = A->ngdofs;
+  return jacobi_pcg_csr(A->ngdofs, A->rowptr.p, A->colgid.p, A->vals.p, A->rhs_override ? A->rhs_override : A->rhs.p,
+                        A->w, A->dinv, A->dred, A->test->model->ctx->stream, rtol, maxit, x, where, stats);
+}
+
+// FP64 Jacobi-PCG on the owned rows of a CSR (global column ids); workspace buffers are
+// (re)allocated as needed: w (5 n: x r z p q), dinv (n), dred (partials and scalars).
+int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals, const double* rhs,
+                   DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
+                   double* x, int where, gd_solve_stats* stats) {
   auto t0 = std::chrono::steady_clock::now();
-  // workspace: x r z p q (5n) + dinv (n); partial sums + scalars in dred
-  if (A->w.n < (size_t)(5 * n)) GD_TRY(dalloc(A->w, 5 * std::max<int64_t>(n, 1)));
-  if (A->dinv.n < (size_t)n) GD_TRY(dalloc(A->dinv, std::max<int64_t>(n, 1)));
-  if (!A->dred.p) GD_TRY(dalloc(A->dred, 4096));
-  double* dx = A->w.p;
+  if (w.n < (size_t)(5 * n)) GD_TRY(dalloc(w, 5 * std::max<int64_t>(n, 1)));
+  if (dinvb.n < (size_t)n) GD_TRY(dalloc(dinvb, std::max<int64_t>(n, 1)));
+  if (!dred.p) GD_TRY(dalloc(dred, 4096));
+  double* dinv = dinvb.p;
+  double* dx = w.p;
   double* dr = dx + n;
   double* dz = dr + n;
   double* dp = dz + n;
   double* dq = dp + n;
-  double* pa = A->dred.p + 16;
+  double* pa = dred.p + 16;
   double* pb = pa + kMaxPartials;
-  Scalars* sc = (Scalars*)(A->dred.p + 16 + 2 * kMaxPartials);
-  int32_t* bad = (int32_t*)A->dred.p;
-  const double* rhs = A->rhs_override ? A->rhs_override : A->rhs.p;
+  Scalars* sc = (Scalars*)(dred.p + 16 + 2 * kMaxPartials);
+  int32_t* bad = (int32_t*)dred.p;
   GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
   GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
-  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, A->dinv.p, bad);
+  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, rowptr, colgid, vals, dinv, bad);
   GD_CUDA_TRY(cudaGetLastError());
   const int gs = grid_for(n, kRowsPerSpmvBlock);
   const int gv = grid_for(n, kVecThreads);
   // r = b - A*0 = b ; bb
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, dr, pa, pb);
+  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dx, rhs, dr, pa, pb);
   k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);   // rz <- bb (temp), rr <- rr
   GD_CUDA_TRY(cudaGetLastError());
   Scalars h{};
@@ -338,7 +344,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   GD_CUDA_TRY(cudaStreamSynchronize(st));
   if (hbad) return fail(GD_ERR_NUMERIC, "gd_solve: non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
   const double bnorm = std::sqrt(h.rz);
-  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, A->dinv.p, dr, dz, dp, pa, pb);
+  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
   k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
   GD_CUDA_TRY(cudaGetLastError());
   int it = 0;
@@ -352,9 +358,9 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
     while (!conv && it < maxit) {
       int nstep = std::min(check_every, maxit - it);
       for (int s = 0; s < nstep; ++s) {
-        k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
+        k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dp, dq, dp, pa);
         k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
-        k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, A->dinv.p, pa, pb);
+        k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, dinv, pa, pb);
         k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
         k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
       }
@@ -366,7 +372,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
       if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
     }
     // true FP64 residual (kept in r for a restart)
-    k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, rhs, dr, pa, pb);
+    k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dx, rhs, dr, pa, pb);
     k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
     GD_CUDA_TRY(cudaGetLastError());
     GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
@@ -374,7 +380,7 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
     const double rel_true = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
     if (!conv || rel_true <= rtol || !std::isfinite(rel_true) || it >= maxit || restart >= kMaxRestarts) break;
     conv = false;
-    k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, A->dinv.p, dr, dz, dp, pa, pb);
+    k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
     k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
     GD_CUDA_TRY(cudaGetLastError());
   }

@@ -173,6 +173,24 @@ __global__ void k_node_pos(Geom g, const DevPart* __restrict__ parts, int64_t to
   posflag[P.node_off + pos] = node_is_dirichlet(g, X) ? 0 : 1;
 }
 
+// Gridap's local node order of one Q_k cell (vertices, edges, faces, interior): for
+// local dof a, its lattice offsets (pos[3a + d] in [0, k]).
+void cell_dof_positions(int dim, int k, std::vector<int>& pos) {
+  int nn = 1;
+  for (int d = 0; d < dim; ++d) nn *= k + 1;
+  pos.assign(3 * nn, 0);
+  const int64_t m[kMaxDim] = {1, 1, 1};
+  for (int t = 0; t < nn; ++t) {
+    int64_t Y[kMaxDim] = {0, 0, 0};
+    for (int d = 0, r = t; d < dim; ++d) {
+      Y[d] = r % (k + 1);
+      r /= k + 1;
+    }
+    const int64_t a = gridap_dof_pos(dim, k, m, Y);
+    for (int d = 0; d < dim; ++d) pos[3 * a + d] = (int)Y[d];
+  }
+}
+
 __global__ void k_node_lid(Geom g, const DevPart* __restrict__ parts, int64_t total_nodes,
                            const int32_t* __restrict__ node_pos, const int32_t* __restrict__ posflag,
                            const int64_t* __restrict__ pscan, int32_t* __restrict__ node_lid,

@@ -12,6 +12,7 @@ from .distributed import (AffineFEOperator, Boundary, CartesianDiscreteModel, FE
                           integral_grad_grad,
                           integral_source, l2_error, lagrangian, quadrature_points, solve,
                           with_gb300)
+from .dg import Skeleton, integral_sipg, integral_sipg_source
 from .multifield import (BlockMultiFieldStyle, BlockPMatrix, BlockPVector, ConsecutiveMultiFieldStyle,
                          MultiFieldFESpace, integral_multifield, integral_multifield_source,
                          restrict_to_field)

@@ -44,6 +44,12 @@ class gd_elasticity(C.Structure):
                 ("where", C.c_int)]
 
 
+class gd_dg_form(C.Structure):
+    _fields_ = [("gamma", C.c_double), ("h", C.c_double), ("degree", C.c_int), ("f_const", C.c_double),
+                ("f_qp", C.c_void_p), ("dirichlet_sides", C.c_void_p), ("ud_qp", C.c_void_p),
+                ("neumann_sides", C.c_void_p), ("g_qp", C.c_void_p), ("where", C.c_int)]
+
+
 class gd_solve_stats(C.Structure):
     _fields_ = [("iterations", C.c_int32), ("converged", C.c_int32), ("rel_residual", C.c_double),
                 ("seconds", C.c_double)]
@@ -128,6 +134,17 @@ SIGNATURES = {
     "gd_mfmat_sizes": [P, C.c_int, I64P, I64P, I64P, I64P],
     "gd_mfmat_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, DP],
     "gd_mfmat_spmv": [P, P, P, C.c_int],
+    "gd_dg_space_create": [P, C.c_int, PP],
+    "gd_dg_space_destroy": [P],
+    "gd_dg_num_free_dofs": [P, I64P],
+    "gd_dg_local_sizes": [P, C.c_int, I64P, I64P, I64P],
+    "gd_dg_get_gids": [P, C.c_int, I64P, I32P],
+    "gd_dg_assemble": [P, C.POINTER(gd_dg_form)],
+    "gd_dg_matrix_sizes": [P, C.c_int, I64P, I64P, I64P, I64P],
+    "gd_dg_matrix_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, DP],
+    "gd_dg_spmv": [P, P, P, C.c_int],
+    "gd_dg_solve": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
+    "gd_dg_l2_error": [P, P, P, C.c_int, C.c_int, DP],
 }
 _RESTYPES = {"gd_last_error": C.c_char_p, "gd_version": C.c_char_p}
 

@@ -304,8 +304,13 @@ class DistributedSingleFieldFESpace:
 
 
 def TestFESpace(model, reffe, dirichlet_tags="boundary", conformity=None):
+    if conformity in ("L2", ":L2"):
+        from .dg import DistributedDGFESpace
+        if reffe[1] is not float:
+            raise NotImplementedError("discontinuous spaces: scalar fields")
+        return DistributedDGFESpace(model, reffe[2])
     if conformity not in (None, "H1", ":H1"):
-        raise NotImplementedError("only conforming (H1) spaces")
+        raise NotImplementedError("conforming (H1) and discontinuous (L2) spaces")
     return DistributedSingleFieldFESpace(model, reffe, dirichlet_tags)
 
 
@@ -629,8 +634,15 @@ def assemble_matrix_and_vector(assem: DistributedSparseMatrixAssembler, data):
 
 class AffineFEOperator:
     def __init__(self, a, l, U, V, assem=None):
+        from .dg import DistributedDGFESpace, assemble_dg
         from .multifield import MultiFieldAssembler, assemble_multifield
         self.U, self.V = U, V
+        if isinstance(V, DistributedDGFESpace):
+            if U is not V or assem is not None:
+                raise NotImplementedError("DG: trial space = test space, the built-in assembly")
+            self.assem = None
+            self.matrix, self.vector = assemble_dg(V, a, l)
+            return
         self.assem = assem if assem is not None else SparseMatrixAssembler(U, V)
         if isinstance(self.assem, MultiFieldAssembler):
             self.matrix, self.vector = assemble_multifield(self.assem, a, l)
@@ -684,6 +696,9 @@ def quadrature_points(model: DistributedDiscreteModel, degree: int):
 def l2_error(uh: "FEFunction", u_exact, measure: Measure) -> float:
     """``sqrt(sum(∫( abs2(u - uh) )dΩ))`` on the device; ``u_exact`` is a vectorised callable
     of the coordinates (a tuple of components on vector spaces)."""
+    from .dg import DGFEFunction, dg_l2_error
+    if isinstance(uh, DGFEFunction):
+        return dg_l2_error(uh, u_exact, measure)
     U = uh.U
     xyz = quadrature_points(U.model, measure.degree)
     vals = u_exact(*[xyz[:, d] for d in range(U.model.dim)])
@@ -699,5 +714,8 @@ def l2_error(uh: "FEFunction", u_exact, measure: Measure) -> float:
 
 
 def solve(op: AffineFEOperator, rtol=1e-12, maxit=100000):
+    from .dg import DGFEFunction, DistributedDGFESpace
     x = op.matrix.solve(rtol=rtol, maxit=maxit)
+    if isinstance(op.U, DistributedDGFESpace):
+        return DGFEFunction(op.U, x)
     return FEFunction(op.U, x)

@@ -355,6 +355,47 @@ int gd_mfmat_export(const gd_mfmat* x, int part, int64_t* rowptr, int32_t* colid
  * global numbering, y over the row group's. */
 int gd_mfmat_spmv(const gd_mfmat* x, const double* xin, double* y, int where);
 
+/* ---- Discontinuous Galerkin (test/PoissonTests.jl:47-77) ----
+ * FESpace(model, ReferenceFE(lagrangian, Float64, k), conformity=:L2), k <= 3: every
+ * cell holds its (k+1)^d dofs (reference node order); a part owns its owned cells' dofs,
+ * numbered cell by cell (lexicographic), parts in order. */
+typedef struct gd_dgspace gd_dgspace;
+int gd_dg_space_create(gd_model* model, int order, gd_dgspace** out);
+int gd_dg_space_destroy(gd_dgspace* s);
+int gd_dg_num_free_dofs(const gd_dgspace* s, int64_t* n);
+int gd_dg_local_sizes(const gd_dgspace* s, int part, int64_t* nlocal, int64_t* nown, int64_t* first);
+int gd_dg_get_gids(const gd_dgspace* s, int part, int64_t* gid, int32_t* owner);
+/* The symmetric interior penalty form of the reference's DG Poisson test:
+ *   a(u,v) = int grad(v).grad(u) + sum_Gd int((gamma/h) v u - v dn(u) - dn(v) u)
+ *            + sum_Skeleton int((gamma/h) [[v n]].[[u n]] - [[v n]].{grad u} - {grad v}.[[u n]])
+ *   l(v)   = int f v + sum_Gn int g v + sum_Gd int((gamma/h) v uD - dn(v) uD)
+ * f: f_const, or f_qp at the cells' Gauss points (cells lexicographic, nq^d points x
+ * fastest); uD / g at the face Gauss points of the flagged sides (layout of
+ * gd_add_boundary_source); nq = (degree + 2) / 2 for cells and faces. */
+typedef struct gd_dg_form {
+  double gamma;
+  double h;
+  int degree;
+  double f_const;
+  const double* f_qp;
+  const int32_t* dirichlet_sides;  /* 2*dim flags */
+  const double* ud_qp;
+  const int32_t* neumann_sides;    /* 2*dim flags */
+  const double* g_qp;
+  int where;                       /* GD_HOST or GD_DEVICE for f_qp, ud_qp, g_qp */
+} gd_dg_form;
+/* Matrix and right-hand side of the owned rows (FullyAssembledRows: each owned row
+ * summed by its part; columns: owned dofs, then the touched ghost dofs in local order). */
+int gd_dg_assemble(gd_dgspace* s, const gd_dg_form* form);
+int gd_dg_matrix_sizes(const gd_dgspace* s, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
+                       int64_t* n_ghost_cols);
+int gd_dg_matrix_export(const gd_dgspace* s, int part, int64_t* rowptr, int32_t* colidx, double* vals,
+                        int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs);
+int gd_dg_spmv(const gd_dgspace* s, const double* x, double* y, int where);
+int gd_dg_solve(gd_dgspace* s, double rtol, int maxit, double* x, int where, gd_solve_stats* stats);
+/* sqrt(sum(int (u - uh)^2 dOmega)): u at the cells' Gauss points (layout of f_qp) */
+int gd_dg_l2_error(const gd_dgspace* s, const double* x, const double* u_qp, int degree, int where, double* err);
+
 #ifdef __cplusplus
 }
 #endif

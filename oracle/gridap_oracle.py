@@ -1126,3 +1126,190 @@ def assemble_multifield(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf):
                                np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32),
                                cown, cg_g, cg_o.astype(np.int32), b[rdi.own_mask]))
     return out
+
+
+# --------------------------------------------------------------------------------------
+# Discontinuous Galerkin (test/PoissonTests.jl:47-77)
+# --------------------------------------------------------------------------------------
+
+
+def _shape_ref(dim, k, lnodes, xi):
+    """Values (NN,) and reference gradients (NN, dim) of the Q_k basis (nodes lnodes,
+    Gridap order) at the reference point xi in [0,1]^dim."""
+    vals, ders = [], []
+    for d in range(dim):
+        v, dv = lagrange_1d(k, np.array([xi[d]]))
+        vals.append(v[0]); ders.append(dv[0])
+    nn = len(lnodes)
+    phi = np.ones(nn)
+    grad = np.ones((nn, dim))
+    for a, node in enumerate(lnodes):
+        for d in range(dim):
+            phi[a] *= vals[d][node[d]]
+            for e in range(dim):
+                grad[a, e] *= ders[d][node[d]] if e == d else vals[d][node[d]]
+    return phi, grad
+
+
+def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neumann_sides, u_dir, g_neu):
+    """Symmetric interior penalty system of test/PoissonTests.jl:47-77 on a Cartesian
+    model, assembled the way a finite-element code does it: cell loops for the volume
+    terms, one loop over the interior faces (each face once, its 2x2-block matrix with
+    [[w n]] = w+ n+ + w- n- and {q} = (q+ + q-)/2 at the physical face points) and the
+    boundary faces (Nitsche terms on the Dirichlet sides, g on the Neumann sides).
+
+    Numbering (Gridap's L2 spaces): a cell's dofs in reference node order; a part's owned
+    cells lexicographic, parts in order; local dofs of every local cell in local-box
+    order.  Returns one LocalMatrix per part with FullyAssembledRows columns (owned dofs,
+    then the touched ghost dofs sorted by local id) and b over the owned rows.
+
+    f: constant; u_dir(x), g_neu(x, normal): callables on the physical face points."""
+    P = make_partition(np_, n)
+    dim = len(n)
+    nn = (k + 1) ** dim
+    lnodes = cell_local_nodes(dim, k)
+    h = [(domain[2 * d + 1] - domain[2 * d]) / n[d] for d in range(dim)]
+    det = float(np.prod(h))
+    nq = quad_points_per_dir(degree)
+    xq, wq = gauss_legendre(nq)
+    ncells = int(np.prod(n))
+    # gids
+    owner = np.array([P.cell_owner(P.cell_coords(c)) for c in range(ncells)], dtype=np.int32)
+    ncell_own = np.bincount(owner, minlength=P.nparts)
+    first = np.concatenate([[0], np.cumsum(nn * ncell_own)[:-1]]).astype(np.int64)
+    rank = np.zeros(ncells, dtype=np.int64)
+    seen = np.zeros(P.nparts, dtype=np.int64)
+    for c in range(ncells):            # lexicographic = each owner's box order
+        rank[c] = seen[owner[c]]
+        seen[owner[c]] += 1
+    gid0 = first[owner] + nn * rank
+    ndofs = int(nn * ncells)
+
+    def cell_x0(ci):
+        return np.array([domain[2 * d] + ci[d] * h[d] for d in range(dim)])
+
+    def phys_shape(ci, x):
+        xi = (x - cell_x0(ci)) / np.array(h)
+        phi, g = _shape_ref(dim, k, lnodes, xi)
+        return phi, g / np.array(h)[None, :]
+
+    rows, cols, vals = [], [], []
+    b = np.zeros(ndofs)
+
+    def add(c1, c2, M):
+        for a in range(nn):
+            for bb in range(nn):
+                rows.append(gid0[c1] + a); cols.append(gid0[c2] + bb); vals.append(M[a, bb])
+
+    qpts = list(itertools.product(range(nq), repeat=dim))
+    for c in range(ncells):
+        ci = P.cell_coords(c)
+        Ke = np.zeros((nn, nn)); be = np.zeros(nn)
+        for q in qpts:
+            x = cell_x0(ci) + np.array([xq[q[d]] * h[d] for d in range(dim)])
+            w = det * np.prod([wq[q[d]] for d in range(dim)])
+            phi, gr = phys_shape(ci, x)
+            Ke += w * gr @ gr.T
+            be += w * f * phi
+        add(c, c, Ke)
+        b[gid0[c]:gid0[c] + nn] += be
+    pen = gamma / hpen
+    for c in range(ncells):
+        ci = P.cell_coords(c)
+        for d in range(dim):
+            tang = [t for t in range(dim) if t != d]
+            fm = float(np.prod([h[t] for t in tang]))
+            fq = list(itertools.product(range(nq), repeat=dim - 1))
+            # the upper face of c along d: interior (with the next cell) or the x_d = max side
+            for side in (0, 1):
+                on_lower = side == 0 and ci[d] == 0
+                if side == 0 and not on_lower:
+                    continue   # interior lower faces are the upper faces of the previous cell
+                nb = list(ci); nb[d] += 1
+                interior = side == 1 and nb[d] < n[d]
+                if side == 1 and not interior and ci[d] != n[d] - 1:
+                    continue
+                normal = np.zeros(dim); normal[d] = 1.0 if side == 1 else -1.0
+                xd = domain[2 * d] + (ci[d] + side) * h[d]
+                if interior:
+                    cn = P.cell_gid(tuple(nb))
+                    A = np.zeros((2 * nn, 2 * nn))
+                    for qf in fq:
+                        x = np.zeros(dim); x[d] = xd
+                        for j, t in enumerate(tang):
+                            x[t] = domain[2 * t] + (ci[t] + xq[qf[j]]) * h[t]
+                        w = fm * np.prod([wq[qf[j]] for j in range(dim - 1)])
+                        pp, gp = phys_shape(ci, x)        # + side (this cell), n+ = normal
+                        pm, gm = phys_shape(nb, x)        # - side, n- = -normal
+                        jv = np.concatenate([pp, -pm])    # [[w n]] . n+ for the 2nn basis
+                        mg = 0.5 * np.concatenate([gp @ normal, gm @ normal])   # {grad w} . n+
+                        A += w * (pen * np.outer(jv, jv) - np.outer(jv, mg) - np.outer(mg, jv))
+                    add(c, c, A[:nn, :nn]); add(c, cn, A[:nn, nn:])
+                    add(cn, c, A[nn:, :nn]); add(cn, cn, A[nn:, nn:])
+                    continue
+                s = 2 * d + side
+                if not (dirichlet_sides[s] or neumann_sides[s]):
+                    continue
+                A = np.zeros((nn, nn)); be = np.zeros(nn)
+                for qf in fq:
+                    x = np.zeros(dim); x[d] = xd
+                    for j, t in enumerate(tang):
+                        x[t] = domain[2 * t] + (ci[t] + xq[qf[j]]) * h[t]
+                    w = fm * np.prod([wq[qf[j]] for j in range(dim - 1)])
+                    phi, gr = phys_shape(ci, x)
+                    dn = gr @ normal
+                    if dirichlet_sides[s]:
+                        A += w * (pen * np.outer(phi, phi) - np.outer(phi, dn) - np.outer(dn, phi))
+                        be += w * (pen * phi - dn) * u_dir(*x)
+                    else:
+                        be += w * phi * g_neu(*x, *normal)
+                if dirichlet_sides[s]:
+                    add(c, c, A)
+                b[gid0[c]:gid0[c] + nn] += be
+    I = np.array(rows, dtype=np.int64); J = np.array(cols, dtype=np.int64); V = np.array(vals)
+    # FullyAssembledRows local parts
+    out = []
+    for p in range(P.nparts):
+        lcells = P.local_cells(p)
+        lid_of = {}
+        for i, cg in enumerate(lcells):
+            for a in range(nn):
+                lid_of[int(gid0[cg]) + a] = i * nn + a
+        own0, own1 = int(first[p]), int(first[p] + nn * ncell_own[p])
+        sel = (I >= own0) & (I < own1)
+        Ip, Jp, Vp = I[sel] - own0, J[sel], V[sel]
+        ghost = sorted({lid_of[int(j)] for j in Jp if not (own0 <= j < own1)})
+        gmap = {l: i for i, l in enumerate(ghost)}
+        lid_gid = {l: g for g, l in lid_of.items()}
+        Jl = np.array([j - own0 if own0 <= j < own1 else (own1 - own0) + gmap[lid_of[int(j)]] for j in Jp],
+                      dtype=np.int64)
+        rowptr, colidx, vv = _compress(own1 - own0, Ip, Jl, Vp, (own1 - own0) + len(ghost))
+        gg = np.array([lid_gid[l] for l in ghost], dtype=np.int64)
+        gown = np.array([int(np.searchsorted(first, g, side="right") - 1) for g in gg], dtype=np.int32)
+        own_g = np.arange(own0, own1, dtype=np.int64)
+        out.append(LocalMatrix(p, own1 - own0, (own1 - own0) + len(ghost), rowptr, colidx, vv, own_g,
+                               np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32),
+                               own_g, gg, gown, b[own0:own1].copy()))
+    return out, gid0, ndofs
+
+
+def dg_l2_error(np_, n, domain, k, degree, x, gid0, u):
+    """sqrt(sum(int (u - uh)^2 dOmega)) for DG dof values x (dg_system's numbering)."""
+    dim = len(n)
+    lnodes = cell_local_nodes(dim, k)
+    h = [(domain[2 * d + 1] - domain[2 * d]) / n[d] for d in range(dim)]
+    det = float(np.prod(h))
+    nq = quad_points_per_dir(degree)
+    xq, wq = gauss_legendre(nq)
+    P = make_partition(np_, n)
+    tot = 0.0
+    for c in range(int(np.prod(n))):
+        ci = P.cell_coords(c)
+        xv = x[gid0[c]:gid0[c] + len(lnodes)]
+        for q in itertools.product(range(nq), repeat=dim):
+            xi = np.array([xq[q[d]] for d in range(dim)])
+            phi, _ = _shape_ref(dim, k, lnodes, xi)
+            pt = [domain[2 * d] + (ci[d] + xi[d]) * h[d] for d in range(dim)]
+            w = det * np.prod([wq[q[d]] for d in range(dim)])
+            tot += w * (u(*pt) - phi @ xv) ** 2
+    return math.sqrt(tot)
