@@ -185,6 +185,7 @@ struct MixedState {
   DBuf<int32_t> node_gid; // lattice node -> gid (-1 Dirichlet)
   DBuf<float> wf;         // prescaled cell coefficients (FP32)
   DBuf<float> vals32;     // FP32 copy of the owned-row values (non-cube spaces)
+  int csr_lanes = 1;      // lanes per row of the FP32 CSR operator (1: one thread per row)
   DBuf<float> zold;       // previous preconditioned residual (flexible CG)
   // lattice-order inner iteration (3D cube Q1): x r z0 z1 p0 p1 q dinv, node-lattice sized
   DBuf<float> lat;

@@ -131,6 +131,87 @@ k_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restr
   if (threadIdx.x == 0) partial_bb[blockIdx.x] = t;
 }
 
+// Long rows (vector and high-order systems: 81 to 375 entries): G lanes per row, each lane
+// a strided share of the row's entries (coalesced across the group), then a log2(G)
+// shuffle tree.  Thread-per-row staging leaves most lanes idle there, because a chunk of
+// staged entries covers only a few rows.
+template <int MODE, int G>
+__device__ __forceinline__ void csr_rows_g(int64_t n, const int64_t* __restrict__ rowptr,
+                                           const int32_t* __restrict__ col, const double* __restrict__ val,
+                                           const double* __restrict__ x, const double* __restrict__ b,
+                                           double* __restrict__ out, const double* __restrict__ w, double& s1,
+                                           double& s2) {
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31, sub = lane / G, gl = lane % G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  for (int64_t rb = warp * RPW; rb < n; rb += nw * RPW) {   // warp-uniform trip count
+    const int64_t r = rb + sub;
+    const bool valid = r < n;
+    double acc = 0.0;
+    if (valid) {
+      const int64_t e1 = rowptr[r + 1];
+      int64_t e = rowptr[r] + gl;
+      for (; e + 3 * G < e1; e += 4 * G) {   // 4 independent entries in flight per lane
+        int32_t c[4];
+        double v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          c[u] = col[e + u * G];
+          v[u] = val[e + u * G];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) acc = fma(v[u], xv[u], acc);
+      }
+      for (; e < e1; e += G) acc = fma(val[e], __ldg(x + col[e]), acc);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if (valid && gl == 0) {
+      if (MODE == 0) {
+        out[r] = acc;
+        if (w) s1 = fma(acc, w[r], s1);
+      } else {
+        const double bv = b[r];
+        const double rv = bv - acc;
+        if (out) out[r] = rv;
+        s1 = fma(rv, rv, s1);
+        s2 = fma(bv, bv, s2);
+      }
+    }
+  }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kSpmvThreads)
+k_spmv_g(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+         const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y,
+         const double* __restrict__ w, double* __restrict__ partial) {
+  __shared__ double sh[kSpmvThreads + kSpmvThreads / 32];
+  double dot = 0.0, unused = 0.0;
+  csr_rows_g<0, G>(n, rowptr, col, val, x, nullptr, y, w, dot, unused);
+  if (partial) {
+    const double t = block_sum_serial(dot, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  }
+}
+
+template <int G>
+__global__ void __launch_bounds__(kSpmvThreads)
+k_residual_g(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+             const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ b,
+             double* __restrict__ r_out, double* __restrict__ partial_rr, double* __restrict__ partial_bb) {
+  __shared__ double sh[kSpmvThreads + kSpmvThreads / 32];
+  double rr = 0.0, bb = 0.0;
+  csr_rows_g<1, G>(n, rowptr, col, val, x, b, r_out, nullptr, rr, bb);
+  double t = block_sum_serial(rr, sh);
+  if (threadIdx.x == 0) partial_rr[blockIdx.x] = t;
+  t = block_sum_serial(bb, sh);
+  if (threadIdx.x == 0) partial_bb[blockIdx.x] = t;
+}
+
 __global__ void k_dinv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                        const double* __restrict__ val, double* __restrict__ dinv, int32_t* __restrict__ bad) {
   int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -314,6 +395,33 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
                    DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
                    double* x, int where, gd_solve_stats* stats) {
   auto t0 = std::chrono::steady_clock::now();
+  // rows per lane group from the average row length (thread per row below 48 entries)
+  int64_t nnz = 0;
+  if (n) {
+    GD_CUDA_TRY(cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  const int64_t avg = n ? nnz / n : 0;
+  const int G = avg >= 256 ? 32 : avg >= 96 ? 16 : avg >= 48 ? 8 : 1;
+  const int gsg = G == 1 ? grid_for(n, kRowsPerSpmvBlock)
+                         : (int)std::max<int64_t>(1, std::min<int64_t>((n * G + kSpmvThreads - 1) / kSpmvThreads,
+                                                                       kMaxPartials));
+  auto spmv = [&](const double* xin, double* yout, const double* wdot, double* part) {
+    switch (G) {
+      case 32: k_spmv_g<32><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
+      case 16: k_spmv_g<16><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
+      case 8: k_spmv_g<8><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
+      default: k_spmv<<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part);
+    }
+  };
+  auto residual = [&](const double* xin, double* rout, double* prr, double* pbb) {
+    switch (G) {
+      case 32: k_residual_g<32><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
+      case 16: k_residual_g<16><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
+      case 8: k_residual_g<8><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
+      default: k_residual<<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb);
+    }
+  };
   if (w.n < (size_t)(5 * n)) GD_TRY(dalloc(w, 5 * std::max<int64_t>(n, 1)));
   if (dinvb.n < (size_t)n) GD_TRY(dalloc(dinvb, std::max<int64_t>(n, 1)));
   if (!dred.p) GD_TRY(dalloc(dred, 4096));
@@ -331,10 +439,10 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
   GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
   k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, rowptr, colgid, vals, dinv, bad);
   GD_CUDA_TRY(cudaGetLastError());
-  const int gs = grid_for(n, kRowsPerSpmvBlock);
+  const int gs = gsg;
   const int gv = grid_for(n, kVecThreads);
   // r = b - A*0 = b ; bb
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dx, rhs, dr, pa, pb);
+  residual(dx, dr, pa, pb);
   k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);   // rz <- bb (temp), rr <- rr
   GD_CUDA_TRY(cudaGetLastError());
   Scalars h{};
@@ -358,7 +466,7 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
     while (!conv && it < maxit) {
       int nstep = std::min(check_every, maxit - it);
       for (int s = 0; s < nstep; ++s) {
-        k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dp, dq, dp, pa);
+        spmv(dp, dq, dp, pa);
         k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
         k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, dinv, pa, pb);
         k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
@@ -372,7 +480,7 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
       if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
     }
     // true FP64 residual (kept in r for a restart)
-    k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, dx, rhs, dr, pa, pb);
+    residual(dx, dr, pa, pb);
     k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
     GD_CUDA_TRY(cudaGetLastError());
     GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));

@@ -137,6 +137,53 @@ k_csr32_apply(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __re
   }
 }
 
+// The same with G lanes per row (long rows: vector and high-order spaces), strided
+// coalesced entries per lane and a shuffle tree; the group's first lane writes the row.
+template <int G>
+__global__ void __launch_bounds__(kMxThreads)
+k_csr32_apply_g(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                const float* __restrict__ val, const float* __restrict__ x, float* __restrict__ y,
+                double* __restrict__ partial) {
+  __shared__ double sh[kMxThreads / 32];
+  constexpr int RPW = 32 / G;
+  const int lane = threadIdx.x & 31, sub = lane / G, gl = lane % G;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  float dot = 0.f;
+  for (int64_t rb = warp * RPW; rb < n; rb += nw * RPW) {   // warp-uniform trip count
+    const int64_t r = rb + sub;
+    float s = 0.f;
+    if (r < n) {
+      const int64_t e1 = rowptr[r + 1];
+      int64_t e = rowptr[r] + gl;
+      for (; e + 3 * G < e1; e += 4 * G) {   // 4 independent entries in flight per lane
+        int32_t c[4];
+        float v[4], xv[4];
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          c[u] = col[e + u * G];
+          v[u] = val[e + u * G];
+        }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+        for (int u = 0; u < 4; ++u) s = fmaf(v[u], xv[u], s);
+      }
+      for (; e < e1; e += G) s = fmaf(val[e], __ldg(x + col[e]), s);
+    }
+#pragma unroll
+    for (int o = G / 2; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (r < n && gl == 0) {
+      y[r] = s;
+      dot = fmaf(s, x[r], dot);
+    }
+  }
+  if (partial) {
+    const double t = block_sum_d((double)dot, sh);
+    if (threadIdx.x == 0) partial[blockIdx.x] = t;
+  }
+}
+
 // diagonal of the FP32 operator -> its inverse
 __global__ void k_mx_dinv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
                           const double* __restrict__ val, float* __restrict__ dinv) {
@@ -312,6 +359,10 @@ int mixed_setup(gd_asm* A) {
   }
   if (n > 0) k_mx_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dinv);
   GD_CUDA_TRY(cudaGetLastError());
+  {   // lanes per row of the FP32 CSR operator, from the average row length
+    const int64_t avg = n > 0 ? A->nnz_own / n : 0;
+    M.csr_lanes = avg >= 256 ? 32 : avg >= 96 ? 16 : avg >= 48 ? 8 : 1;
+  }
   M.numeric_epoch = A->numeric_epoch;
   M.ready = true;
   return GD_OK;
@@ -324,6 +375,12 @@ int mixed_apply(gd_asm* A, const float* x, float* y, double* partial, cudaStream
   if (M.matrix_free)
     k_mf_apply<<<gb, kMxThreads, 0, st>>>(A->test->geom, n, A->row_node.p, M.node_gid.p, M.wf.p, M.ratio, x, y,
                                           partial);
+  else if (M.csr_lanes == 32)
+    k_csr32_apply_g<32><<<gb, kMxThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, M.vals32.p, x, y, partial);
+  else if (M.csr_lanes == 16)
+    k_csr32_apply_g<16><<<gb, kMxThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, M.vals32.p, x, y, partial);
+  else if (M.csr_lanes == 8)
+    k_csr32_apply_g<8><<<gb, kMxThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, M.vals32.p, x, y, partial);
   else
     k_csr32_apply<<<gb, kMxThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, M.vals32.p, x, y, partial);
   GD_CUDA_TRY(cudaGetLastError());
