@@ -288,22 +288,36 @@ __device__ __forceinline__ bool bad_coefficient(double k) {
 // Each thread streams 4 cells as two 16-byte loads issued together (one 8-byte load in
 // flight per thread would cap the kernel near 2.5 TB/s); kappa must be 16-byte aligned
 // (w always is), otherwise k_prescale_scalar runs.
-__global__ void k_prescale(int64_t ncells, const double* __restrict__ kappa, double scale, double* __restrict__ w,
-                           int32_t* __restrict__ bad) {
+// w = scale * kappa per cell with the coefficient check; 16-byte accesses, four of them in
+// flight per thread (8 cells), kappa read with streaming loads (not reused) so that w,
+// which the matrix kernel reads next, keeps the L2.
+__global__ void __launch_bounds__(256)
+k_prescale(int64_t ncells, const double* __restrict__ kappa, double scale, double* __restrict__ w,
+           int32_t* __restrict__ bad) {
   int nbad = 0;
-  const int64_t n4 = ncells >> 2;
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n4; i += (int64_t)gridDim.x * blockDim.x) {
-    const double2 a = __ldg(reinterpret_cast<const double2*>(kappa) + 2 * i);
-    const double2 b = __ldg(reinterpret_cast<const double2*>(kappa) + 2 * i + 1);
-    nbad += bad_coefficient(a.x) + bad_coefficient(a.y) + bad_coefficient(b.x) + bad_coefficient(b.y);
-    reinterpret_cast<double2*>(w)[2 * i] = make_double2(scale * a.x, scale * a.y);
-    reinterpret_cast<double2*>(w)[2 * i + 1] = make_double2(scale * b.x, scale * b.y);
+  const int64_t n2 = ncells >> 1;   // double2 units
+  const double2* k2 = reinterpret_cast<const double2*>(kappa);
+  double2* w2 = reinterpret_cast<double2*>(w);
+  const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+  for (int64_t i0 = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i0 < n2; i0 += 4 * stride) {
+    double2 a[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t i = i0 + u * stride;
+      a[u] = i < n2 ? __ldcs(k2 + i) : make_double2(1.0, 1.0);
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int64_t i = i0 + u * stride;
+      if (i >= n2) break;
+      nbad += bad_coefficient(a[u].x) + bad_coefficient(a[u].y);
+      w2[i] = make_double2(scale * a[u].x, scale * a[u].y);
+    }
   }
-  if (blockIdx.x == 0 && threadIdx.x < (ncells & 3)) {   // tail
-    const int64_t i = (n4 << 2) + threadIdx.x;
-    const double k = kappa[i];
+  if (blockIdx.x == 0 && threadIdx.x == 0 && (ncells & 1)) {   // tail
+    const double k = kappa[ncells - 1];
     nbad += bad_coefficient(k);
-    w[i] = scale * k;
+    w[ncells - 1] = scale * k;
   }
   if (nbad) atomicAdd(bad, nbad);
 }
@@ -698,7 +712,7 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
   if (cube) {   // w = Kc[3] * kappa, validated on the way
     if (A->w_cells.n != (size_t)ncells) GD_TRY(dalloc(A->w_cells, ncells));
     if (((uintptr_t)kappa & 15) == 0) {
-      const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((ncells / 4 + 255) / 256, 8192));
+      const int blocks = (int)std::max<int64_t>(1, std::min<int64_t>((ncells / 8 + 255) / 256, 152 * 8));
       k_prescale<<<blocks, 256, 0, st>>>(ncells, kappa, q.Kc[3], A->w_cells.p, bad);
     } else {
       const int blocks = (int)std::min<int64_t>((ncells + 255) / 256, 4096);
