@@ -374,7 +374,10 @@ k_lat_dots(int nlat, const float* __restrict__ r, const float* __restrict__ z, c
 // limit is only ever reached if the launch was not co-resident.)
 
 constexpr unsigned long long kLatSyncTimeoutNs = 2000000000ull;   // 2 s per barrier
-constexpr int kPadBlocksPerSM = 3;   // k_pad_cg: 80 registers per thread
+// k_pad_cg: one block of 768 threads per SM (80 registers per thread): 152 arrivals per
+// grid barrier instead of 456 with 3 blocks of 256, the same 24 warps per SM
+constexpr int kPadThreads = 768;
+constexpr int kPadBlocksPerSM = 1;
 
 __device__ __forceinline__ unsigned long long lat_globaltimer() {
   unsigned long long t;
@@ -432,7 +435,7 @@ __device__ __forceinline__ bool lat_tag_is(unsigned long long w, unsigned epoch)
 // blocks still waiting see it (checked every 256 polls), and all return false.
 template <int NV, int W>
 __device__ bool lat_allreduce(LatRed* R, const float (&f)[NV], unsigned nb, unsigned epoch, float (&out)[NV]) {
-  __shared__ float wsum[NV][kLatThreads / 32];
+  __shared__ float wsum[NV][32];   // up to 32 warps per block
   __shared__ int last_s, ok_s;
   __shared__ unsigned long long w_s[NV];
   LatSync* S = &R->sync;
@@ -787,7 +790,7 @@ __device__ __forceinline__ void pad_update(const PadGeom& pg, float alpha, float
 // barrier/all-reduces per step (p.q; r.z and r.r), so every block holds the same alpha,
 // beta and r.r and takes the same exit.  Block 0 writes the step count and the final
 // scalars.
-__global__ void __launch_bounds__(kLatThreads, kPadBlocksPerSM)
+__global__ void __launch_bounds__(kPadThreads, kPadBlocksPerSM)
 k_pad_cg(PadGeom pg, const float* __restrict__ wpad, float ratio, float* x, float* r, float* z, float* p, float* q,
          const float* __restrict__ dpad, LatRed* R, int max_it, double tol2) {
   const unsigned nb = gridDim.x;
@@ -876,10 +879,9 @@ static int lat_grid(int64_t n) {
   return (int)(b < 1 ? 1 : b);
 }
 
-// Cooperative grid of k_pad_cg: the same number of blocks on every SM (all the blocks
-// that stay resident, kPadBlocksPerSM by the register bound), so that equal chunks mean
-// equal work per SM; fewer for small lattices.  0 when the device cannot launch
-// cooperatively.
+// Cooperative grid of k_pad_cg: the same number of blocks on every SM (kPadBlocksPerSM,
+// resident by the register bound), so that equal chunks mean equal work per SM; fewer for
+// small lattices.  0 when the device cannot launch cooperatively.
 static int lat_coop_grid(int64_t ngroups) {
   static int cap[64] = {0};   // 0: not yet queried, -1: no cooperative launch
   int dev = 0;
@@ -888,12 +890,12 @@ static int lat_coop_grid(int64_t ngroups) {
     int coop = 0, sms = 0, per = 0;
     if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess) coop = 0;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) sms = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pad_cg, kLatThreads, 0) != cudaSuccess) per = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pad_cg, kPadThreads, 0) != cudaSuccess) per = 0;
     cudaGetLastError();
     cap[dev] = coop && sms > 0 && per > 0 ? std::min(std::min(per, kPadBlocksPerSM) * sms, kLatMaxBlocks) : -1;
   }
   if (cap[dev] < 0) return 0;
-  int64_t b = (ngroups + kLatThreads - 1) / kLatThreads;
+  int64_t b = (ngroups + kPadThreads - 1) / kPadThreads;
   if (b > cap[dev]) b = cap[dev];
   return (int)(b < 1 ? 1 : b);
 }
@@ -1013,7 +1015,7 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
       int mi = inner_max;
       double t2 = tol_in * tol_in;
       void* args[] = {&pga, &wpad, &rat, &px, &pr, &pz, &pp, &pq, &dpad, &R, &mi, &t2};
-      GD_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_pad_cg, dim3(gc), dim3(kLatThreads), args, 0, st));
+      GD_CUDA_TRY(cudaLaunchCooperativeKernel((const void*)k_pad_cg, dim3(gc), dim3(kPadThreads), args, 0, st));
       LatSync hs{};
       GD_CUDA_TRY(cudaMemcpyAsync(&hs, &R->sync, sizeof(hs), cudaMemcpyDeviceToHost, st));
       GD_CUDA_TRY(cudaStreamSynchronize(st));
