@@ -434,7 +434,8 @@ __device__ __forceinline__ bool lat_tag_is(unsigned long long w, unsigned epoch)
 // totals.  The wait is bounded by wall time: past the limit a block sets the error flag,
 // blocks still waiting see it (checked every 256 polls), and all return false.
 template <int NV, int W>
-__device__ bool lat_allreduce(LatRed* R, const float (&f)[NV], unsigned nb, unsigned epoch, float (&out)[NV]) {
+__device__ bool lat_allreduce(LatRed* R, const float (&f)[NV], unsigned nb, unsigned epoch, float (&out)[NV],
+                              unsigned long long timeout_ns = kLatSyncTimeoutNs) {
   __shared__ float wsum[NV][32];   // up to 32 warps per block
   __shared__ int last_s, ok_s;
   __shared__ unsigned long long w_s[NV];
@@ -515,7 +516,7 @@ __device__ bool lat_allreduce(LatRed* R, const float (&f)[NV], unsigned nb, unsi
             ok = 0;
             break;
           }
-          if (lat_globaltimer() - t0 > kLatSyncTimeoutNs) {
+          if (lat_globaltimer() - t0 > timeout_ns) {
             atomicExch(&S->err, 1);
             ok = 0;
             break;
@@ -1128,3 +1129,41 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
 }
 
 }  // namespace gd
+
+namespace gd {
+
+// One grid all-reduce across the launched blocks, waiting for `expected` arrivals: with
+// expected > gridDim.x the last arrival never comes and every block's wait runs out
+// after timeout_ns (a flag nothing sets), which is how the bounded wait is tested.
+__global__ void k_barrier_probe(LatRed* R, unsigned expected, unsigned long long timeout_ns) {
+  const float f[1] = {1.0f};
+  float out[1];
+  lat_allreduce<1, 0>(R, f, expected, 1u, out, timeout_ns);
+}
+
+}  // namespace gd
+
+using namespace gd;
+
+// Diagnostics: exercises the bounded wait of the persistent kernels' grid barrier.
+extern "C" int gd_debug_barrier_probe(gd_ctx* ctx, int blocks, int expected, double timeout_s) {
+  if (!ctx || blocks < 1 || blocks > 152 || expected < 1 || !(timeout_s > 0.0) || timeout_s > 5.0)
+    return fail(GD_ERR_ARG, "gd_debug_barrier_probe: 1..152 blocks, expected >= 1, 0 < timeout <= 5 s");
+  cudaStream_t st = ctx->stream;
+  DBuf<double> buf;
+  GD_TRY(dalloc(buf, (sizeof(LatRed) + sizeof(double) - 1) / sizeof(double)));
+  LatRed* R = reinterpret_cast<LatRed*>(buf.p);
+  unsigned ex = (unsigned)expected;
+  unsigned long long tns = (unsigned long long)(timeout_s * 1e9);
+  void* args[] = {&R, &ex, &tns};
+  cudaError_t e = cudaMemsetAsync(buf.p, 0, sizeof(LatRed), st);
+  if (e == cudaSuccess)
+    e = cudaLaunchCooperativeKernel((const void*)k_barrier_probe, dim3(blocks), dim3(kLatThreads), args, 0, st);
+  LatSync hs{};
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&hs, &R->sync, sizeof(hs), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  dfreeb(buf);
+  if (e != cudaSuccess) return fail(GD_ERR_CUDA, std::string("gd_debug_barrier_probe: ") + cudaGetErrorString(e));
+  if (hs.err) return fail(GD_ERR_TIMEOUT, "gd_debug_barrier_probe: the grid barrier wait ran out");
+  return GD_OK;
+}

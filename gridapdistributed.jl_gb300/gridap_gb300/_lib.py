@@ -145,6 +145,7 @@ SIGNATURES = {
     "gd_dg_spmv": [P, P, P, C.c_int],
     "gd_dg_solve": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_dg_l2_error": [P, P, P, C.c_int, C.c_int, DP],
+    "gd_debug_barrier_probe": [P, C.c_int, C.c_int, C.c_double],
 }
 _RESTYPES = {"gd_last_error": C.c_char_p, "gd_version": C.c_char_p}
 

@@ -396,6 +396,12 @@ int gd_dg_solve(gd_dgspace* s, double rtol, int maxit, double* x, int where, gd_
 /* sqrt(sum(int (u - uh)^2 dOmega)): u at the cells' Gauss points (layout of f_qp) */
 int gd_dg_l2_error(const gd_dgspace* s, const double* x, const double* u_qp, int degree, int where, double* err);
 
+/* Diagnostics (no reference counterpart): launches `blocks` blocks of the persistent
+ * kernels' grid barrier waiting for `expected` arrivals.  expected > blocks makes the
+ * bounded wait run out after timeout_s (<= 5 s): GD_ERR_TIMEOUT, the context stays
+ * usable; expected == blocks: GD_OK. */
+int gd_debug_barrier_probe(gd_ctx* ctx, int blocks, int expected, double timeout_s);
+
 #ifdef __cplusplus
 }
 #endif
