@@ -285,12 +285,10 @@ __device__ __forceinline__ bool bad_coefficient(double k) {
 // Cube cells: w_c = Kc[3] * kappa_c once per cell (validated here), so a 3D row needs
 // 12 adds for the face diagonals, 3 adds + 1 multiply for the diagonal, and nothing
 // for the corners (w itself) and the edge neighbours (exactly 0 on a cube).
-// Each thread streams 4 cells as two 16-byte loads issued together (one 8-byte load in
-// flight per thread would cap the kernel near 2.5 TB/s); kappa must be 16-byte aligned
-// (w always is), otherwise k_prescale_scalar runs.
 // w = scale * kappa per cell with the coefficient check; 16-byte accesses, four of them in
 // flight per thread (8 cells), kappa read with streaming loads (not reused) so that w,
-// which the matrix kernel reads next, keeps the L2.
+// which the matrix kernel reads next, keeps the L2.  kappa must be 16-byte aligned (w
+// always is), otherwise k_prescale_scalar runs.
 __global__ void __launch_bounds__(256)
 k_prescale(int64_t ncells, const double* __restrict__ kappa, double scale, double* __restrict__ w,
            int32_t* __restrict__ bad) {

@@ -59,6 +59,8 @@ CASES = [
     dict(dim=2, n=(6, 4), parts=(2, 2), order=1, sides=(0, 1, 1, 0), seed=11, f_nodal=True,
          u=lambda x, y: 1.0 + x * y),
     dict(dim=3, n=(7, 6, 5), parts=(3, 2, 1), order=1, seed=12, u=lambda x, y, z: 2.0 - x),
+    # cube cells, an odd number of them (the coefficient scaling's last single cell)
+    dict(dim=3, n=(5, 3, 7), parts=(1, 1, 2), order=1, seed=13, domain=(0, 1.25, 0, 0.75, 0, 1.75)),
 ]
 
 
