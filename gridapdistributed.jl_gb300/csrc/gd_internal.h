@@ -164,10 +164,43 @@ int launch_rows_table(gd_asm* A, const double* kappa, const double* table, doubl
 int launch_rhs_table(gd_asm* A, const double* kappa, const double* table, double f_const, double* rhs, int32_t* bad,
                      cudaStream_t st);
 int reference_element(gd_asm* A, int degree);
-// FP64 Jacobi-PCG on the owned rows of a CSR with global column ids (gd_solve.cu)
+// Sliced-ELL copy of a CSR's rows for the FP64 solver (gd_solve.cu): slices of 32 rows,
+// stored entry k of row r at 32 off[r / 32] + 32 k + r % 32, so the 32 threads of a warp
+// (one row each) read their k-th entries from one contiguous 256-byte line.  Exact zeros
+// are dropped; the other entries keep their CSR order, so a row's sum is bit-identical to
+// the CSR kernel's.  version: the matrix values it was built from (-1: none).
+struct SellMat {
+  DBuf<int64_t> off;     // per slice, in units of 32 entries (nslices + 1)
+  DBuf<int32_t> width;   // per slice: its longest stored row
+  DBuf<int32_t> len;     // per row: stored entries
+  DBuf<double> val;
+  DBuf<int32_t> col;
+  int64_t n = -1, version = -1;
+  void release() {
+    dfreeb(off);
+    dfreeb(width);
+    dfreeb(len);
+    dfreeb(val);
+    dfreeb(col);
+    n = -1;
+    version = -1;
+  }
+};
+// Rows short enough for one thread per row (average below 48 entries) go through the
+// sliced-ELL copy; longer ones use lane groups on the CSR itself.
+inline bool sell_suits(int64_t n, int64_t nnz) { return n > 0 && nnz / n < 48; }
+int sell_build(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, SellMat& S, int64_t version,
+               cudaStream_t st);
+
+// FP64 Jacobi-PCG on the owned rows of a CSR with global column ids (gd_solve.cu).  sell:
+// the caller's cached sliced-ELL copy for matrix version `version` (null: a temporary one).
 int jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals, const double* rhs,
                    DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
-                   double* x, int where, gd_solve_stats* stats);
+                   double* x, int where, gd_solve_stats* stats, SellMat* sell = nullptr, int64_t version = -1);
+// r = b - A x over the assembler's owned rows with partials of r.r and b.b (the
+// sliced-ELL copy where it suits, the CSR otherwise); *nblocks partials each.
+int residual_fp64_asm(gd_asm* A, const double* x, const double* b, double* r, double* prr, double* pbb,
+                      cudaStream_t st, int* nblocks);
 
 }  // namespace gd
 
@@ -317,4 +350,5 @@ struct gd_asm {
   gd::DBuf<double> w;              // vectors
   gd::DBuf<double> dred;           // reduction partials
   gd::DBuf<double> dinv;
+  gd::SellMat sell;                // sliced-ELL copy of the owned rows (FP64 solves)
 };

@@ -974,8 +974,7 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
   int status = GD_OK;
   while (true) {
     int gr = 0;
-    GD_TRY(residual_fp64(n, A->rowptr.p, A->colgid.p, A->vals.p, x64, A->rhs_override ? A->rhs_override : A->rhs.p,
-                         r64, pa, pbb, st, &gr));
+    GD_TRY(residual_fp64_asm(A, x64, A->rhs_override ? A->rhs_override : A->rhs.p, r64, pa, pbb, st, &gr));
     double h2[2];
     GD_TRY(sum_partials_host(pa, pbb, gr, h2, st));
     const double rnorm = std::sqrt(h2[0]);

@@ -20,6 +20,7 @@ namespace gd {
 constexpr int kSpmvThreads = 128;                // one row per thread
 constexpr int kRowsPerSpmvBlock = kSpmvThreads;
 constexpr int kSpmvCap = 3584;                   // staged entries per chunk (43 KB)
+constexpr int kStageBatch = 8;                   // staging loads per thread in flight
 constexpr int kVecThreads = 256;
 constexpr int kMaxPartials = 1024;             // blocks that write partial sums
 
@@ -80,13 +81,40 @@ __device__ __forceinline__ void csr_rows(int64_t n, const int64_t* __restrict__ 
     for (int64_t c0 = E0; c0 < E1; c0 += kSpmvCap) {
       const int cn = (int)(E1 - c0 < kSpmvCap ? E1 - c0 : kSpmvCap);
       __syncthreads();   // the previous chunk has been consumed
-      for (int i = threadIdx.x; i < cn; i += kSpmvThreads) {
-        sval[i] = val[c0 + i];
-        scol[i] = col[c0 + i];
+      // 8 values and 8 column ids per thread in flight at once (a chunk is at most 28 per
+      // thread): the loads of one round, then the stores
+      for (int i0 = threadIdx.x; i0 < cn; i0 += kStageBatch * kSpmvThreads) {
+        double v[kStageBatch];
+        int32_t c[kStageBatch];
+#pragma unroll
+        for (int u = 0; u < kStageBatch; ++u) {
+          const int i = i0 + u * kSpmvThreads;
+          if (i < cn) {
+            v[u] = __ldcs(val + c0 + i);
+            c[u] = __ldcs(col + c0 + i);
+          }
+        }
+#pragma unroll
+        for (int u = 0; u < kStageBatch; ++u) {
+          const int i = i0 + u * kSpmvThreads;
+          if (i < cn) {
+            sval[i] = v[u];
+            scol[i] = c[u];
+          }
+        }
       }
       __syncthreads();
-      const int64_t lo = rs > c0 ? rs : c0, hi = re < c0 + cn ? re : c0 + cn;
-      for (int64_t e = lo; e < hi; ++e) acc = fma(sval[e - c0], __ldg(x + scol[e - c0]), acc);
+      const int lo = (int)((rs > c0 ? rs : c0) - c0), hi = (int)((re < c0 + cn ? re : c0 + cn) - c0);
+      // 8 gathers of x in flight before their FMAs (the row's FMA order is unchanged)
+      int e = lo;
+      for (; e + 8 <= hi; e += 8) {
+        double xv[8];
+#pragma unroll
+        for (int u = 0; u < 8; ++u) xv[u] = __ldg(x + scol[e + u]);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc = fma(sval[e + u], xv[u], acc);
+      }
+      for (; e < hi; ++e) acc = fma(sval[e], __ldg(x + scol[e]), acc);
     }
     if (valid) {
       if (MODE == 0) {
@@ -103,8 +131,9 @@ __device__ __forceinline__ void csr_rows(int64_t n, const int64_t* __restrict__ 
   }
 }
 
-// y = A x over owned rows; optional partial dot(y, w) per block
-__global__ void __launch_bounds__(kSpmvThreads)
+// y = A x over owned rows; optional partial dot(y, w) per block.  Shared memory allows 5
+// blocks per SM; the launch bound keeps the registers within that too.
+__global__ void __launch_bounds__(kSpmvThreads, 5)
 k_spmv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
        const double* __restrict__ val, const double* __restrict__ x, double* __restrict__ y,
        const double* __restrict__ w, double* __restrict__ partial) {
@@ -118,7 +147,7 @@ k_spmv(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict_
 }
 
 // r = b - A x (partials of r.r and b.b)
-__global__ void __launch_bounds__(kSpmvThreads)
+__global__ void __launch_bounds__(kSpmvThreads, 5)
 k_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
            const double* __restrict__ val, const double* __restrict__ x, const double* __restrict__ b,
            double* __restrict__ r_out, double* __restrict__ partial_rr, double* __restrict__ partial_bb) {
@@ -129,6 +158,116 @@ k_residual(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restr
   if (threadIdx.x == 0) partial_rr[blockIdx.x] = t;
   t = block_sum_serial(bb, sh);
   if (threadIdx.x == 0) partial_bb[blockIdx.x] = t;
+}
+
+// ---------------------------------------------------------------------------------
+// Sliced ELL (short rows): one thread per row, the warp's 32 rows read their k-th entries
+// as one coalesced 256-byte line, with no shared-memory staging and no block barrier, so
+// the blocks stay resident at full occupancy and the FP64 FMAs overlap the HBM stream.
+// ---------------------------------------------------------------------------------
+constexpr int kSellThreads = 256;
+
+// stored entries per row (the non-zeros) and each 32-row slice's longest row
+__global__ void k_sell_len(int64_t n, const int64_t* __restrict__ rowptr, const double* __restrict__ val,
+                           int32_t* __restrict__ len, int32_t* __restrict__ width) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int c = 0;
+  if (r < n) {
+    for (int64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) c += val[e] != 0.0;
+    len[r] = c;
+  }
+  int m = c;
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0 && r < n) width[r >> 5] = m;   // lane 0 holds the slice's first row
+}
+
+__global__ void k_sell_fill(int64_t n, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ col,
+                            const double* __restrict__ val, const int64_t* __restrict__ off, double* __restrict__ sval,
+                            int32_t* __restrict__ scol) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= n) return;
+  const int64_t base = 32 * off[r >> 5] + (r & 31);
+  int64_t k = 0;
+  for (int64_t e = rowptr[r]; e < rowptr[r + 1]; ++e) {
+    const double v = val[e];
+    if (v != 0.0) {
+      sval[base + 32 * k] = v;
+      scol[base + 32 * k] = col[e];
+      ++k;
+    }
+  }
+}
+
+// MODE 0: y = A x with the partial of y.w per block (w may be null); MODE 1: r = b - A x
+// (r may be null) with the partials of r.r and b.b.  A row's products are summed in CSR
+// order, four loads of the row in flight at a time.
+template <int MODE>
+__global__ void __launch_bounds__(kSellThreads)
+k_sell_rows(int64_t n, const int64_t* __restrict__ off, const int32_t* __restrict__ len,
+            const double* __restrict__ sval, const int32_t* __restrict__ scol, const double* __restrict__ x,
+            const double* __restrict__ b, double* __restrict__ out, const double* __restrict__ w,
+            double* __restrict__ p1, double* __restrict__ p2) {
+  __shared__ double sh[32];
+  double s1 = 0.0, s2 = 0.0;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t base = 32 * off[r >> 5] + (r & 31);
+    const double* pv = sval + base;
+    const int32_t* pc = scol + base;
+    const int L = len[r];
+    double acc = 0.0;
+    int k = 0;
+    for (; k + 4 <= L; k += 4) {
+      double v[4], xv[4];
+      int32_t c[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        v[u] = __ldcs(pv + 32 * (k + u));
+        c[u] = __ldcs(pc + 32 * (k + u));
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u) xv[u] = __ldg(x + c[u]);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) acc = fma(v[u], xv[u], acc);
+    }
+    for (; k < L; ++k) acc = fma(__ldcs(pv + 32 * k), __ldg(x + __ldcs(pc + 32 * k)), acc);
+    if (MODE == 0) {
+      out[r] = acc;
+      if (w) s1 = fma(acc, w[r], s1);
+    } else {
+      const double bv = b[r];
+      const double rv = bv - acc;
+      if (out) out[r] = rv;
+      s1 = fma(rv, rv, s1);
+      s2 = fma(bv, bv, s2);
+    }
+  }
+  if (p1) {
+    const double t = block_sum(s1, sh);
+    if (threadIdx.x == 0) p1[blockIdx.x] = t;
+  }
+  if (MODE == 1 && p2) {
+    const double t = block_sum(s2, sh);
+    if (threadIdx.x == 0) p2[blockIdx.x] = t;
+  }
+}
+
+// grid-stride over the rows with only as many blocks as are resident at once (and at most
+// kMaxPartials, the partial sums the scalar kernels read)
+static int sell_grid(int64_t n) {
+  static int resident[64] = {0};
+  int64_t b = std::max<int64_t>(1, std::min<int64_t>((n + kSellThreads - 1) / kSellThreads, kMaxPartials));
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess && dev >= 0 && dev < 64) {
+    if (!resident[dev]) {
+      int sms = 0, per_sm = 0;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_sell_rows<1>, kSellThreads, 0);
+      cudaGetLastError();
+      resident[dev] = sms * per_sm > 0 ? sms * per_sm : kMaxPartials;
+    }
+    if (b > resident[dev]) b = resident[dev];
+  }
+  return (int)b;
 }
 
 // Long rows (vector and high-order systems: 81 to 375 entries): G lanes per row, each lane
@@ -321,6 +460,36 @@ int residual_fp64(int64_t n, const int64_t* rowptr, const int32_t* col, const do
   return GD_OK;
 }
 
+int sell_build(int64_t n, const int64_t* rowptr, const int32_t* col, const double* val, SellMat& S, int64_t version,
+               cudaStream_t st) {
+  if (version >= 0 && S.version == version && S.n == n) return GD_OK;
+  S.version = -1;
+  if (n <= 0) {
+    S.n = n;
+    S.version = version;
+    return GD_OK;
+  }
+  const int64_t ns = (n + 31) / 32;
+  if (S.len.n < (size_t)n) GD_TRY(dalloc(S.len, n));
+  if (S.width.n < (size_t)ns) GD_TRY(dalloc(S.width, ns));
+  if (S.off.n < (size_t)(ns + 1)) GD_TRY(dalloc(S.off, ns + 1));
+  const unsigned gb = (unsigned)((n + kSellThreads - 1) / kSellThreads);
+  k_sell_len<<<gb, kSellThreads, 0, st>>>(n, rowptr, val, S.len.p, S.width.p);
+  GD_CUDA_TRY(cudaGetLastError());
+  GD_TRY(exclusive_scan_i32(S.width.p, S.off.p, ns, st));
+  int64_t total = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&total, S.off.p + ns, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  const size_t ne = (size_t)std::max<int64_t>(32 * total, 1);
+  if (S.val.n < ne) GD_TRY(dalloc(S.val, ne));
+  if (S.col.n < ne) GD_TRY(dalloc(S.col, ne));
+  k_sell_fill<<<gb, kSellThreads, 0, st>>>(n, rowptr, col, val, S.off.p, S.val.p, S.col.p);
+  GD_CUDA_TRY(cudaGetLastError());
+  S.n = n;
+  S.version = version;
+  return GD_OK;
+}
+
 static int grid_for(int64_t n, int per_block) {
   int64_t b = (n + per_block - 1) / per_block;
   if (b > kMaxPartials) b = kMaxPartials;
@@ -340,6 +509,20 @@ static int grid_for(int64_t n, int per_block) {
     }
   }
   return (int)b;
+}
+
+int residual_fp64_asm(gd_asm* A, const double* x, const double* b, double* r, double* prr, double* pbb,
+                      cudaStream_t st, int* nblocks) {
+  const int64_t n = A->ngdofs;
+  if (!sell_suits(n, A->nnz_own))
+    return residual_fp64(n, A->rowptr.p, A->colgid.p, A->vals.p, x, b, r, prr, pbb, st, nblocks);
+  GD_TRY(sell_build(n, A->rowptr.p, A->colgid.p, A->vals.p, A->sell, A->numeric_epoch, st));
+  const int gs = sell_grid(n);
+  k_sell_rows<1><<<gs, kSellThreads, 0, st>>>(n, A->sell.off.p, A->sell.len.p, A->sell.val.p, A->sell.col.p, x, b, r,
+                                              nullptr, prr, pbb);
+  GD_CUDA_TRY(cudaGetLastError());
+  *nblocks = gs;
+  return GD_OK;
 }
 
 }  // namespace gd
@@ -386,16 +569,18 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
   if (method != GD_SOLVE_JACOBI_PCG) return fail(GD_ERR_UNSUPPORTED, "gd_solve: unknown method");
   if (!x || !(rtol > 0.0) || maxit < 0) return fail(GD_ERR_ARG, "gd_solve: bad argument");
   return jacobi_pcg_csr(A->ngdofs, A->rowptr.p, A->colgid.p, A->vals.p, A->rhs_override ? A->rhs_override : A->rhs.p,
-                        A->w, A->dinv, A->dred, A->test->model->ctx->stream, rtol, maxit, x, where, stats);
+                        A->w, A->dinv, A->dred, A->test->model->ctx->stream, rtol, maxit, x, where, stats, &A->sell,
+                        A->numeric_epoch);
 }
 
 // FP64 Jacobi-PCG on the owned rows of a CSR (global column ids); workspace buffers are
 // (re)allocated as needed: w (5 n: x r z p q), dinv (n), dred (partials and scalars).
 int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals, const double* rhs,
                    DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
-                   double* x, int where, gd_solve_stats* stats) {
+                   double* x, int where, gd_solve_stats* stats, SellMat* sell, int64_t version) {
   auto t0 = std::chrono::steady_clock::now();
-  // rows per lane group from the average row length (thread per row below 48 entries)
+  // rows per lane group from the average row length; below 48 entries one thread per row
+  // on the sliced-ELL copy (the caller's cached one, else a temporary freed on return)
   int64_t nnz = 0;
   if (n) {
     GD_CUDA_TRY(cudaMemcpyAsync(&nnz, rowptr + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
@@ -403,7 +588,16 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
   }
   const int64_t avg = n ? nnz / n : 0;
   const int G = avg >= 256 ? 32 : avg >= 96 ? 16 : avg >= 48 ? 8 : 1;
-  const int gsg = G == 1 ? grid_for(n, kRowsPerSpmvBlock)
+  SellMat local;
+  struct Release {
+    SellMat* m;
+    ~Release() {
+      if (m) m->release();
+    }
+  } release_local{sell ? nullptr : &local};
+  SellMat* S = sell ? sell : &local;
+  if (G == 1) GD_TRY(sell_build(n, rowptr, colgid, vals, *S, sell ? version : -1, st));
+  const int gsg = G == 1 ? sell_grid(n)
                          : (int)std::max<int64_t>(1, std::min<int64_t>((n * G + kSpmvThreads - 1) / kSpmvThreads,
                                                                        kMaxPartials));
   auto spmv = [&](const double* xin, double* yout, const double* wdot, double* part) {
@@ -411,7 +605,9 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
       case 32: k_spmv_g<32><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
       case 16: k_spmv_g<16><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
       case 8: k_spmv_g<8><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part); break;
-      default: k_spmv<<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, yout, wdot, part);
+      default:
+        k_sell_rows<0><<<gsg, kSellThreads, 0, st>>>(n, S->off.p, S->len.p, S->val.p, S->col.p, xin, nullptr, yout,
+                                                     wdot, part, nullptr);
     }
   };
   auto residual = [&](const double* xin, double* rout, double* prr, double* pbb) {
@@ -419,7 +615,9 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
       case 32: k_residual_g<32><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
       case 16: k_residual_g<16><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
       case 8: k_residual_g<8><<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb); break;
-      default: k_residual<<<gsg, kSpmvThreads, 0, st>>>(n, rowptr, colgid, vals, xin, rhs, rout, prr, pbb);
+      default:
+        k_sell_rows<1><<<gsg, kSellThreads, 0, st>>>(n, S->off.p, S->len.p, S->val.p, S->col.p, xin, rhs, rout,
+                                                     nullptr, prr, pbb);
     }
   };
   if (w.n < (size_t)(5 * n)) GD_TRY(dalloc(w, 5 * std::max<int64_t>(n, 1)));

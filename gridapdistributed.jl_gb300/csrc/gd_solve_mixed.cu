@@ -424,8 +424,7 @@ int mixed_solve(gd_asm* A, double rtol, int maxit, double* x_out, int where, gd_
   while (true) {
     // FP64 residual of the current iterate
     int gr = 0;
-    GD_TRY(residual_fp64(n, A->rowptr.p, A->colgid.p, A->vals.p, x64, A->rhs_override ? A->rhs_override : A->rhs.p,
-                         r64, pa, pb, st, &gr));
+    GD_TRY(residual_fp64_asm(A, x64, A->rhs_override ? A->rhs_override : A->rhs.p, r64, pa, pb, st, &gr));
     k_mx_scalars<<<1, kMxThreads, 0, st>>>(0, gr, pa, pb, nullptr, sc);
     GD_CUDA_TRY(cudaGetLastError());
     MxScalars h{};

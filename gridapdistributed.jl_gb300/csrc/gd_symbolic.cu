@@ -609,6 +609,7 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->w);
   dfreeb(A->dred);
   dfreeb(A->dinv);
+  A->sell.release();
   dfreeb(A->row_pat);
   dfreeb(A->pat);
   dfreeb(A->w_cells);
