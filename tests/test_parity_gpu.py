@@ -127,7 +127,10 @@ def test_solve_matches_gathered_lu(backend, case):
                                   # 11 blocks of the persistent kernel whose chunks start and end
                                   # mid-row, Dirichlet and natural sides mixed
                                   dict(dim=3, n=(35, 30, 28), parts=(2, 2, 1), order=1, seed=35,
-                                       sides=(1, 1, 0, 1, 1, 0), domain=(0, 4.375, 0, 3.75, 0, 3.5))],
+                                       sides=(1, 1, 0, 1, 1, 0), domain=(0, 4.375, 0, 3.75, 0, 3.5)),
+                                  # rows of 141 nodes over 8 blocks of the persistent kernel
+                                  dict(dim=3, n=(140, 30, 4), parts=(2, 1, 1), order=1, seed=37,
+                                       sides=(1, 0, 1, 1, 0, 1), domain=(0, 17.5, 0, 3.75, 0, 0.5))],
                          ids=case_id)
 def test_mixed_solver_matches_gathered_lu(backend, case):
     """FP64 refinement around FP32 CG (matrix-free on cube Q1, FP32 CSR otherwise)."""
