@@ -550,8 +550,23 @@ extern "C" int gd_spmv(gd_asm* A, const double* x, double* y, int where) {
     dx = tx.p;
     dy = ty.p;
   }
-  k_spmv<<<grid_for(n, kRowsPerSpmvBlock), kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, dy,
-                                                                  nullptr, nullptr);
+  if (sell_suits(n, A->nnz_own)) {   // the solver's sliced-ELL copy (built once per numeric assembly)
+    GD_TRY(sell_build(n, A->rowptr.p, A->colgid.p, A->vals.p, A->sell, A->numeric_epoch, st));
+    k_sell_rows<0><<<sell_grid(n), kSellThreads, 0, st>>>(n, A->sell.off.p, A->sell.len.p, A->sell.val.p,
+                                                          A->sell.col.p, dx, nullptr, dy, nullptr, nullptr, nullptr);
+  } else if (n > 0) {   // long rows: lane groups on the CSR, as in the solver
+    const int64_t avg = A->nnz_own / n;
+    const int G = avg >= 256 ? 32 : avg >= 96 ? 16 : 8;
+    const int gs = (int)std::max<int64_t>(1, std::min<int64_t>((n * G + kSpmvThreads - 1) / kSpmvThreads, kMaxPartials));
+    const int64_t* rp = A->rowptr.p;
+    const int32_t* cg = A->colgid.p;
+    const double* v = A->vals.p;
+    switch (G) {
+      case 32: k_spmv_g<32><<<gs, kSpmvThreads, 0, st>>>(n, rp, cg, v, dx, dy, nullptr, nullptr); break;
+      case 16: k_spmv_g<16><<<gs, kSpmvThreads, 0, st>>>(n, rp, cg, v, dx, dy, nullptr, nullptr); break;
+      default: k_spmv_g<8><<<gs, kSpmvThreads, 0, st>>>(n, rp, cg, v, dx, dy, nullptr, nullptr);
+    }
+  }
   GD_CUDA_TRY(cudaGetLastError());
   if (where == GD_HOST) GD_CUDA_TRY(cudaMemcpyAsync(y, dy, sizeof(double) * n, cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));

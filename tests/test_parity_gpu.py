@@ -101,6 +101,23 @@ def test_parity_against_oracle(backend, case, strategy):
         assert np.abs(b_parts[p] - M.b).max() <= VAL_TOL * scale
 
 
+@pytest.mark.parametrize("case", [CASES[6], CASES[14], CASES[7], CASES[8], CASES[2]], ids=case_id)
+def test_mul_matches_gathered_oracle(backend, case):
+    """A14 `mul!`: Q1 rows (the sliced-ELL copy, exact zeros of cube cells dropped) and Q2/Q3
+    rows (lane groups on the CSR) against the oracle's gathered matrix; twice, so the second
+    product reuses the cached copy.  |y - y_ref| <= 1e-12 * max |y_ref|."""
+    pb = make_problem(**case)
+    fe = go.build_fespace(pb)
+    A_ref, _ = go.gather_global(go.assemble(pb, fe, "sub"), fe.dofs[0].ngdofs)
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    rng = np.random.default_rng(17)
+    for _ in range(2):
+        x = rng.normal(size=fe.dofs[0].ngdofs)
+        y_ref = A_ref @ x
+        y = op.matrix.mul(x)
+        assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
+
+
 @pytest.mark.parametrize("case", [CASES[1], CASES[6], CASES[7]], ids=case_id)
 def test_solve_matches_gathered_lu(backend, case):
     pb = make_problem(**case)
