@@ -66,6 +66,56 @@ def parse():
     return ap.parse_args()
 
 
+def gpu_numa_node(local):
+    """NUMA node of the host CPUs attached to GPU `local` (its PCI device in sysfs), or None."""
+    try:
+        bus = subprocess.run(["nvidia-smi", "-i", str(local), "--query-gpu=pci.bus_id", "--format=csv,noheader"],
+                             capture_output=True, text=True, timeout=30).stdout.strip()
+    except (OSError, subprocess.SubprocessError):
+        return None
+    if ":" not in bus:
+        return None
+    dom, rest = bus.split(":", 1)   # nvidia-smi prints an 8-digit PCI domain, sysfs a 4-digit one
+    try:
+        names = [f"{int(dom, 16):04x}:{rest}".lower(), bus.lower()]
+    except ValueError:
+        return None
+    for name in names:
+        f = Path("/sys/bus/pci/devices") / name / "numa_node"
+        if f.exists():
+            try:
+                node = int(f.read_text().strip())
+            except ValueError:
+                return None
+            return node if node >= 0 else None
+    return None
+
+
+def bind_host_to_gpu(local):
+    """Run on the CPUs of the GPU's own NUMA node, so that the pinned host buffers of the
+    end-to-end measurement (first touched by this thread) sit next to the GPU; returns the
+    node, or None where the topology is not visible (nothing changed then)."""
+    node = gpu_numa_node(local)
+    if node is None:
+        return None
+    f = Path(f"/sys/devices/system/node/node{node}/cpulist")
+    if not f.exists():
+        return None
+    cpus = set()
+    for part in f.read_text().strip().split(","):
+        if not part:
+            continue
+        a, _, b = part.partition("-")
+        cpus.update(range(int(a), int(b or a) + 1))
+    if not cpus:
+        return None
+    try:
+        os.sched_setaffinity(0, cpus)
+    except OSError:
+        return None
+    return node
+
+
 def dist_env():
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -438,6 +488,7 @@ def run_gb300(args, rank, world, local):
     import gridap_gb300 as G
     from gridap_gb300 import _lib as L
 
+    host_node = bind_host_to_gpu(local)
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
     w, kappa = workload(args.cells)
@@ -613,7 +664,8 @@ def run_gb300(args, rank, world, local):
                                            "frac": mat_gbs / peak},
                          "rhs_kernel_ms": ms_rhs, "ghost_zero_ms": ms_zero},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": 8 * ncells,
-                    "d2h_bytes_per_step": 8 * nnz + 8 * ngdofs, "ms_per_step": 1e3 * e2e_s, "rhs_checksum": checksum},
+                    "d2h_bytes_per_step": 8 * nnz + 8 * ngdofs, "ms_per_step": 1e3 * e2e_s, "rhs_checksum": checksum,
+                    "host_numa_node": host_node},
             "gpu_launches": kernels_per_step * args.steps,
             "autotune": tuning,
             "clocks": clk,
