@@ -75,7 +75,7 @@ k_l2_error(Geom g, int64_t ncells, int bs, const int32_t* __restrict__ node_gid,
         }
         const int64_t lin = lattice_lin(g, X);
         const int32_t gid = node_gid[lin];
-        U[a] = gid >= 0 ? x[(int64_t)bs * gid + comp] : (u_dir ? u_dir[lin] : 0.0);
+        U[a] = gid >= 0 ? x[(int64_t)bs * gid + comp] : (u_dir ? u_dir[(int64_t)bs * lin + comp] : 0.0);
       }
       for (int q = 0; q < nqt; ++q) {
         int qi[3] = {0, 0, 0};

@@ -638,8 +638,7 @@ extern "C" int gd_space_set_dirichlet(gd_space* S, const double* u, int where) {
     S->has_dirichlet_values = false;
     return GD_OK;
   }
-  if (S->ncomp > 1) return fail(GD_ERR_UNSUPPORTED, "gd_space_set_dirichlet: vector spaces take homogeneous values");
-  int64_t n = 1;
+  int64_t n = S->ncomp > 1 ? S->ncomp : 1;   // values per lattice node
   for (int d = 0; d < S->geom.dim; ++d) n *= S->geom.N[d];
   GD_TRY(dalloc(S->u_dir, n));
   GD_CUDA_TRY(cudaMemcpyAsync(S->u_dir.p, u, sizeof(double) * n,

@@ -424,17 +424,67 @@ k_numeric_elasticity(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowp
   }
 }
 
-// rhs of owned vector row r = (node, c): force_c * int phi_node over the node's cells
+// Dirichlet lifting of owned vector row (node X, component c): minus the sum over the
+// node's cells of E_cell * Kel[(c NN + li) M + d NN + lj] * u_D(node lj, d) over the
+// cell's Dirichlet nodes lj and all components d (FESpaces.jl:703-715: b_e -= K_e[:,D] u_D).
+template <int DIM, int K>
+__device__ double elasticity_lifting(const Geom& g, int64_t lin, int c, const double* __restrict__ E,
+                                     const double* __restrict__ Kel, const double* __restrict__ u_dir) {
+  using L = Lat<DIM, K>;
+  constexpr int M = DIM * L::NN;
+  int64_t X[3] = {0, 0, 0};
+  for (int d = 0; d < DIM; ++d) {
+    X[d] = lin % g.N[d];
+    lin /= g.N[d];
+  }
+  int64_t clo[3] = {0, 0, 0}, chi[3] = {0, 0, 0};
+  for (int d = 0; d < DIM; ++d) {
+    const int64_t cc = X[d] / K;
+    if (X[d] % K == 0) {
+      clo[d] = cc - 1 < 0 ? 0 : cc - 1;
+      chi[d] = cc > g.n[d] - 1 ? g.n[d] - 1 : cc;
+    } else {
+      clo[d] = chi[d] = cc;
+    }
+  }
+  double b = 0.0;
+  for (int64_t cz = clo[2]; cz <= chi[2]; ++cz)
+    for (int64_t cy = clo[1]; cy <= chi[1]; ++cy)
+      for (int64_t cx = clo[0]; cx <= chi[0]; ++cx) {
+        const int64_t cc[3] = {cx, cy, cz};
+        const double e = __ldg(E + cell_lin(g, cc));
+        int li = 0;
+        for (int d = DIM - 1; d >= 0; --d) li = li * L::KP1 + (int)(X[d] - K * cc[d]);
+        const double* krow = Kel + (size_t)(c * L::NN + li) * M;
+        for (int lj = 0; lj < L::NN; ++lj) {
+          int64_t Y[3] = {0, 0, 0};
+          for (int d = 0, rest = lj; d < DIM; ++d) {
+            Y[d] = K * cc[d] + rest % L::KP1;
+            rest /= L::KP1;
+          }
+          if (!node_is_dirichlet(g, Y)) continue;
+          const int64_t ylin = lattice_lin(g, Y);
+          for (int d = 0; d < DIM; ++d) b -= e * __ldg(krow + d * L::NN + lj) * __ldg(u_dir + DIM * ylin + d);
+        }
+      }
+  return b;
+}
+
+// rhs of owned vector row r = (node, c): force_c * int phi_node over the node's cells,
+// minus the Dirichlet lifting when the trial space has values (u_dir non-null)
 template <int DIM, int K>
 __global__ void k_rhs_elasticity(Geom g, int64_t nrows_own, const int32_t* __restrict__ row_node,
                                  const double* __restrict__ E, const double* __restrict__ Khat,
                                  const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f0,
-                                 double f1, double f2, double* __restrict__ rhs, int32_t* __restrict__ bad) {
+                                 double f1, double f2, const double* __restrict__ Kel,
+                                 const double* __restrict__ u_dir, double* __restrict__ rhs,
+                                 int32_t* __restrict__ bad) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows_own) return;
   const int c = (int)(r % DIM);
   const double f = c == 0 ? f0 : (c == 1 ? f1 : f2);
   const int nbad = qk_rhs_row<DIM, K>(g, r, row_node, E, Khat, Mhat, Fhat, f, nullptr, nullptr, rhs);
+  if (u_dir) rhs[r] += elasticity_lifting<DIM, K>(g, row_node[r], c, E, Kel, u_dir);
   if (nbad) atomicAdd(bad, nbad);
 }
 
@@ -451,9 +501,10 @@ static int launch_elasticity(gd_asm* A, const double* E, const double* force, in
   kern<<<nbw, 256, smem, st>>>(g, R, A->rowptr.p, A->row_node.p, reinterpret_cast<const uint16_t*>(A->code.p), E,
                                A->Kel.p, A->vals.p);
   GD_CUDA_TRY(cudaGetLastError());
+  const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
   k_rhs_elasticity<DIM, K><<<(unsigned)((R + 127) / 128), 128, 0, st>>>(
       g, R, A->row_node.p, E, A->Khat.p, A->Mhat.p, A->Fhat.p, force[0], force[1], DIM == 3 ? force[2] : 0.0,
-      A->rhs.p, bad);
+      A->Kel.p, udir, A->rhs.p, bad);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
@@ -483,8 +534,6 @@ extern "C" int gd_assemble_elasticity(gd_asm* A, const gd_elasticity* c) {
   const Geom& g = A->test->geom;
   if (A->bs != g.dim) return fail(GD_ERR_UNSUPPORTED, "gd_assemble_elasticity: needs a vector space with dim components");
   if (!(c->nu > -1.0 && c->nu < 0.5)) return fail(GD_ERR_ARG, "gd_assemble_elasticity: Poisson ratio outside (-1, 0.5)");
-  if (A->trial->has_dirichlet_values)
-    return fail(GD_ERR_UNSUPPORTED, "gd_assemble_elasticity: non-zero Dirichlet values");
   cudaStream_t st = A->test->model->ctx->stream;
   GD_TRY(reference_element(A, c->degree));
   if (A->el_degree != c->degree || A->el_nu != c->nu || !A->Kel.p) {

@@ -321,10 +321,29 @@ def TrialFESpace(u, V: DistributedSingleFieldFESpace):
     """``TrialFESpace(u, V)``: nodal interpolation of ``u`` on the Dirichlet nodes.
 
     ``u`` is a number, a vectorised callable of the coordinates, or a dense
-    array over the global node lattice."""
+    array over the global node lattice.  On a vector space: a constant vector (tuple), a
+    callable returning one array (or number) per component, or a dense array of shape
+    (lattice nodes, ncomp)."""
     if u is None or (np.isscalar(u) and u == 0):
         L.call("gd_space_set_dirichlet", V.handle, None, L.GD_HOST)
         V.dirichlet_values = None
+        return V
+    if V.ncomp > 1:
+        nn = int(np.prod(V.lattice))
+        if callable(u):
+            xyz = V.lattice_xyz()
+            comps = u(*[xyz[:, d] for d in range(V.model.dim)])
+            if len(comps) != V.ncomp:
+                raise ValueError(f"TrialFESpace: u returns {len(comps)} components, the space has {V.ncomp}")
+            vals = np.stack([np.broadcast_to(np.asarray(c, dtype=np.float64), (nn,)) for c in comps], axis=1)
+        else:
+            vals = np.asarray(u, dtype=np.float64)
+            if vals.ndim == 1 and vals.shape[0] == V.ncomp:
+                vals = np.broadcast_to(vals, (nn, V.ncomp))
+            vals = vals.reshape(nn, V.ncomp)
+        vals = np.ascontiguousarray(vals)
+        L.call("gd_space_set_dirichlet", V.handle, L.ptr(vals, C.c_double), L.GD_HOST)
+        V.dirichlet_values = vals
         return V
     if callable(u):
         xyz = V.lattice_xyz()

@@ -123,7 +123,9 @@ int gd_space_get_gids(const gd_space* space, int part, int64_t* ldof_to_gdof,
 /* Global lattice node index of every local free DOF of one part. */
 int gd_space_dof_nodes(const gd_space* space, int part, int64_t* ldof_to_node);
 /* TrialFESpace(u, V) (FESpaces.jl:396-401): Dirichlet values as a dense array
- * over the global node lattice (only Dirichlet nodes are read); NULL = zero. */
+ * over the global node lattice (only Dirichlet nodes are read); NULL = zero.  On a
+ * vector space, ncomp values per node, the components of a node together
+ * (u_lattice[ncomp * node + c]). */
 int gd_space_set_dirichlet(gd_space* space, const double* u_lattice, int where);
 
 /* ---- A9-A13: SparseMatrixAssembler + assemble_matrix_and_vector --------------

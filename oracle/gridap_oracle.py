@@ -588,7 +588,8 @@ class Problem:
     kappa: np.ndarray = None        # per global cell (lexicographic); default 1
     f_const: float = 0.0            # constant source
     f_nodal: np.ndarray = None      # or nodal source values on the global lattice (b = M f)
-    u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0
+    u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0;
+                                    # elasticity: (lattice nodes, dim), components of a node together
     neumann: dict = None            # {side: g(*xyz, *normal)}, side 2d (x_d = min) / 2d+1 (max): l += int(v g)dGamma
     physics: str = "poisson"        # or "elasticity"
     nu: float = 0.3                 # Poisson ratio (elasticity)
@@ -663,13 +664,22 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
     lnodes = np.array(cell_local_nodes(dim, pb.order))
     mats, vecs = [], []
     if pb.physics == "elasticity":
-        assert pb.u_dir is None and pb.f_nodal is None, "elasticity: homogeneous Dirichlet, constant force"
+        # element DOFs component-major (c * nnode + a), as Kel; u_dir: (lattice nodes, dim)
+        assert pb.f_nodal is None, "elasticity: constant body force"
         Kel = reference_elasticity(dim, pb.order, pb.h, pb.degree, pb.nu)
         force = pb.force if pb.force is not None else (0.0,) * dim
         be = np.concatenate([force[c] * Fh for c in range(dim)])
+        ud_all = None if pb.u_dir is None else np.asarray(pb.u_dir, dtype=np.float64).reshape(-1, dim)
         for ic, g in enumerate(sp.cells):
-            mats.append(pb.kappa[g] * Kel)
-            vecs.append(be.copy())
+            Ke = pb.kappa[g] * Kel
+            bv = be.copy()
+            if ud_all is not None:
+                ci = np.array(P_cell_coords(pb.n, int(g)))
+                nl = pb.node_lin(pb.order * ci[None, :] + lnodes)
+                ud = np.where(sp.cell_dofs[ic] < 0, np.concatenate([ud_all[nl, c] for c in range(dim)]), 0.0)
+                bv = bv - Ke @ ud
+            mats.append(Ke)
+            vecs.append(bv)
         return mats, vecs
     nbt = neumann_tables(pb) if pb.neumann else None
     for ic, g in enumerate(sp.cells):

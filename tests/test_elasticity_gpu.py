@@ -42,7 +42,7 @@ def gpu_system(be, pb, strategy):
     tags = ["left", "right", "bottom", "top", "back", "front"]
     sides = [t for t, s in zip(tags, pb.dirichlet_sides) if s]
     V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, G.VectorValue, pb.order), dirichlet_tags=sides)
-    U = G.TrialFESpace(0.0, V)
+    U = G.TrialFESpace(pb.u_dir if pb.u_dir is not None else 0.0, V)
     dO = G.Measure(G.Triangulation(model), pb.degree)
     a = G.integral_elasticity(pb.kappa, pb.nu, dO)
     l = G.integral_source(pb.force, dO)
@@ -111,3 +111,55 @@ def test_vector_space_rejects_order_3(backend):
     model = G.CartesianDiscreteModel(ranks, (2, 1, 1), (0, 1, 0, 1, 0, 1), (2, 2, 2))
     with pytest.raises(GdError):
         G.TestFESpace(model, G.ReferenceFE(G.lagrangian, G.VectorValue, 3))
+
+
+def lattice_field(pb, fn):
+    """Dense (lattice nodes, dim) array of fn(xyz) in lattice order (x fastest)."""
+    dim, N = pb.dim, pb.lattice
+    X = np.stack(np.meshgrid(*[np.arange(N[d]) for d in range(dim)], indexing="ij"), axis=-1).reshape(-1, dim)
+    u = np.empty((int(np.prod(N)), dim))
+    u[pb.node_lin(X)] = fn(pb.node_xyz(X))
+    return u
+
+
+@pytest.mark.parametrize("strategy", ["sub", "full"])
+@pytest.mark.parametrize("case", [CASES[0], CASES[1], CASES[4], CASES[5]], ids=case_id)
+def test_elasticity_dirichlet_values_match_oracle(backend, case, strategy):
+    """TrialFESpace(u, V) on a vector space: the lifted right-hand side (b -= K[:,D] u_D,
+    E per cell) against the oracle's, 1e-12 relative; the matrix does not change."""
+    pb = problem(case)
+    pb.u_dir = lattice_field(pb, lambda x: np.stack([np.sin(1.0 + x[:, d]) * (d + 1.0) + x[:, 0] * x[:, -1]
+                                                     for d in range(pb.dim)], axis=1))
+    fe = go.build_fespace(pb)
+    parts = go.assemble(pb, fe, strategy)
+    V, op = gpu_system(backend, pb, strategy)
+    for p, (rp, ci, vv) in enumerate(op.matrix.csr_parts()):
+        O = parts[p]
+        assert np.array_equal(ci, O.colidx)
+        if len(O.vals):
+            assert np.abs(vv - O.vals).max() <= VAL_TOL * np.abs(O.vals).max()
+        if len(O.b):
+            assert np.abs(op.vector.partition[p] - O.b).max() <= VAL_TOL * max(np.abs(O.b).max(), 1e-300)
+
+
+@pytest.mark.parametrize("dim,order,parts,n", [(2, 1, (2, 1), (4, 3)), (2, 2, (2, 2), (3, 3)),
+                                                (3, 1, (2, 1, 2), (4, 3, 3)), (3, 2, (1, 2, 1), (2, 3, 2))])
+def test_affine_displacement_kat_on_gpu(backend, dim, order, parts, n):
+    """Known answer: u = B x + t on the whole boundary, E constant, no body force; the
+    affine field has constant stress and lies in the space, so the device solve
+    reproduces it: L2 error < 1e-9 (and the oracle's LU, tests/test_oracle_elasticity.py)."""
+    import gridap_gb300 as G
+    rng = np.random.default_rng(90 + 10 * dim + order)
+    B, t = rng.normal(size=(dim, dim)), rng.normal(size=dim)
+    domain = tuple(v for d in range(dim) for v in (0.0, 1.0 + 0.5 * d))
+    ranks = backend.distribute(range(int(np.prod(parts))))
+    model = G.CartesianDiscreteModel(ranks, parts, domain, n)
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, G.VectorValue, order), dirichlet_tags="boundary")
+    u = lambda *x: tuple(sum(B[c, d] * x[d] for d in range(dim)) + t[c] for c in range(dim))
+    U = G.TrialFESpace(u, V)
+    dO = G.Measure(G.Triangulation(model), 2 * order)
+    op = G.AffineFEOperator(G.integral_elasticity(np.full(int(np.prod(n)), 2.5), 0.3, dO),
+                            G.integral_source((0.0,) * dim, dO), U, V)
+    uh = G.solve(op, rtol=1e-14)
+    assert op.matrix.last_stats.converged
+    assert G.l2_error(uh, u, dO) < 1e-9
