@@ -15,7 +15,9 @@ device->host inside every timed step.  `roofline` uses the algorithmic bytes
 `solve` reports Jacobi-PCG (FP64) and the mixed-precision refinement to 1e-8 relative
 residual on the assembled system; `learned` the learned-preconditioner flexible CG
 against both on 96^3 lognormal diffusion (sigma 1.5); `batched` the 64-problem uneven
-batch (Q1-Q3, 16^3..96^3 cells) assembled one persistent launch per memory wave.
+batch (Q1-Q3, 16^3..96^3 cells) assembled one persistent launch per memory wave; `c1` the
+2D Q2 Poisson problem on 128^2 cells (u = (x+y)^2 on the boundary, f = -4): assembly,
+solves and the known-answer L2 error.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 Under torchrun with N>1 every rank runs its own replica of the workload on its own
@@ -60,6 +62,7 @@ def parse():
     ap.add_argument("--batched-sample-gb", type=float, default=16.0, help="device memory of the sample wave")
     ap.add_argument("--batched-solve", action="store_true", help="also Jacobi-PCG every batched problem")
     ap.add_argument("--no-learned", action="store_true")
+    ap.add_argument("--no-c1", action="store_true", help="skip the 2D Q2 128^2 Poisson section")
     ap.add_argument("--no-elasticity", action="store_true")
     ap.add_argument("--elasticity-solve", action="store_true", help="also solve the elasticity system (seconds)")
     ap.add_argument("--elasticity-cells", type=int, default=64, help="cells per direction of the elasticity workload")
@@ -481,6 +484,75 @@ def run_learned(args, be, dev):
 
 
 # ------------------------------------------------------------------------------------
+# C1: 2D Q2 Poisson, 128^2 cells, parts (2,2), u = (x+y)^2 on the boundary, f = -4
+# ------------------------------------------------------------------------------------
+def run_c1(args, be, dev, stream, flush):
+    """Numeric assembly (device-resident, per-step CUDA events, L2 flushed between steps),
+    the solves to 1e-8 through the Python mirror, and the known answer: Q2 reproduces
+    (x+y)^2, so the L2 error of the FP64 solve at rtol 1e-13 is the solver's alone."""
+    import torch
+    import gridap_gb300 as G
+    from gridap_gb300 import _lib as L
+    cells, parts, degree, f = (128, 128), (2, 2), 4, -4.0
+    u = lambda x, y: (x + y) ** 2
+    ranks = be.distribute(range(4))
+    model = G.CartesianDiscreteModel(ranks, parts, (0.0, 1.0, 0.0, 1.0), cells)
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 2), dirichlet_tags="boundary")
+    U = G.TrialFESpace(u, V)
+    assem = G.SparseMatrixAssembler(U, V, G.SubAssembledRows())
+    assem.symbolic()
+    ng, nnz_own = C.c_int64(), C.c_int64()
+    L.call("gd_assembler_counts", assem.handle, C.byref(ng), C.byref(nnz_own), None, None)
+    ngdofs, nnz = ng.value, nnz_own.value
+    ncells = cells[0] * cells[1]
+    kappa_d = torch.ones(ncells, dtype=torch.float64, device=dev)
+    coeffs = L.gd_coeffs()
+    coeffs.kappa = kappa_d.data_ptr()
+    coeffs.f_nodal = None
+    coeffs.f_const = f
+    coeffs.degree = degree
+    coeffs.where = L.GD_DEVICE
+    L.call("gd_assemble_numeric", assem.handle, C.byref(coeffs))
+    for _ in range(max(args.warmup, 3)):
+        L.call("gd_assemble_numeric_async", assem.handle, C.byref(coeffs))
+    torch.cuda.synchronize()
+    steps = max(args.steps, 10)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    for i in range(steps):
+        flush.zero_()
+        ev[i][0].record(stream)
+        L.call("gd_assemble_numeric_async", assem.handle, C.byref(coeffs))
+        ev[i][1].record(stream)
+    torch.cuda.synchronize()
+    ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+    peak, peak_kind = measured_peaks()
+    alg = 8 * nnz + 8 * ngdofs + 8 * ncells
+    out = {"workload": "poisson2d_q2_128^2_parts2x2", "cells": list(cells), "parts": list(parts), "order": 2,
+           "quadrature_degree": degree, "free_dofs": ngdofs, "nnz": nnz,
+           "assembly": {"ms": ms, "steps": steps, "nnz_per_s": nnz / (ms * 1e-3),
+                        "roofline": {"bound": "hbm", "algorithmic_bytes": alg, "achieved": alg / (ms * 1e-3) / 1e9,
+                                     "peak": peak, "unit": "GB/s", "frac": alg / (ms * 1e-3) / 1e9 / peak,
+                                     "peak_kind": peak_kind}}}
+    dO = G.Measure(G.Triangulation(model), degree)
+    op = G.AffineFEOperator(G.integral_grad_grad(None, dO), G.integral_source(f, dO), U, V)
+    solves = {}
+    for name, method in (("jacobi_pcg_fp64", "jacobi_pcg"), ("mixed_ir_jacobi", "mixed_ir")):
+        op.matrix.solve(rtol=1e-8, method=method)   # warm: one-time buffers
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        op.matrix.solve(rtol=1e-8, method=method)
+        t = time.perf_counter() - t0
+        st = op.matrix.last_stats
+        solves[name] = {"rtol": 1e-8, "seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                        "converged": bool(st.converged)}
+    out["solve"] = solves
+    uh = G.solve(op, rtol=1e-13)
+    out["kat"] = {"check": "u = (x+y)^2 reproduced by Q2 (test/PoissonTests.jl:14-45 at 128^2), FP64 Jacobi-PCG "
+                           "to rtol 1e-13", "l2_error": G.l2_error(uh, u, dO), "bound": 1e-9}
+    return out
+
+
+# ------------------------------------------------------------------------------------
 # GB300 arm
 # ------------------------------------------------------------------------------------
 def run_gb300(args, rank, world, local):
@@ -630,6 +702,9 @@ def run_gb300(args, rank, world, local):
     learned = None
     if not args.no_learned:
         learned = run_learned(args, be, dev)
+    c1 = None
+    if not args.no_c1:
+        c1 = run_c1(args, be, dev, stream, flush)
     elasticity = None
     if not args.no_elasticity:
         elasticity = run_elasticity(args, be, stream, dev)
@@ -673,6 +748,7 @@ def run_gb300(args, rank, world, local):
             "wall_s_timed_region": t_wall,
             "solve": solve,
             "learned": learned,
+            "c1": c1,
             "elasticity": elasticity,
             "batched": batched,
             "cpu_baseline": cpu,

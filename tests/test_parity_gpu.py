@@ -118,6 +118,34 @@ def test_mul_matches_gathered_oracle(backend, case):
         assert np.abs(y - y_ref).max() <= 1e-12 * np.abs(y_ref).max()
 
 
+def test_c1_poisson2d_q2_128(backend):
+    """The C1 configuration at full size: 2D Q2 on 128 x 128 cells, parts (2,2), quadrature
+    degree 4, u = (x+y)^2 on the boundary, f = -4 (test/PoissonTests.jl:14-45 on a 128^2
+    mesh).  Local parts against the oracle (pattern bit-exact, values 1e-12), the device FP64
+    solve against the oracle's gathered sparse LU (1e-8), and the known answer: Q2 reproduces
+    (x+y)^2, L2 error < 1e-9 (the discretisation error is zero; the solver's at rtol 1e-13 is
+    ~1e-12)."""
+    import gridap_gb300 as G
+    u = lambda x, y: (x + y) ** 2
+    pb = make_problem(2, (128, 128), (2, 2), 2, f=-4.0, u=u)
+    fe = go.build_fespace(pb)
+    ref = go.assemble(pb, fe, "sub")
+    model, V, U, op = gpu_system(backend, pb, "sub")
+    A = op.matrix
+    for p, M in enumerate(ref):
+        rp, ci, vv = A.csr_parts()[p]
+        assert np.array_equal(rp, M.rowptr), f"rowptr part {p}"
+        assert np.array_equal(ci, M.colidx), f"colidx part {p}"
+        assert row_scaled_error(vv, M.vals, M.rowptr) <= VAL_TOL
+        assert np.abs(op.vector.partition[p] - M.b).max() <= VAL_TOL * np.abs(M.b).max()
+    x_ref = go.solve_lu(ref, fe.dofs[0].ngdofs)
+    uh = G.solve(op, rtol=1e-13)
+    assert op.matrix.last_stats.converged
+    assert np.abs(uh.free_values - x_ref).max() / np.abs(x_ref).max() <= SOL_TOL
+    dO = G.Measure(G.Triangulation(model), pb.degree)
+    assert G.l2_error(uh, u, dO) < 1e-9
+
+
 @pytest.mark.parametrize("case", [CASES[1], CASES[6], CASES[7]], ids=case_id)
 def test_solve_matches_gathered_lu(backend, case):
     pb = make_problem(**case)
