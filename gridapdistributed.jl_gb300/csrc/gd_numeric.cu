@@ -952,5 +952,60 @@ extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nn
   return GD_OK;
 }
 
+// assemble_vector(assem, collect_cell_vector(V, l)) for l(v) = int(v f): the load vector
+// alone (no Dirichlet lifting, which Gridap applies only with a cell matrix), over the
+// owned rows in global order, into a caller buffer; the assembler's matrix values and
+// right-hand side are left as they are.
+extern "C" int gd_assemble_vector(gd_asm* A, const gd_coeffs* c, double* b, int where_b) {
+  using namespace gd;
+  if (!A || !c || !b) return fail(GD_ERR_ARG, "gd_assemble_vector: null argument");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_assemble_vector: run gd_assemble_symbolic first");
+  if (A->bs > 1) return fail(GD_ERR_UNSUPPORTED, "gd_assemble_vector: scalar spaces only");
+  const Geom& g = A->test->geom;
+  cudaStream_t st = A->test->model->ctx->stream;
+  GD_TRY(reference_element(A, c->degree));
+  const int64_t R = A->ngdofs;
+  int64_t nnodes = 1;
+  for (int d = 0; d < g.dim; ++d) nnodes *= g.N[d];
+  const double* fn = c->f_nodal;
+  if (fn && c->where == GD_HOST) {
+    if (A->f_dev.n != (size_t)nnodes) GD_TRY(dalloc(A->f_dev, nnodes));
+    GD_CUDA_TRY(cudaMemcpyAsync(A->f_dev.p, fn, sizeof(double) * nnodes, cudaMemcpyHostToDevice, st));
+    fn = A->f_dev.p;
+  }
+  if (R == 0) return GD_OK;
+  DBuf<double> tmp;
+  double* out = b;
+  if (where_b == GD_HOST) {
+    GD_TRY(dalloc(tmp, R));
+    out = tmp.p;
+  }
+  if (!A->dred.p) GD_TRY(dalloc(A->dred, 4096));
+  int32_t* bad = (int32_t*)A->dred.p;
+  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
+  const unsigned nb = (unsigned)((R + 127) / 128);
+  const int sel = g.dim * 10 + g.k;
+#define GD_VEC_LAUNCH(D, K)                                                                                    \
+  k_numeric_rhs<D, K><<<nb, 128, 0, st>>>(g, R, A->row_node.p, nullptr, A->Khat.p, A->Mhat.p, A->Fhat.p, c->f_const, \
+                                          fn, nullptr, out, bad)
+  switch (sel) {
+    case 21: GD_VEC_LAUNCH(2, 1); break;
+    case 22: GD_VEC_LAUNCH(2, 2); break;
+    case 23: GD_VEC_LAUNCH(2, 3); break;
+    case 31: GD_VEC_LAUNCH(3, 1); break;
+    case 32: GD_VEC_LAUNCH(3, 2); break;
+    case 33: GD_VEC_LAUNCH(3, 3); break;
+    default:
+      dfreeb(tmp);
+      return fail(GD_ERR_UNSUPPORTED, "gd_assemble_vector: unsupported dim/order");
+  }
+#undef GD_VEC_LAUNCH
+  GD_CUDA_TRY(cudaGetLastError());
+  if (where_b == GD_HOST) GD_CUDA_TRY(cudaMemcpyAsync(b, out, sizeof(double) * R, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  dfreeb(tmp);
+  return GD_OK;
+}
+
 extern "C" int gd_assemble_numeric(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, true); }
 extern "C" int gd_assemble_numeric_async(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, false); }

@@ -4,12 +4,14 @@
 ``include/gdgpu.h``; ``_lib`` is the ctypes binding of ``libgdgpu.so``.
 """
 from . import _lib
-from .distributed import (AffineFEOperator, Boundary, CartesianDiscreteModel, FEFunction, FESpace,
-                          FullyAssembledRows, GB300Backend, Measure, PSparseMatrix, PVector,
+from .distributed import (AffineFEOperator, AssembledPVector, Boundary, CartesianDiscreteModel, FEFunction,
+                          FESpace, FullyAssembledRows, GB300Backend, Measure, PSparseMatrix, PVector,
                           ReferenceFE, SparseMatrixAssembler, SubAssembledRows, TestFESpace,
-                          Triangulation, TrialFESpace, VectorValue, assemble_matrix_and_vector,
-                          collect_cell_matrix_and_vector, integral_boundary_source, integral_elasticity,
-                          integral_grad_grad,
+                          Triangulation, TrialFESpace, VectorValue, allocate_matrix, allocate_matrix_and_vector,
+                          allocate_vector, assemble_matrix, assemble_matrix_, assemble_matrix_and_vector,
+                          assemble_matrix_and_vector_, assemble_vector, assemble_vector_, collect_cell_matrix,
+                          collect_cell_matrix_and_vector, collect_cell_vector, integral_boundary_source,
+                          integral_elasticity, integral_grad_grad,
                           integral_source, l2_error, lagrangian, quadrature_points, solve,
                           with_gb300)
 from .dg import Skeleton, integral_sipg, integral_sipg_source

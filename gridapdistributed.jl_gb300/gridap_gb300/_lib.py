@@ -85,6 +85,7 @@ SIGNATURES = {
     "gd_assemble_symbolic": [P],
     "gd_assemble_numeric": [P, C.POINTER(gd_coeffs)],
     "gd_assemble_numeric_async": [P, C.POINTER(gd_coeffs)],
+    "gd_assemble_vector": [P, C.POINTER(gd_coeffs), DP, C.c_int],
     "gd_assembler_set_profiling": [P, C.c_int],
     "gd_assembler_phase_times": [P, DP, DP, DP],
     "gd_assembler_counts": [P, I64P, I64P, I64P, I32P],

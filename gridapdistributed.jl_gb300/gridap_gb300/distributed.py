@@ -606,16 +606,25 @@ class PSparseMatrix:
         L.call("gd_spmv", self.assem.handle, L.vptr(x), L.vptr(y), L.GD_HOST)
         return y
 
-    def solve(self, rtol=1e-12, maxit=100000, method="jacobi_pcg"):
-        """``A \\ b`` for the assembled right-hand side.
+    def solve(self, rtol=1e-12, maxit=100000, method="jacobi_pcg", b=None):
+        """``A \\ b``: for the assembled right-hand side, or for ``b`` (a PVector, an
+        AssembledPVector or a global array in gid order) when given.
 
         ``method``: "jacobi_pcg" (FP64 Jacobi-PCG) or "mixed_ir" (FP64 iterative
         refinement around FP32 Jacobi-PCG with FP64 inner products)."""
         codes = {"jacobi_pcg": L.GD_SOLVE_JACOBI_PCG, "mixed_ir": L.GD_SOLVE_MIXED_IR}
         x = np.zeros(self.n_global)
         st = L.gd_solve_stats()
-        L.call("gd_solve", self.assem.handle, codes[method], float(rtol), int(maxit), L.vptr(x), L.GD_HOST,
-               C.byref(st))
+        if b is None:
+            L.call("gd_solve", self.assem.handle, codes[method], float(rtol), int(maxit), L.vptr(x), L.GD_HOST,
+                   C.byref(st))
+        else:
+            bv = b.global_values() if hasattr(b, "global_values") else b
+            bv = np.ascontiguousarray(bv, dtype=np.float64)
+            if bv.shape != (self.n_global,):
+                raise ValueError(f"solve: b has {bv.shape[0]} entries, the matrix {self.n_global} rows")
+            L.call("gd_solve_rhs", self.assem.handle, codes[method], float(rtol), int(maxit), L.vptr(bv), L.vptr(x),
+                   L.GD_HOST, C.byref(st))
         self.last_stats = st
         return x
 
@@ -644,11 +653,146 @@ def collect_cell_matrix_and_vector(U, V, a, l, uhd=None):
     return (a, l)
 
 
+def collect_cell_matrix(U, V, a):
+    """``collect_cell_matrix(U, V, a(du, dv))``: the bilinear form alone."""
+    return _MatrixData(a)
+
+
+def collect_cell_vector(V, l):
+    """``collect_cell_vector(V, l(dv))``: the linear form alone (no Dirichlet lifting)."""
+    return _VectorData(l)
+
+
+@dataclass
+class _MatrixData:
+    a: object
+
+
+@dataclass
+class _VectorData:
+    l: object
+
+
+def _matrix_form(data):
+    return data.a if isinstance(data, _MatrixData) else data
+
+
+def _check_owner(obj, assem, what):
+    if obj.assem is not assem:
+        raise ValueError(f"{what} was allocated by another assembler")
+
+
 def assemble_matrix_and_vector(assem: DistributedSparseMatrixAssembler, data):
     a, l = data
     assem.numeric(a, l)
     A = PSparseMatrix(assem)
     return A, PVector(assem, A)
+
+
+def allocate_matrix_and_vector(assem: DistributedSparseMatrixAssembler, data):
+    """The symbolic phase: a PSparseMatrix with the pattern and zero values and its PVector,
+    to be filled by ``assemble_matrix_and_vector_`` (Julia's ``assemble_matrix_and_vector!``)."""
+    assem.symbolic()
+    A = PSparseMatrix(assem)
+    return A, PVector(assem, A)
+
+
+def assemble_matrix_and_vector_(A: "PSparseMatrix", b: "PVector", assem: DistributedSparseMatrixAssembler, data):
+    """``assemble_matrix_and_vector!(A, b, assem, data)``: new values into the pattern of A."""
+    _check_owner(A, assem, "the matrix")
+    _check_owner(b, assem, "the vector")
+    a, l = data
+    assem.numeric(a, l)
+    A._parts = None
+    return A, b
+
+
+def assemble_matrix(assem: DistributedSparseMatrixAssembler, data):
+    """``assemble_matrix(assem, collect_cell_matrix(U, V, a))``.  The device assembles the
+    right-hand side alongside (with f = 0); a PVector made from this assembler later shows it."""
+    assem.numeric(_matrix_form(data), None)
+    return PSparseMatrix(assem)
+
+
+def allocate_matrix(assem: DistributedSparseMatrixAssembler, data):
+    assem.symbolic()
+    return PSparseMatrix(assem)
+
+
+def assemble_matrix_(A: "PSparseMatrix", assem: DistributedSparseMatrixAssembler, data):
+    """``assemble_matrix!(A, assem, data)``."""
+    _check_owner(A, assem, "the matrix")
+    assem.numeric(_matrix_form(data), None)
+    A._parts = None
+    return A
+
+
+def _vector_coeffs(V, l):
+    if isinstance(l, _VectorData):
+        l = l.l
+    if not isinstance(l, SourceForm):
+        raise NotImplementedError("assemble_vector: one volume source term int(v f)")
+    c = L.gd_coeffs()
+    c.kappa = None
+    keep = None
+    if np.isscalar(l.f):
+        c.f_nodal = None
+        c.f_const = float(l.f)
+    else:
+        keep = np.ascontiguousarray(l.f, dtype=np.float64)
+        c.f_nodal = keep.ctypes.data
+        c.f_const = 0.0
+    c.degree = int(l.measure.degree if l.measure is not None else 2 * V.order)
+    c.where = L.GD_HOST
+    return c, keep
+
+
+def assemble_vector(assem: DistributedSparseMatrixAssembler, data):
+    """``assemble_vector(assem, collect_cell_vector(V, l))``: the load vector alone, a new
+    vector (the assembler's matrix and right-hand side are not touched)."""
+    b = allocate_vector(assem, data)
+    return assemble_vector_(b, assem, data)
+
+
+def allocate_vector(assem: DistributedSparseMatrixAssembler, data):
+    assem.symbolic()
+    return AssembledPVector(assem, np.zeros(assem.V.num_free_dofs()))
+
+
+def assemble_vector_(b: "AssembledPVector", assem: DistributedSparseMatrixAssembler, data):
+    """``assemble_vector!(b, assem, data)``."""
+    _check_owner(b, assem, "the vector")
+    assem.symbolic()
+    c, keep = _vector_coeffs(assem.V, data)
+    L.call("gd_assemble_vector", assem.handle, C.byref(c), L.ptr(b.values, C.c_double), L.GD_HOST)
+    return b
+
+
+class AssembledPVector:
+    """A PVector from ``assemble_vector``: global values over the owned rows (gid order); the
+    per-part layout is the assembler's row partition (owned rows, then its ghost rows, which
+    hold zeros)."""
+
+    def __init__(self, assem: DistributedSparseMatrixAssembler, values: np.ndarray):
+        self.assem = assem
+        self.values = np.ascontiguousarray(values, dtype=np.float64)
+
+    def __len__(self):
+        return len(self.values)
+
+    def global_values(self):
+        return self.values.copy()
+
+    @property
+    def partition(self):
+        out = []
+        V = self.assem.V
+        for p in range(V.model.num_parts):
+            nr, nc, nnz, ngr, ngc = (C.c_int64() for _ in range(5))
+            L.call("gd_matrix_sizes", self.assem.handle, p, *[C.byref(x) for x in (nr, nc, nnz, ngr, ngc)])
+            _, nown, first = V.local_sizes(p)
+            out.append(np.concatenate([self.values[first:first + nown], np.zeros(ngr.value)]))
+        return out
 
 
 class AffineFEOperator:

@@ -154,6 +154,12 @@ typedef struct gd_coeffs {
 int gd_assemble_numeric(gd_asm* a, const gd_coeffs* c);
 /* Same, without the final stream synchronisation (for timing loops). */
 int gd_assemble_numeric_async(gd_asm* a, const gd_coeffs* c);
+/* assemble_vector(assem, collect_cell_vector(V, l)) for l(v) = int(v f) (Gridap's
+ * assemble_vector, called at test/FESpacesTests.jl:65-69): the load vector without
+ * Dirichlet lifting, over the owned rows in global order (length = free DOFs), into b
+ * (where_b: GD_HOST or GD_DEVICE).  c->kappa is not used; the assembler's matrix values
+ * and right-hand side are not changed.  Scalar spaces. */
+int gd_assemble_vector(gd_asm* a, const gd_coeffs* c, double* b, int where_b);
 
 /* Linear elasticity on a vector space (gd_space_create with ncomp = dim, orders 1-2):
  * a(u,v) = int C(E) eps(u):eps(v), isotropic C with Young's modulus E per cell and

@@ -203,6 +203,56 @@ def test_fespaces_kat_on_gpu(backend, parts, strategy):
     assert np.abs(r).max() < 1e-10
 
 
+@pytest.mark.parametrize("strategy", ["sub", "full"])
+@pytest.mark.parametrize("parts", [(2, 2), (1, 1), (2, 1), (1, 2)])
+def test_fespaces_assemble_tests_sequence(backend, parts, strategy):
+    """test/FESpacesTests.jl:12-70 (`assemble_tests`) call by call on the GPU path: Q1 on
+    (0,4)^2 with 4 x 4 cells, u = x+y on the boundary, a = int(grad v . grad u), l = int(0 v),
+    degree 3.  assemble_matrix_and_vector (and the local matrix sizes), allocate_matrix_and_vector
+    + assemble_matrix_and_vector!, AffineFEOperator, assemble_matrix and allocate_matrix +
+    assemble_matrix! solved against the operator's vector: L2 error < 1e-9 each; then
+    assemble_vector and allocate_vector + assemble_vector! of int(1 v) on a fresh assembler:
+    sum(b) == length(b) to 1e-12 (no Dirichlet lifting in a vector-only assembly)."""
+    import gridap_gb300 as G
+    u = lambda x, y: x + y
+    ranks = backend.distribute(range(int(np.prod(parts))))
+    model = G.CartesianDiscreteModel(ranks, parts, (0, 4, 0, 4), (4, 4))
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 1), dirichlet_tags="boundary")
+    U = G.TrialFESpace(u, V)
+    das = G.SubAssembledRows() if strategy == "sub" else G.FullyAssembledRows()
+    dO = G.Measure(G.Triangulation(model), 3)
+    a = G.integral_grad_grad(None, dO)
+    l = G.integral_source(0.0, dO)
+    assem = G.SparseMatrixAssembler(U, V, das)
+    err = lambda x: G.l2_error(G.FEFunction(U, x), u, dO)
+
+    data = G.collect_cell_matrix_and_vector(U, V, a, l)
+    A1, b1 = G.assemble_matrix_and_vector(assem, data)
+    assert err(A1.solve(rtol=1e-14)) < 1e-9
+    for mat, rows, cols in zip(A1.matrix_partition, A1.row_partition, A1.col_partition):
+        assert mat.shape == (rows.local_length(), cols.local_length())
+    A2, b2 = G.allocate_matrix_and_vector(assem, data)
+    G.assemble_matrix_and_vector_(A2, b2, assem, data)
+    assert err(A2.solve(rtol=1e-14)) < 1e-9
+    op = G.AffineFEOperator(a, l, U, V, G.SparseMatrixAssembler(U, V, das))
+    assert err(G.solve(op, rtol=1e-14).free_values) < 1e-9
+    mdata = G.collect_cell_matrix(U, V, a)
+    A3 = G.assemble_matrix(assem, mdata)
+    assert err(A3.solve(rtol=1e-14, b=op.vector)) < 1e-9
+    A4 = G.allocate_matrix(assem, mdata)
+    G.assemble_matrix_(A4, assem, mdata)
+    assert err(A4.solve(rtol=1e-14, b=op.vector)) < 1e-9
+
+    vecdata = G.collect_cell_vector(V, G.integral_source(1.0, dO))
+    assem = G.SparseMatrixAssembler(U, V, das)
+    bv1 = G.assemble_vector(assem, vecdata)
+    assert abs(bv1.global_values().sum() - len(bv1)) < 1e-12
+    bv2 = G.allocate_vector(assem, vecdata)
+    G.assemble_vector_(bv2, assem, vecdata)
+    assert abs(bv2.global_values().sum() - len(bv2)) < 1e-12
+    assert all(len(bp) == rows.local_length() for bp, rows in zip(bv2.partition, A1.row_partition))
+
+
 def test_poisson_q2_kat_on_gpu(backend):
     """test/PoissonTests.jl:14-45 (all-Dirichlet): Q2 reproduces (x+y)^2."""
     import gridap_gb300 as G
