@@ -10,10 +10,11 @@ from .distributed import (AffineFEOperator, AssembledPVector, Boundary, Cartesia
                           Triangulation, TrialFESpace, VectorValue, allocate_matrix, allocate_matrix_and_vector,
                           allocate_vector, assemble_matrix, assemble_matrix_, assemble_matrix_and_vector,
                           assemble_matrix_and_vector_, assemble_vector, assemble_vector_, collect_cell_matrix,
-                          collect_cell_matrix_and_vector, collect_cell_vector, integral_boundary_source,
-                          integral_elasticity, integral_grad_grad,
-                          integral_source, l2_error, lagrangian, quadrature_points, solve,
-                          with_gb300)
+                          collect_cell_matrix_and_vector, collect_cell_vector, get_dirichlet_dof_values,
+                          integral_boundary_source, integral_elasticity, integral_grad_grad,
+                          integral_source, interpolate, interpolate_dirichlet, interpolate_dirichlet_,
+                          interpolate_everywhere, interpolate_everywhere_, l2_error, lagrangian,
+                          quadrature_points, solve, with_gb300, zero_dirichlet_values, zero_free_values)
 from .dg import Skeleton, integral_sipg, integral_sipg_source
 from .multifield import (BlockMultiFieldStyle, BlockPMatrix, BlockPVector, ConsecutiveMultiFieldStyle,
                          MultiFieldFESpace, integral_multifield, integral_multifield_source,

@@ -328,34 +328,40 @@ def TrialFESpace(u, V: DistributedSingleFieldFESpace):
         L.call("gd_space_set_dirichlet", V.handle, None, L.GD_HOST)
         V.dirichlet_values = None
         return V
+    vals = _lattice_values(V, u)
+    L.call("gd_space_set_dirichlet", V.handle, L.ptr(vals, C.c_double), L.GD_HOST)
+    V.dirichlet_values = vals
+    return V
+
+
+def _lattice_values(V, u):
+    """Nodal interpolation of u over the global node lattice, in the layout of the Dirichlet
+    values: (lattice nodes,) or, on a vector space, (lattice nodes, ncomp).  u: a number, a
+    vectorised callable of the coordinates (a tuple of components on a vector space), a
+    constant vector, a dense array, or an FEFunction (its nodal values)."""
+    nn = int(np.prod(V.lattice))
+    if isinstance(u, FEFunction):
+        return u.nodal_values()
     if V.ncomp > 1:
-        nn = int(np.prod(V.lattice))
         if callable(u):
             xyz = V.lattice_xyz()
             comps = u(*[xyz[:, d] for d in range(V.model.dim)])
             if len(comps) != V.ncomp:
-                raise ValueError(f"TrialFESpace: u returns {len(comps)} components, the space has {V.ncomp}")
+                raise ValueError(f"u returns {len(comps)} components, the space has {V.ncomp}")
             vals = np.stack([np.broadcast_to(np.asarray(c, dtype=np.float64), (nn,)) for c in comps], axis=1)
         else:
             vals = np.asarray(u, dtype=np.float64)
             if vals.ndim == 1 and vals.shape[0] == V.ncomp:
                 vals = np.broadcast_to(vals, (nn, V.ncomp))
             vals = vals.reshape(nn, V.ncomp)
-        vals = np.ascontiguousarray(vals)
-        L.call("gd_space_set_dirichlet", V.handle, L.ptr(vals, C.c_double), L.GD_HOST)
-        V.dirichlet_values = vals
-        return V
+        return np.ascontiguousarray(vals)
     if callable(u):
         xyz = V.lattice_xyz()
         vals = np.asarray(u(*[xyz[:, d] for d in range(V.model.dim)]), dtype=np.float64)
-        vals = np.broadcast_to(vals, (xyz.shape[0],)).copy()
-    elif np.isscalar(u):
-        vals = np.full(int(np.prod(V.lattice)), float(u))
-    else:
-        vals = np.ascontiguousarray(u, dtype=np.float64)
-    L.call("gd_space_set_dirichlet", V.handle, L.ptr(vals, C.c_double), L.GD_HOST)
-    V.dirichlet_values = vals
-    return V
+        return np.broadcast_to(vals, (xyz.shape[0],)).copy()
+    if np.isscalar(u):
+        return np.full(nn, float(u))
+    return np.ascontiguousarray(np.asarray(u, dtype=np.float64).reshape(nn))
 
 
 # --------------------------------------------------------------------------------------
@@ -814,11 +820,18 @@ class AffineFEOperator:
 
 
 class FEFunction:
-    """``FEFunction(U, x)``: free values made consistent on every part."""
+    """``FEFunction(U, x)`` / ``FEFunction(U, x, dirichlet_values)``: free values made
+    consistent on every part; the Dirichlet values are the trial space's unless given (in
+    the trial space's layout: one value per lattice node, (nodes, ncomp) on vector spaces)."""
 
-    def __init__(self, U: DistributedSingleFieldFESpace, x: np.ndarray):
+    def __init__(self, U: DistributedSingleFieldFESpace, x: np.ndarray, dirichlet_values=None):
         self.U = U
         self.free_values = np.ascontiguousarray(x, dtype=np.float64)
+        self.dirichlet_values = (None if dirichlet_values is None
+                                 else np.ascontiguousarray(dirichlet_values, dtype=np.float64))
+
+    def _dirichlet(self):
+        return self.dirichlet_values if self.dirichlet_values is not None else self.U.dirichlet_values
 
     def local_values(self, p):
         nl, _, _ = self.U.local_sizes(p)
@@ -828,12 +841,82 @@ class FEFunction:
         return out
 
     def nodal_values(self):
-        """Dense lattice array of nodal values (Dirichlet values from the trial space)."""
-        N = int(np.prod(self.U.lattice))
-        u = np.zeros(N) if self.U.dirichlet_values is None else self.U.dirichlet_values.copy()
+        """Dense lattice array of nodal values, (nodes,) or (nodes, ncomp): free values from
+        x, Dirichlet values from this function (else from the trial space)."""
+        N, nc = int(np.prod(self.U.lattice)), self.U.ncomp
+        shape = (N,) if nc == 1 else (N, nc)
+        d = self._dirichlet()
+        u = np.zeros(shape) if d is None else np.asarray(d, dtype=np.float64).reshape(shape).copy()
         for p in range(self.U.model.num_parts):
-            u[self.U.dof_nodes(p)] = self.local_values(p)
+            nodes, vals = self.U.dof_nodes(p), self.local_values(p)
+            if nc == 1:
+                u[nodes] = vals
+            else:
+                u[nodes, np.arange(len(nodes)) % nc] = vals
         return u
+
+
+# interpolation (FESpaces.jl interpolate* on the distributed spaces; the function is
+# evaluated at the lattice nodes on the host, like the Dirichlet values of TrialFESpace)
+def zero_free_values(U: DistributedSingleFieldFESpace) -> np.ndarray:
+    return np.zeros(U.num_free_dofs())
+
+
+def zero_dirichlet_values(U: DistributedSingleFieldFESpace) -> np.ndarray:
+    N = int(np.prod(U.lattice))
+    return np.zeros(N if U.ncomp == 1 else (N, U.ncomp))
+
+
+def get_dirichlet_dof_values(U: DistributedSingleFieldFESpace) -> np.ndarray:
+    """The trial space's Dirichlet values (lattice layout; only Dirichlet nodes are read)."""
+    return zero_dirichlet_values(U) if U.dirichlet_values is None else U.dirichlet_values.copy()
+
+
+def _free_values_of(U, u) -> np.ndarray:
+    """u at every free DOF of U, global order."""
+    if isinstance(u, FEFunction) and u.U is U:
+        return u.free_values.copy()
+    lat = _lattice_values(U, u)
+    out = np.zeros(U.num_free_dofs())
+    for p in range(U.model.num_parts):
+        li = U.gids.partition()[p]
+        own = li.local_to_owner == p
+        nodes = U.dof_nodes(p)[own]
+        if U.ncomp == 1:
+            out[li.local_to_global[own]] = lat[nodes]
+        else:
+            comp = np.arange(len(li.local_to_global))[own] % U.ncomp
+            out[li.local_to_global[own]] = lat[nodes, comp]
+    return out
+
+
+def interpolate(u, U: DistributedSingleFieldFESpace) -> FEFunction:
+    """``interpolate(u, U)``: u at the free DOFs; the Dirichlet values stay the space's."""
+    return FEFunction(U, _free_values_of(U, u))
+
+
+def interpolate_everywhere(u, U: DistributedSingleFieldFESpace) -> FEFunction:
+    """``interpolate_everywhere(u, U)``: u at the free and at the Dirichlet DOFs."""
+    return FEFunction(U, _free_values_of(U, u), _lattice_values(U, u))
+
+
+def interpolate_dirichlet(u, U: DistributedSingleFieldFESpace) -> FEFunction:
+    """``interpolate_dirichlet(u, U)``: zero free values, u at the Dirichlet DOFs."""
+    return FEFunction(U, zero_free_values(U), _lattice_values(U, u))
+
+
+def interpolate_everywhere_(u, free_values, dirichlet_values, U: DistributedSingleFieldFESpace) -> FEFunction:
+    """``interpolate_everywhere!(u, free_values, dirichlet_values, U)``."""
+    free_values[...] = _free_values_of(U, u)
+    dirichlet_values[...] = np.asarray(_lattice_values(U, u)).reshape(np.shape(dirichlet_values))
+    return FEFunction(U, free_values, dirichlet_values)
+
+
+def interpolate_dirichlet_(u, free_values, dirichlet_values, U: DistributedSingleFieldFESpace) -> FEFunction:
+    """``interpolate_dirichlet!(u, free_values, dirichlet_values, U)``."""
+    free_values[...] = 0.0
+    dirichlet_values[...] = np.asarray(_lattice_values(U, u)).reshape(np.shape(dirichlet_values))
+    return FEFunction(U, free_values, dirichlet_values)
 
 
 def _gauss01(nq):
@@ -871,8 +954,18 @@ def l2_error(uh: "FEFunction", u_exact, measure: Measure) -> float:
         vals = np.broadcast_to(np.asarray(vals, dtype=np.float64), (xyz.shape[0],))
     vals = np.ascontiguousarray(vals, dtype=np.float64).reshape(-1)
     err = C.c_double()
-    L.call("gd_l2_error", U.handle, L.vptr(uh.free_values), L.vptr(vals), int(measure.degree), L.GD_HOST,
-           C.byref(err))
+    # a function with its own Dirichlet values: the space carries them for this call
+    own = uh.dirichlet_values
+    swap = own is not None and own is not U.dirichlet_values
+    if swap:
+        L.call("gd_space_set_dirichlet", U.handle, L.ptr(own, C.c_double), L.GD_HOST)
+    try:
+        L.call("gd_l2_error", U.handle, L.vptr(uh.free_values), L.vptr(vals), int(measure.degree), L.GD_HOST,
+               C.byref(err))
+    finally:
+        if swap:
+            L.call("gd_space_set_dirichlet", U.handle,
+                   None if U.dirichlet_values is None else L.ptr(U.dirichlet_values, C.c_double), L.GD_HOST)
     return err.value
 
 

@@ -97,3 +97,41 @@ def test_vector_l2_norm_matches_componentwise_oracle(backend):
         comps[comp, nodes] = x[li.local_to_global]
     ref = np.sqrt(sum(go.l2_error(pb, comps[c], lambda x_, y_, z_: 0.0) ** 2 for c in range(3)))
     assert abs(dev - ref) <= 1e-10 * ref
+
+
+@pytest.mark.parametrize("parts", [(2, 2), (1, 1), (2, 1), (1, 2)])
+def test_fespaces_interpolation_kat_on_gpu(backend, parts):
+    """test/FESpacesTests.jl:88-139 (`_interpolation_tests` with a Julia function): Q1 on
+    (0,4)^2, 4 x 4 cells, u = x+y, U = TrialFESpace(u, V).  interpolate, interpolate_everywhere
+    (of u and of an FEFunction), interpolate_everywhere!, interpolate_dirichlet(!), and
+    FEFunction(U, free, dirichlet): L2 error of u - uh < 1e-9 (degree 3), computed on the device.
+    Then a space with zero Dirichlet values: a function carrying its own Dirichlet values is
+    measured with them, and afterwards the space's own (zero) values are back in place."""
+    import gridap_gb300 as G
+    u = lambda x, y: x + y
+    ranks = backend.distribute(range(int(np.prod(parts))))
+    model = G.CartesianDiscreteModel(ranks, parts, (0, 4, 0, 4), (4, 4))
+    reffe = G.ReferenceFE(G.lagrangian, float, 1)
+    V = G.TestFESpace(model, reffe, dirichlet_tags="boundary")
+    U = G.TrialFESpace(u, V)
+    dO = G.Measure(G.Triangulation(model), 3)
+    err = lambda uh: G.l2_error(uh, u, dO)
+    assert G.zero_free_values(U).shape == (U.num_free_dofs(),)
+    assert err(G.interpolate(u, U)) < 1e-9
+    free_values = G.zero_free_values(U)
+    dirichlet_values = G.get_dirichlet_dof_values(U)
+    uh_dir = G.interpolate_dirichlet_(u, free_values, dirichlet_values, U)
+    assert np.all(uh_dir.free_values == 0.0)
+    uh_e = G.interpolate_everywhere(u, U)
+    assert err(uh_e) < 1e-9
+    uh_e_ = G.interpolate_everywhere_(u, free_values, G.zero_dirichlet_values(U), U)
+    assert err(uh_e_) < 1e-9
+    assert err(G.interpolate_everywhere(uh_e, U)) < 1e-9
+    assert err(G.interpolate_everywhere_(uh_e, free_values, dirichlet_values, U)) < 1e-9
+    assert err(G.FEFunction(U, free_values, dirichlet_values)) < 1e-9
+
+    V0 = G.TestFESpace(model, reffe, dirichlet_tags="boundary")
+    U0 = G.TrialFESpace(0.0, V0)
+    assert err(G.interpolate_everywhere(u, U0)) < 1e-9     # its own Dirichlet values
+    assert err(G.interpolate(u, U0)) > 1e-2                # the space's zero values again
+    assert err(G.interpolate_dirichlet(u, U0)) > 1e-2      # zero free values
