@@ -109,3 +109,16 @@ def test_golden_fixture_reproduces(fixture):
         assert np.array_equal(g[f"p{p}_gcol_gid"], M.col_ghost_gids)
         assert np.allclose(g[f"p{p}_vals"], M.vals, rtol=0, atol=1e-13)
         assert np.allclose(g[f"p{p}_b"], M.b, rtol=0, atol=1e-13)
+
+
+def test_c1_q2_128_solution_kat():
+    """The C1 configuration at full size (2D Q2, 128^2 cells, parts (2,2), degree 4,
+    u = (x+y)^2 on the boundary, f = -4): the known answer of test/PoissonTests.jl:14-45
+    holds for the oracle's assembly and gathered LU at the size the GPU parity test uses
+    (L2 error < 1e-9; the discretisation reproduces (x+y)^2 exactly)."""
+    u = lambda x, y: (x + y) ** 2
+    pb = make_problem(2, (128, 128), (2, 2), 2, f=-4.0, u=u)
+    fe = go.build_fespace(pb)
+    assert fe.dofs[0].ngdofs == 255 * 255
+    x = go.solve_lu(go.assemble(pb, fe, "sub"), fe.dofs[0].ngdofs)
+    assert go.l2_error(pb, go.nodal_solution(pb, fe, x), u) < 1e-9
