@@ -217,12 +217,16 @@ __global__ void k_numeric_rhs(Geom g, int64_t nrows_own, const int32_t* __restri
 
 
 // ---- Q1 fast path: one thread per owned row, values staged in shared memory ----------------
-// Each thread loads the kappa of the 2^DIM cells around its node once and forms the
-// whole 3^DIM stencil in registers (64 FMAs in 3D, unrolled at compile time); the row's
-// pattern id gives the CSR position of every neighbour.  A 128-row chunk of values
-// is contiguous in the CSR value array; it is written into a shared-memory buffer and
-// streamed to global memory with one TMA bulk store (cp.async.bulk), double-buffered
-// so the store of one chunk overlaps the computation of the next.  The right-hand side
+// Each thread loads the coefficients of the 2^DIM cells around its node once and forms
+// the whole 3^DIM stencil in registers from class sums (q1_row_values: on cube cells
+// about 16 FP64 operations per 3D row, a separable subset-sum tree on other boxes); the
+// row's pattern id gives the CSR position of every neighbour.  A chunk of consecutive
+// rows (64, 128 or 256, the launch shape the autotuner picks, with one or two staging
+// buffers) is contiguous in the CSR value array; it is written into a shared-memory
+// buffer and streamed to global memory with one TMA bulk store (cp.async.bulk), the
+// unaligned first and last entries by plain stores, double-buffered so that the store of
+// one chunk overlaps the computation of the next.  The row ids, patterns and coefficients
+// of the next chunk are prefetched while the current one is stored.  The right-hand side
 // (source term and Dirichlet lifting) is fused.  Per row the kernel reads 4 bytes of
 // node id and 2 bytes of pattern id; per entry it only writes the value.
 constexpr int kQ1Rows = 128;
@@ -938,6 +942,14 @@ extern "C" int gd_assembler_tuning(const gd_asm* A, int32_t* shape, int32_t* row
   if (ms)
     for (int i = 0; i < gd::kNumQ1Shapes; ++i) ms[i] = A->q1_shape_ms[i];
   if (nshapes) *nshapes = gd::kNumQ1Shapes;
+  return GD_OK;
+}
+
+extern "C" int gd_assembler_set_shape(gd_asm* A, int shape) {
+  if (!A || !A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_set_shape: run gd_assemble_symbolic first");
+  if (!A->fast_q1) return gd::fail(GD_ERR_UNSUPPORTED, "gd_assembler_set_shape: the assembler does not use the Q1 kernel");
+  if (shape < -1 || shape >= gd::kNumQ1Shapes) return gd::fail(GD_ERR_ARG, "gd_assembler_set_shape: shape out of range");
+  A->q1_shape = shape;   // -1: the next numeric assembly times every shape again
   return GD_OK;
 }
 

@@ -9,7 +9,6 @@
 // deterministic two-stage reductions.
 #include <chrono>
 #include <cmath>
-#include <mutex>
 #include <string>
 
 #include "gd_internal.h"
@@ -24,10 +23,14 @@ constexpr int kStageBatch = 8;                   // staging loads per thread in 
 constexpr int kVecThreads = 256;
 constexpr int kMaxPartials = 1024;             // blocks that write partial sums
 
+// CG scalars on the device.  tol2 = (rtol |b|)^2: once r.r falls to it, `done` is set, the
+// step count `iters` stops and later steps take alpha = 0 (x and r stay as they are), so
+// the host, which checks every few steps, reads the exact iteration count.
 struct Scalars {
-  double rz, pq, alpha, beta, rr, bb, rz_new;
-  int32_t done;
+  double rz, pq, alpha, beta, rr, bb, rz_new, tol2;
+  int32_t done, iters;
 };
+static_assert(sizeof(Scalars) <= 16 * sizeof(double), "Scalars must fit its 16-double slot");
 
 __device__ inline double block_sum(double v, double* sh) {
   for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
@@ -433,12 +436,23 @@ __global__ void k_pcg_scalars(int mode, int nb, const double* __restrict__ pa, c
     sc->rr = sb;
   } else if (mode == 1) {
     sc->pq = sa;
-    sc->alpha = sa != 0.0 ? sc->rz / sa : 0.0;
+    sc->alpha = (!sc->done && sa != 0.0) ? sc->rz / sa : 0.0;
   } else {
     sc->beta = sc->rz != 0.0 ? sa / sc->rz : 0.0;
     sc->rz = sa;
     sc->rr = sb;
+    if (!sc->done) {
+      ++sc->iters;
+      if (sb <= sc->tol2) sc->done = 1;
+    }
   }
+}
+
+// Starts a CG cycle: no step taken yet, stop at r.r <= tol2.
+__global__ void k_pcg_arm(Scalars* __restrict__ sc, double tol2) {
+  sc->tol2 = tol2;
+  sc->done = 0;
+  sc->iters = 0;
 }
 
 __global__ void k_gather_local(int64_t n, const int64_t* __restrict__ lid_gid, const double* __restrict__ xg,
@@ -588,12 +602,123 @@ extern "C" int gd_solve(gd_asm* A, int method, double rtol, int maxit, double* x
                         A->numeric_epoch);
 }
 
+namespace gd {
+
+// Device buffers of one FP64 Jacobi-PCG: five vectors, the inverse diagonal, two arrays of
+// per-block partial sums, the scalars and the bad-diagonal counter.
+struct PcgBufs {
+  double *x, *r, *z, *p, *q, *dinv, *pa, *pb;
+  Scalars* sc;
+  int32_t* bad;
+};
+
+// Every DOF is a Dirichlet DOF: nothing to solve.
+static int pcg_empty(gd_solve_stats* stats, std::chrono::steady_clock::time_point t0) {
+  if (stats) {
+    stats->iterations = 0;
+    stats->converged = 1;
+    stats->rel_residual = 0.0;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  return GD_OK;
+}
+
+// The FP64 Jacobi-PCG iteration shared by gd_solve and gd_solve_noalloc; `spmv` (y = A p
+// with partials of p.y) and `residual` (r = b - A x with partials of r.r and b.b) launch
+// the matrix kernels on gs blocks, the vector kernels run on gv.  CG checks the recursive
+// residual every few steps on the host; when it meets the tolerance but the true residual
+// (recomputed in FP64) does not -- rounding makes the two drift apart near tight
+// tolerances -- CG restarts from the true residual, at most kMaxRestarts times.
+template <typename SpmvF, typename ResidF>
+static int pcg_run(const char* fn, int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals,
+                   const PcgBufs& B, int gs, int gv, SpmvF& spmv, ResidF& residual, cudaStream_t st, double rtol,
+                   int maxit, double* x, int where, gd_solve_stats* stats,
+                   std::chrono::steady_clock::time_point t0) {
+  const std::string name(fn);
+  GD_CUDA_TRY(cudaMemsetAsync(B.bad, 0, sizeof(int32_t), st));
+  GD_CUDA_TRY(cudaMemsetAsync(B.x, 0, sizeof(double) * n, st));
+  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, rowptr, colgid, vals, B.dinv, B.bad);
+  GD_CUDA_TRY(cudaGetLastError());
+  // r = b - A*0 = b ; bb
+  residual(B.x, B.r, B.pa, B.pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, B.pb, B.pa, B.sc);   // rz <- bb (temp), rr <- rr
+  GD_CUDA_TRY(cudaGetLastError());
+  Scalars h{};
+  int32_t hbad = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&h, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, B.bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hbad)
+    return fail(GD_ERR_NUMERIC, name + ": non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
+  const double bnorm = std::sqrt(h.rz);
+  const double tol2 = (rtol * bnorm) * (rtol * bnorm);
+  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, B.dinv, B.r, B.z, B.p, B.pa, B.pb);
+  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, B.pa, B.pb, B.sc);
+  k_pcg_arm<<<1, 1, 0, st>>>(B.sc, tol2);
+  GD_CUDA_TRY(cudaGetLastError());
+  int launched = 0, taken = 0;
+  bool conv = bnorm == 0.0;
+  const int check_every = 8;
+  constexpr int kMaxRestarts = 3;
+  for (int restart = 0;; ++restart) {
+    int cycle = 0;
+    while (!conv && launched < maxit) {
+      const int nstep = std::min(check_every, maxit - launched);
+      for (int s = 0; s < nstep; ++s) {
+        spmv(B.p, B.q, B.p, B.pa);
+        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, B.pa, nullptr, B.sc);
+        k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, B.sc, B.x, B.r, B.z, B.p, B.q, B.dinv, B.pa, B.pb);
+        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, B.pa, B.pb, B.sc);
+        k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, B.sc, B.z, B.p);
+      }
+      GD_CUDA_TRY(cudaGetLastError());
+      launched += nstep;
+      GD_CUDA_TRY(cudaMemcpyAsync(&h, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+      GD_CUDA_TRY(cudaStreamSynchronize(st));
+      cycle = h.iters;
+      if (!std::isfinite(h.rr)) break;
+      if (h.done) conv = true;
+    }
+    taken += cycle;
+    // true FP64 residual (kept in r for a restart)
+    residual(B.x, B.r, B.pa, B.pb);
+    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, B.pa, B.pb, B.sc);
+    GD_CUDA_TRY(cudaGetLastError());
+    GD_CUDA_TRY(cudaMemcpyAsync(&h, B.sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+    const double rel_true = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
+    if (!conv || rel_true <= rtol || !std::isfinite(rel_true) || launched >= maxit || restart >= kMaxRestarts) break;
+    conv = false;
+    k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, B.dinv, B.r, B.z, B.p, B.pa, B.pb);
+    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, B.pa, B.pb, B.sc);
+    k_pcg_arm<<<1, 1, 0, st>>>(B.sc, tol2);
+    GD_CUDA_TRY(cudaGetLastError());
+  }
+  GD_CUDA_TRY(cudaMemcpyAsync(x, B.x, sizeof(double) * n,
+                              where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  const double rel = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
+  if (stats) {
+    stats->iterations = taken;
+    stats->converged = rel <= rtol;
+    stats->rel_residual = rel;
+    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+  }
+  if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, name + ": residual is not finite");
+  if (rel > rtol)
+    return fail(GD_ERR_NOTCONVERGED, name + ": tolerance not reached in " + std::to_string(taken) + " iterations");
+  return GD_OK;
+}
+
+}  // namespace gd
+
 // FP64 Jacobi-PCG on the owned rows of a CSR (global column ids); workspace buffers are
 // (re)allocated as needed: w (5 n: x r z p q), dinv (n), dred (partials and scalars).
 int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, const double* vals, const double* rhs,
                    DBuf<double>& w, DBuf<double>& dinvb, DBuf<double>& dred, cudaStream_t st, double rtol, int maxit,
                    double* x, int where, gd_solve_stats* stats, SellMat* sell, int64_t version) {
   auto t0 = std::chrono::steady_clock::now();
+  if (n == 0) return pcg_empty(stats, t0);
   // rows per lane group from the average row length; below 48 entries one thread per row
   // on the sliced-ELL copy (the caller's cached one, else a temporary freed on return)
   int64_t nnz = 0;
@@ -638,86 +763,19 @@ int gd::jacobi_pcg_csr(int64_t n, const int64_t* rowptr, const int32_t* colgid, 
   if (w.n < (size_t)(5 * n)) GD_TRY(dalloc(w, 5 * std::max<int64_t>(n, 1)));
   if (dinvb.n < (size_t)n) GD_TRY(dalloc(dinvb, std::max<int64_t>(n, 1)));
   if (!dred.p) GD_TRY(dalloc(dred, 4096));
-  double* dinv = dinvb.p;
-  double* dx = w.p;
-  double* dr = dx + n;
-  double* dz = dr + n;
-  double* dp = dz + n;
-  double* dq = dp + n;
-  double* pa = dred.p + 16;
-  double* pb = pa + kMaxPartials;
-  Scalars* sc = (Scalars*)(dred.p + 16 + 2 * kMaxPartials);
-  int32_t* bad = (int32_t*)dred.p;
-  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
-  GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
-  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, rowptr, colgid, vals, dinv, bad);
-  GD_CUDA_TRY(cudaGetLastError());
-  const int gs = gsg;
-  const int gv = grid_for(n, kVecThreads);
-  // r = b - A*0 = b ; bb
-  residual(dx, dr, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);   // rz <- bb (temp), rr <- rr
-  GD_CUDA_TRY(cudaGetLastError());
-  Scalars h{};
-  int32_t hbad = 0;
-  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
-  if (hbad) return fail(GD_ERR_NUMERIC, "gd_solve: non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
-  const double bnorm = std::sqrt(h.rz);
-  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
-  GD_CUDA_TRY(cudaGetLastError());
-  int it = 0;
-  bool conv = bnorm == 0.0;
-  const int check_every = 8;
-  // When the recursive residual meets the tolerance but the true one (recomputed in FP64)
-  // does not -- rounding makes the two drift apart near tight tolerances -- CG restarts
-  // from the true residual, at most kMaxRestarts times.
-  constexpr int kMaxRestarts = 3;
-  for (int restart = 0;; ++restart) {
-    while (!conv && it < maxit) {
-      int nstep = std::min(check_every, maxit - it);
-      for (int s = 0; s < nstep; ++s) {
-        spmv(dp, dq, dp, pa);
-        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
-        k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, dinv, pa, pb);
-        k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
-        k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
-      }
-      GD_CUDA_TRY(cudaGetLastError());
-      it += nstep;
-      GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-      GD_CUDA_TRY(cudaStreamSynchronize(st));
-      if (!std::isfinite(h.rr)) break;
-      if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
-    }
-    // true FP64 residual (kept in r for a restart)
-    residual(dx, dr, pa, pb);
-    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
-    GD_CUDA_TRY(cudaGetLastError());
-    GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-    GD_CUDA_TRY(cudaStreamSynchronize(st));
-    const double rel_true = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
-    if (!conv || rel_true <= rtol || !std::isfinite(rel_true) || it >= maxit || restart >= kMaxRestarts) break;
-    conv = false;
-    k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
-    k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
-    GD_CUDA_TRY(cudaGetLastError());
-  }
-  GD_CUDA_TRY(cudaMemcpyAsync(x, dx, sizeof(double) * n,
-                              where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
-  const double rel = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
-  if (stats) {
-    stats->iterations = it;
-    stats->converged = rel <= rtol;
-    stats->rel_residual = rel;
-    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
-  if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, "gd_solve: residual is not finite");
-  if (rel > rtol) return fail(GD_ERR_NOTCONVERGED, "gd_solve: tolerance not reached in " + std::to_string(it) + " iterations");
-  return GD_OK;
+  PcgBufs B;
+  B.x = w.p;
+  B.r = B.x + n;
+  B.z = B.r + n;
+  B.p = B.z + n;
+  B.q = B.p + n;
+  B.dinv = dinvb.p;
+  B.pa = dred.p + 16;
+  B.pb = B.pa + kMaxPartials;
+  B.sc = (Scalars*)(dred.p + 16 + 2 * kMaxPartials);
+  B.bad = (int32_t*)dred.p;
+  return pcg_run("gd_solve", n, rowptr, colgid, vals, B, gsg, grid_for(n, kVecThreads), spmv, residual, st, rtol, maxit,
+                 x, where, stats, t0);
 }
 
 extern "C" int gd_fe_function_local(const gd_space* S, int part, const double* x_global, int where, double* x_local) {
@@ -759,16 +817,19 @@ extern "C" int gd_fe_function_local(const gd_space* S, int part, const double* x
 // or time-stepping loop in which a cudaMalloc -- which may synchronise the whole
 // device, or fail part-way through a run -- is not acceptable.  gd_solve allocates
 // its Jacobi-PCG workspace on first use; gd_solve_noalloc runs the same iteration
+// (pcg_run: the same steps, restarts from the true FP64 residual and stopping rule)
 // with every scratch vector, partial sum and scalar in one file-scope device array
-// instead, so it calls no cudaMalloc/cudaFree at all.
+// instead, so it calls no cudaMalloc/cudaFree at all.  Its matrix kernel is the CSR
+// one (k_spmv / k_residual: one thread per row, entries staged through shared memory),
+// since the sliced-ELL copy that gd_solve builds for short rows would need memory.
 //
 // Limits and rules (also stated in gdgpu.h):
 //  * at most kNoAllocMaxDofs global DOFs; larger systems are rejected with GD_ERR_ARG;
 //  * the array (about 12.6 MB) is held by every device that loads the library, until
 //    the process exits;
-//  * the first call on a device looks the array's device address up
-//    (cudaGetSymbolAddress) with that device current; make that first call before
-//    any stream capture;
+//  * every call looks the array's device address up (cudaGetSymbolAddress, which
+//    allocates nothing) with the assembler's device current, and puts the caller's
+//    current device back before it returns;
 //  * every call shares the one array and it keeps the last call's contents: each call
 //    clears what must start at zero, and calls that overlap on the GPU (other streams,
 //    other host threads) race on it.
@@ -780,24 +841,30 @@ constexpr int64_t kNoAllocDoubles = 6 * kNoAllocMaxDofs + 2 * kMaxPartials + 64;
 
 static __device__ __align__(256) double g_noalloc_scratch[kNoAllocDoubles];
 
-constexpr int kNoAllocMaxDevices = 64;
-static std::mutex g_noalloc_mutex;
-static double* g_noalloc_ptr[kNoAllocMaxDevices] = {nullptr};
-
-// Device address of the scratch array for the current device (looked up once per device).
-static int noalloc_scratch(double** out) {
-  int dev = 0;
-  GD_CUDA_TRY(cudaGetDevice(&dev));
-  if (dev < 0 || dev >= kNoAllocMaxDevices) return fail(GD_ERR_UNSUPPORTED, "gd_solve_noalloc: device index too large");
-  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-  if (!g_noalloc_ptr[dev]) {
-    void* p = nullptr;
-    const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-    if (e != cudaSuccess || !p)
-      return fail(GD_ERR_CUDA, std::string("gd_solve_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
-    g_noalloc_ptr[dev] = static_cast<double*>(p);
+// Makes `dev` current for the lifetime of the guard, then restores the caller's device.
+struct DeviceGuard {
+  int prev = -1;
+  bool changed = false;
+  int set(int dev) {
+    GD_CUDA_TRY(cudaGetDevice(&prev));
+    if (prev != dev) {
+      GD_CUDA_TRY(cudaSetDevice(dev));
+      changed = true;
+    }
+    return GD_OK;
   }
-  *out = g_noalloc_ptr[dev];
+  ~DeviceGuard() {
+    if (changed) cudaSetDevice(prev);
+  }
+};
+
+// Device address of the scratch array on the current device.
+static int noalloc_scratch(double** out) {
+  void* p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p)
+    return fail(GD_ERR_CUDA, std::string("gd_solve_noalloc: cudaGetSymbolAddress failed: ") + cudaGetErrorString(e));
+  *out = static_cast<double*>(p);
   return GD_OK;
 }
 
@@ -810,77 +877,37 @@ extern "C" int gd_solve_noalloc(gd_asm* A, double rtol, int maxit, double* x, in
   if (n > kNoAllocMaxDofs)
     return fail(GD_ERR_ARG, "gd_solve_noalloc: " + std::to_string(n) + " DOFs exceed the static scratch limit of " +
                                 std::to_string(kNoAllocMaxDofs) + " (use gd_solve)");
-  GD_CUDA_TRY(cudaSetDevice(A->test->model->ctx->device));
+  auto t0 = std::chrono::steady_clock::now();
+  if (n == 0) return pcg_empty(stats, t0);
+  DeviceGuard guard;
+  GD_TRY(guard.set(A->test->model->ctx->device));
   double* base = nullptr;
   GD_TRY(noalloc_scratch(&base));
   cudaStream_t st = A->test->model->ctx->stream;
-  auto t0 = std::chrono::steady_clock::now();
-  double* dx = base;
-  double* dr = base + 1 * kNoAllocMaxDofs;
-  double* dz = base + 2 * kNoAllocMaxDofs;
-  double* dp = base + 3 * kNoAllocMaxDofs;
-  double* dq = base + 4 * kNoAllocMaxDofs;
-  double* dinv = base + 5 * kNoAllocMaxDofs;
-  double* pa = base + 6 * kNoAllocMaxDofs;
-  double* pb = pa + kMaxPartials;
-  Scalars* sc = reinterpret_cast<Scalars*>(pb + kMaxPartials);
-  int32_t* bad = reinterpret_cast<int32_t*>(pb + kMaxPartials + 16);
-  // the array keeps the previous call's contents: clear what must start at zero
-  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
-  GD_CUDA_TRY(cudaMemsetAsync(dx, 0, sizeof(double) * n, st));
-  k_dinv<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dinv, bad);
-  GD_CUDA_TRY(cudaGetLastError());
+  PcgBufs B;
+  B.x = base;
+  B.r = base + 1 * kNoAllocMaxDofs;
+  B.z = base + 2 * kNoAllocMaxDofs;
+  B.p = base + 3 * kNoAllocMaxDofs;
+  B.q = base + 4 * kNoAllocMaxDofs;
+  B.dinv = base + 5 * kNoAllocMaxDofs;
+  B.pa = base + 6 * kNoAllocMaxDofs;
+  B.pb = B.pa + kMaxPartials;
+  B.sc = reinterpret_cast<Scalars*>(B.pb + kMaxPartials);          // a 16-double slot
+  B.bad = reinterpret_cast<int32_t*>(B.pb + kMaxPartials + 16);   // after it
+  const int64_t* rowptr = A->rowptr.p;
+  const int32_t* col = A->colgid.p;
+  const double* val = A->vals.p;
+  const double* rhs = A->rhs.p;
   const int gs = grid_for(n, kRowsPerSpmvBlock);
-  const int gv = grid_for(n, kVecThreads);
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, dr, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pb, pa, sc);
-  GD_CUDA_TRY(cudaGetLastError());
-  Scalars h{};
-  int32_t hbad = 0;
-  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
-  if (hbad) return fail(GD_ERR_NUMERIC, "gd_solve_noalloc: non-positive or missing diagonal in " + std::to_string(hbad) + " rows");
-  const double bnorm = std::sqrt(h.rz);
-  k_pcg_init<<<gv, kVecThreads, 0, st>>>(n, dinv, dr, dz, dp, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gv, pa, pb, sc);
-  GD_CUDA_TRY(cudaGetLastError());
-  int it = 0;
-  bool conv = bnorm == 0.0;
-  const int check_every = 8;
-  while (!conv && it < maxit) {
-    const int nstep = std::min(check_every, maxit - it);
-    for (int s = 0; s < nstep; ++s) {
-      k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dp, dq, dp, pa);
-      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(1, gs, pa, nullptr, sc);
-      k_pcg_update<<<gv, kVecThreads, 0, st>>>(n, sc, dx, dr, dz, dp, dq, dinv, pa, pb);
-      k_pcg_scalars<<<1, kVecThreads, 0, st>>>(2, gv, pa, pb, sc);
-      k_pcg_pupdate<<<gv, kVecThreads, 0, st>>>(n, sc, dz, dp);
-    }
-    GD_CUDA_TRY(cudaGetLastError());
-    it += nstep;
-    GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-    GD_CUDA_TRY(cudaStreamSynchronize(st));
-    if (!std::isfinite(h.rr)) break;
-    if (std::sqrt(h.rr) <= rtol * bnorm) conv = true;
-  }
-  k_residual<<<gs, kSpmvThreads, 0, st>>>(n, A->rowptr.p, A->colgid.p, A->vals.p, dx, A->rhs.p, nullptr, pa, pb);
-  k_pcg_scalars<<<1, kVecThreads, 0, st>>>(0, gs, pa, pb, sc);
-  GD_CUDA_TRY(cudaGetLastError());
-  GD_CUDA_TRY(cudaMemcpyAsync(&h, sc, sizeof(Scalars), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaMemcpyAsync(x, dx, sizeof(double) * n,
-                              where == GD_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st));
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
-  const double rel = bnorm > 0.0 ? std::sqrt(h.rz) / bnorm : 0.0;
-  if (stats) {
-    stats->iterations = it;
-    stats->converged = rel <= rtol;
-    stats->rel_residual = rel;
-    stats->seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-  }
-  if (!std::isfinite(rel)) return fail(GD_ERR_NUMERIC, "gd_solve_noalloc: residual is not finite");
-  if (rel > rtol) return fail(GD_ERR_NOTCONVERGED, "gd_solve_noalloc: tolerance not reached in " + std::to_string(it) + " iterations");
-  return GD_OK;
+  auto spmv = [&](const double* xin, double* yout, const double* wdot, double* part) {
+    k_spmv<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, col, val, xin, yout, wdot, part);
+  };
+  auto residual = [&](const double* xin, double* rout, double* prr, double* pbb) {
+    k_residual<<<gs, kSpmvThreads, 0, st>>>(n, rowptr, col, val, xin, rhs, rout, prr, pbb);
+  };
+  return pcg_run("gd_solve_noalloc", n, rowptr, col, val, B, gs, grid_for(n, kVecThreads), spmv, residual, st, rtol,
+                 maxit, x, where, stats, t0);
 }
 
 // x = A \ b for a caller-given right-hand side (device or host), same methods as gd_solve.

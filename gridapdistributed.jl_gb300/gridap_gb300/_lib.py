@@ -90,6 +90,7 @@ SIGNATURES = {
     "gd_assembler_phase_times": [P, DP, DP, DP],
     "gd_assembler_counts": [P, I64P, I64P, I64P, I32P],
     "gd_assembler_tuning": [P, I32P, I32P, I32P, C.POINTER(C.c_float), I32P],
+    "gd_assembler_set_shape": [P, C.c_int],
     "gd_matrix_sizes": [P, C.c_int, I64P, I64P, I64P, I64P, I64P],
     "gd_matrix_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, I64P, I32P],
     "gd_vector_export": [P, C.c_int, DP],

@@ -806,6 +806,7 @@ class AffineFEOperator:
         from .dg import DistributedDGFESpace, assemble_dg
         from .multifield import MultiFieldAssembler, assemble_multifield
         self.U, self.V = U, V
+        self.a, self.l = a, l
         if isinstance(V, DistributedDGFESpace):
             if U is not V or assem is not None:
                 raise NotImplementedError("DG: trial space = test space, the built-in assembly")

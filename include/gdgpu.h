@@ -187,8 +187,9 @@ int gd_add_boundary_source(gd_asm* a, const int32_t* sides, const double* g_qp, 
 
 /* Record CUDA events around the phases of every numeric assembly (off by default). */
 int gd_assembler_set_profiling(gd_asm* a, int on);
-/* Event-timed durations (ms) of the last profiled numeric assembly: clearing the
- * ghost-row values, the matrix-value kernel, the right-hand-side kernel. */
+/* Event-timed durations (ms) of the last profiled numeric assembly: the coefficient
+ * pre-scaling (k_prescale on 3D Q1 cube cells, empty otherwise), the matrix-value kernel,
+ * the right-hand-side kernel (empty where the matrix kernel computes the rhs too). */
 int gd_assembler_phase_times(const gd_asm* a, double* ms_ghost_zero, double* ms_matrix, double* ms_rhs);
 /* Counts of the assembled system: global DOFs, stored entries of the owned rows,
  * stored entries of all rows (owned + ghost), and the kernels one numeric
@@ -201,6 +202,11 @@ int gd_assembler_counts(const gd_asm* a, int64_t* ngdofs, int64_t* nnz_owned, in
  * chunk, staging buffers, and the measured ms of each of the `nshapes` candidates. */
 int gd_assembler_tuning(const gd_asm* a, int32_t* shape, int32_t* rows, int32_t* nbuf, float* ms_per_shape,
                         int32_t* nshapes);
+/* Fix the launch shape of the Q1 numeric kernel (0 .. nshapes-1 of gd_assembler_tuning)
+ * for the following numeric assemblies, or -1 to have the next one time every shape
+ * again.  Every shape writes the same values; this exists to check that.  GD_ERR_UNSUPPORTED
+ * when the assembler does not use the Q1 kernel. */
+int gd_assembler_set_shape(gd_asm* a, int shape);
 
 /* Sizes of one part's local matrix: rows (owned + ghost), columns (owned + ghost),
  * stored entries, ghost rows, ghost columns. */
@@ -244,13 +250,15 @@ int gd_solve_rhs(gd_asm* a, int method, double rtol, int maxit, const double* b,
 /* gd_solve without device allocation.  No counterpart in the reference: for callers
  * that cannot allocate device memory while they run (an application whose device
  * memory belongs to its own pool allocator, or a loop where a cudaMalloc -- which can
- * synchronise the device or fail mid-run -- is not acceptable).  Same Jacobi-PCG and
- * arguments as gd_solve; all scratch lives in one file-scope device array of fixed size
- * (about 12.6 MB per device that loads the library, held until the process exits).
- * At most 262,144 global DOFs: larger systems return GD_ERR_ARG.  The first call on a
- * device looks up the array's address with that device current: make it before any
- * stream capture.  Every call shares the array and clears what must start at zero;
- * calls that overlap on the GPU race on it. */
+ * synchronise the device or fail mid-run -- is not acceptable).  The Jacobi-PCG
+ * iteration of gd_solve (same steps, restarts and stopping rule; the matrix kernel is
+ * the CSR one, where gd_solve uses a sliced-ELL copy for short rows) with the same
+ * arguments; all scratch lives in one file-scope device array of fixed size (about
+ * 12.6 MB per device that loads the library, held until the process exits).  At most
+ * 262,144 global DOFs: larger systems return GD_ERR_ARG.  Each call looks the array's
+ * address up with the assembler's device current and restores the caller's current
+ * device before it returns.  Every call shares the array and clears what must start at
+ * zero; calls that overlap on the GPU race on it. */
 int gd_solve_noalloc(gd_asm* a, double rtol, int maxit, double* x, int where, gd_solve_stats* stats);
 /* sqrt(sum(int(abs2(u - u_h)) dOmega)) (test/PoissonTests.jl:43-45): u_h = FEFunction(U, x)
  * with x the global free values (dim components interleaved on vector spaces) and the

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import gridap_oracle as go
-from helpers import make_problem, row_scaled_error
+from helpers import gpu_system, make_problem, row_scaled_error
 
 pytestmark = pytest.mark.gpu
 
@@ -22,23 +22,6 @@ def backend():
     be = G.GB300Backend(0)
     yield be
     be.close()
-
-
-def gpu_system(backend, pb, strategy):
-    import gridap_gb300 as G
-    ranks = backend.distribute(range(int(np.prod(pb.np))))
-    model = G.CartesianDiscreteModel(ranks, pb.np, pb.domain, pb.n)
-    tags = ["left", "right", "bottom", "top", "back", "front"]
-    sides = [t for t, s in zip(tags, pb.dirichlet_sides) if s]
-    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, pb.order), dirichlet_tags=sides)
-    U = G.TrialFESpace(pb.u_dir, V) if pb.u_dir is not None else G.TrialFESpace(0.0, V)
-    dO = G.Measure(G.Triangulation(model), pb.degree)
-    a = G.integral_grad_grad(pb.kappa, dO)
-    l = G.integral_source(pb.f_nodal if pb.f_nodal is not None else pb.f_const, dO)
-    strat = G.SubAssembledRows() if strategy == "sub" else G.FullyAssembledRows()
-    assem = G.SparseMatrixAssembler(U, V, strat)
-    op = G.AffineFEOperator(a, l, U, V, assem)
-    return model, V, U, op
 
 
 CASES = [
