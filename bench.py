@@ -68,6 +68,8 @@ def parse():
     ap.add_argument("--no-elasticity-solve", dest="elasticity_solve", action="store_false",
                     help="skip the elasticity solves to 1e-8 (about 30 s)")
     ap.add_argument("--elasticity-cells", type=int, default=64, help="cells per direction of the elasticity workload")
+    ap.add_argument("--no-qp", action="store_true", help="skip the Gauss-point elasticity section (tensor cores)")
+    ap.add_argument("--qp-cells", type=int, default=64, help="cells per direction of the Gauss-point workload")
     return ap.parse_args()
 
 
@@ -214,6 +216,18 @@ def measured_peaks():
         d = json.loads(p.read_text())
         return float(d["hbm_gbs"]), "measured"
     return 6800.0, "fallback"
+
+
+def measured_tensor_peak(sustained=True):
+    """Dense BF16 tensor throughput (TFLOP/s) of this machine's GPUs: the measured
+    seconds-long figure (a kernel timed inside a longer step) or the burst one."""
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        key = "bf16_tflops_sustained" if sustained else "bf16_tflops"
+        if key in d:
+            return float(d[key]), "measured"
+    return (1700.0 if sustained else 1900.0), "fallback"
 
 
 def profiled_traffic(workload_name):
@@ -430,6 +444,154 @@ def run_elasticity(args, be, stream, dev):
             except Exception as e:   # not converged within maxit
                 out[f"solve_{name}"] = {"seconds": time.perf_counter() - t0, "error": str(e)[:200]}
     del assem, U, V, model
+    return out
+
+
+# ------------------------------------------------------------------------------------
+# elasticity with E at the Gauss points: element matrices on the tensor cores
+# ------------------------------------------------------------------------------------
+def run_qp(args, be, stream, dev):
+    """64^3 vector-Q2 elasticity with E = exp(g) known at the 27 Gauss points of every
+    cell: K_e = sum_q E_q H_q formed by the tcgen05 contraction (BF16 operands split into
+    1, 2 or 3 terms, FP32 accumulation) and, for comparison, in FP64 on the CUDA cores.
+    Per mode: the assembly time, the contraction kernel's time, tensor and HBM rates, and
+    the error against the FP64 mode (y = A x for a random x, and the solution of the
+    mixed-precision solve to 1e-8)."""
+    import torch
+    import gridap_gb300 as G
+    from gridap_gb300 import _lib as L
+    from gridap_gb300.synthetic import ELASTICITY3D_64, lognormal_at_points
+    w = dict(ELASTICITY3D_64)
+    if args.qp_cells != 64:
+        w["cells"] = (args.qp_cells,) * 3
+    name = f"elasticity3d_vq2_{w['cells'][0]}^3_parts2x2x2_E_at_gauss_points"
+    ranks = be.distribute(range(int(np.prod(w["parts"]))))
+    model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], w["cells"])
+    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, G.VectorValue, w["order"]), dirichlet_tags="left")
+    U = G.TrialFESpace(0.0, V)
+    assem = G.SparseMatrixAssembler(U, V, G.SubAssembledRows())
+    assem.symbolic()
+    ng, nnz_own, nnz_tot, kpn = C.c_int64(), C.c_int64(), C.c_int64(), C.c_int32()
+    L.call("gd_assembler_counts", assem.handle, C.byref(ng), C.byref(nnz_own), C.byref(nnz_tot), C.byref(kpn))
+    ncells = int(np.prod(w["cells"]))
+    xq = G.distributed.quadrature_points(model, w["degree"]).reshape(ncells, -1, 3)
+    E_qp = lognormal_at_points(w["cells"], xq, w["sigma"], w["corr_len"], w["seed"])
+    nqt = E_qp.shape[1]
+    E_d = torch.from_numpy(np.ascontiguousarray(E_qp)).to(dev)
+    del xq
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=dev)
+    xr = torch.from_numpy(np.random.default_rng(7).normal(size=ng.value)).to(dev)
+    hbm, hbm_kind = measured_peaks()
+    tpk, tpk_kind = measured_tensor_peak(sustained=True)
+    out = {"workload": name, "free_dofs": ng.value, "nnz": nnz_own.value, "quadrature_points_per_cell": nqt,
+           "field": "E = exp(g), g the seeded GRF (sigma 0.5, correlation 0.1) interpolated to the Gauss points",
+           "modes": {}}
+    y_ref = x_ref = x_bf = None
+    for mode in ("fp64", "bf16x6", "bf16x3", "bf16"):
+        c = L.gd_elasticity_qp()
+        c.E_qp = E_d.data_ptr()
+        c.nu = w["nu"]
+        for i in range(3):
+            c.force[i] = w["force"][i]
+        c.degree = w["degree"]
+        c.precision = L.QP_PRECISIONS[mode]
+        c.where = L.GD_DEVICE
+        for _ in range(max(args.warmup, 3)):
+            L.call("gd_assemble_elasticity_qp", assem.handle, C.byref(c))
+        torch.cuda.synchronize()
+        steps = max(3, min(args.steps, 10))
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        for e0, e1 in ev:
+            flush.zero_()
+            e0.record(stream)
+            L.call("gd_assemble_elasticity_qp", assem.handle, C.byref(c))
+            e1.record(stream)
+        torch.cuda.synchronize()
+        ms = float(np.mean([a.elapsed_time(b) for a, b in ev]))
+        # phase split from the assembler's own events, in separate untimed calls
+        L.call("gd_assembler_set_profiling", assem.handle, 1)
+        kms, rms = [], []
+        for _ in range(3):
+            flush.zero_()
+            L.call("gd_assemble_elasticity_qp", assem.handle, C.byref(c))
+            pts, ent, kp, et = (C.c_int32() for _ in range(4))
+            m_e, m_r = C.c_double(), C.c_double()
+            L.call("gd_qp_info", assem.handle, C.byref(pts), C.byref(ent), C.byref(kp), C.byref(et),
+                   C.byref(m_e), C.byref(m_r))
+            kms.append(m_e.value)
+            rms.append(m_r.value)
+        L.call("gd_assembler_set_profiling", assem.handle, 0)
+        ms_k, ms_r = float(np.mean(kms)), float(np.mean(rms))
+        nnep = (ent.value + 31) // 32 * 32
+        ke_bytes = 4 * ncells * nnep if mode != "fp64" else 8 * ncells * nnep
+        y = torch.empty_like(xr)
+        L.call("gd_spmv", assem.handle, C.c_void_p(xr.data_ptr()), C.c_void_p(y.data_ptr()), L.GD_DEVICE)
+        torch.cuda.synchronize()
+        rec = {"ms": ms, "nnz_per_s": nnz_own.value / (ms * 1e-3), "element_kernel_ms": ms_k, "row_kernels_ms": ms_r,
+               "element_matrices_bytes": ke_bytes}
+        alg = 8 * nnz_own.value + 8 * ng.value + 8 * ncells * nqt
+        rec["roofline_assembly"] = {"bound": "hbm", "algorithmic_bytes": alg, "achieved": alg / (ms * 1e-3) / 1e9,
+                                    "peak": hbm, "unit": "GB/s", "frac": alg / (ms * 1e-3) / 1e9 / hbm,
+                                    "peak_kind": hbm_kind}
+        if mode != "fp64":
+            nprod = {"bf16": 1, "bf16x3": 3, "bf16x6": 6}[mode]
+            nct = 128 if kp.value >= 64 else 256
+            n_ct = (ncells + nct - 1) // nct
+            flops = 2.0 * (128 * et.value) * (nct * n_ct) * kp.value * nprod   # issued by the MMAs
+            useful = 2.0 * ent.value * ncells * nqt                              # sum_q E_q H_q in exact arithmetic
+            rec["contraction"] = {
+                "kernel": "k_qp_gemm (tcgen05.mma kind::f16, BF16 x BF16 -> FP32 in TMEM)",
+                "products_per_term": nprod, "k_padded": kp.value, "issued_tflop": flops / 1e12,
+                "tensor": {"achieved": flops / (ms_k * 1e-3) / 1e12, "peak": tpk, "unit": "TFLOP/s",
+                           "frac": flops / (ms_k * 1e-3) / 1e12 / tpk, "peak_kind": tpk_kind + " sustained"},
+                "useful_tflop_per_s": useful / (ms_k * 1e-3) / 1e12,
+                "hbm": {"bytes": ke_bytes, "achieved": ke_bytes / (ms_k * 1e-3) / 1e9, "peak": hbm, "unit": "GB/s",
+                        "frac": ke_bytes / (ms_k * 1e-3) / 1e9 / hbm},
+                "bound": "hbm (FP32 element matrices written once)"}
+        if y_ref is None:
+            y_ref = y.clone()
+        else:
+            rec["error_vs_fp64"] = {"spmv_rel_inf": float((y - y_ref).abs().max() / y_ref.abs().max())}
+        if mode in ("fp64", "bf16x6") and args.elasticity_solve:
+            x = torch.empty_like(xr)
+            st = L.gd_solve_stats()
+            t0 = time.perf_counter()
+            rc = L.load().gd_solve(assem.handle, L.GD_SOLVE_MIXED_IR, 1e-8, args.solve_maxit,
+                                   C.c_void_p(x.data_ptr()), L.GD_DEVICE, C.byref(st))
+            rec["solve_mixed_ir"] = {"seconds": time.perf_counter() - t0, "iterations": st.iterations,
+                                     "rel_residual": st.rel_residual, "converged": bool(st.converged and rc == 0)}
+            if x_ref is None:
+                x_ref = x.clone()
+            else:
+                rec["error_vs_fp64"]["solution_rel_inf"] = float((x - x_ref).abs().max() / x_ref.abs().max())
+        if mode == "bf16x6" and x_ref is not None and "solve_mixed_ir" in rec:
+            x_bf = x.clone()
+        out["modes"][mode] = rec
+    out["speedup_bf16x6_vs_fp64"] = out["modes"]["fp64"]["ms"] / out["modes"]["bf16x6"]["ms"]
+    if x_ref is not None and "solve_mixed_ir" in out["modes"].get("bf16x6", {}):
+        # backward error against the FP64 operator: ||b - A_fp64 x|| / ||b|| for the FP64
+        # solution and for the solution of the bf16x6 system (the residual the FP64
+        # matrix assigns to it); the gap between the two solutions is conditioning
+        c = L.gd_elasticity_qp()
+        c.E_qp = E_d.data_ptr()
+        c.nu = w["nu"]
+        for i in range(3):
+            c.force[i] = w["force"][i]
+        c.degree = w["degree"]
+        c.precision = L.GD_QP_FP64
+        c.where = L.GD_DEVICE
+        L.call("gd_assemble_elasticity_qp", assem.handle, C.byref(c))
+        b = np.zeros(ng.value)
+        L.call("gd_system_download", assem.handle, L.ptr(b, C.c_double), None)
+        bnorm = np.linalg.norm(b)
+        for key, xs in (("fp64_solution", x_ref), ("bf16x6_solution", x_bf)):
+            y = torch.empty_like(xs)
+            L.call("gd_spmv", assem.handle, C.c_void_p(xs.data_ptr()), C.c_void_p(y.data_ptr()), L.GD_DEVICE)
+            torch.cuda.synchronize()
+            out.setdefault("backward_error_vs_fp64_operator", {})[key] = float(
+                np.linalg.norm(b - y.cpu().numpy()) / bnorm)
+    del assem, U, V, model, E_d
+    torch.cuda.empty_cache()
     return out
 
 
@@ -709,6 +871,9 @@ def run_gb300(args, rank, world, local):
     elasticity = None
     if not args.no_elasticity:
         elasticity = run_elasticity(args, be, stream, dev)
+    quadrature = None
+    if not args.no_qp:
+        quadrature = run_qp(args, be, stream, dev)
     batched = None
     if args.batched != "off":
         batched = run_batched(args, be, stream, dev, args.batched)
@@ -752,6 +917,7 @@ def run_gb300(args, rank, world, local):
             "learned": learned,
             "c1": c1,
             "elasticity": elasticity,
+            "quadrature": quadrature,
             "batched": batched,
             "cpu_baseline": cpu,
         }

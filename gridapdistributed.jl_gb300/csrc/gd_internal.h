@@ -205,6 +205,9 @@ int residual_fp64_asm(gd_asm* A, const double* x, const double* b, double* r, do
 }  // namespace gd
 
 namespace gd {
+// Workspace of the quadrature-point assembly (gd_qp.cu).
+struct QpState;
+void qp_release(QpState* q);
 // Workspace of the mixed-precision solver (gd_solve_mixed.cu).
 struct MixedState {
   bool ready = false;
@@ -351,4 +354,8 @@ struct gd_asm {
   gd::DBuf<double> dred;           // reduction partials
   gd::DBuf<double> dinv;
   gd::SellMat sell;                // sliced-ELL copy of the owned rows (FP64 solves)
+  // quadrature-point assembly (gd_qp.cu); qp_values: the current values came from it, so
+  // the cell-coefficient shortcuts of the solvers (matrix-free lattice operators) do not apply
+  gd::QpState* qp = nullptr;
+  bool qp_values = false;
 };

@@ -1131,8 +1131,9 @@ extern "C" int gd_learned_create(gd_asm* A, int levels, int flags, uint64_t seed
   if (levels < 1 || levels > kMaxLevels) return fail(GD_ERR_ARG, "gd_learned_create: levels must be 1..6");
   if (flags & ~GD_LEARNED_COARSE_START) return fail(GD_ERR_ARG, "gd_learned_create: unknown flags");
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_learned_create: assemble the system first");
-  if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3))
-    return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells");
+  if (!(A->fast_q1 && A->q1c_cube && A->test->geom.dim == 3) || A->qp_values)
+    return fail(GD_ERR_UNSUPPORTED,
+                "gd_learned_create: the learned preconditioner needs 3D Q1 on cube cells with cell-wise coefficients");
   const Geom& g = A->test->geom;
   if ((double)g.N[0] * g.N[1] * g.N[2] * kC >= 2147483647.0)
     return fail(GD_ERR_UNSUPPORTED, "gd_learned_create: node lattice too large (8 channels must index in 32 bits)");
@@ -1360,6 +1361,9 @@ extern "C" int gd_solve_learned(gd_asm* A, gd_learned* N, double rtol, int maxit
                                 gd_solve_stats* stats, int32_t* fallback_used) {
   if (!A || !N || N->A != A || !x) return fail(GD_ERR_ARG, "gd_solve_learned: bad argument");
   if (!A->numeric_done) return fail(GD_ERR_STATE, "gd_solve_learned: assemble the system first");
+  if (A->qp_values)
+    return fail(GD_ERR_UNSUPPORTED, "gd_solve_learned: the network reads cell-wise coefficients; the system was "
+                                    "assembled from quadrature-point values");
   cudaStream_t st = A->test->model->ctx->stream;
   GD_TRY(net_prepare(N, st));
   MixedPrecond pc{N, apply_as_precond, apply_as_precond_lattice, N->serial};

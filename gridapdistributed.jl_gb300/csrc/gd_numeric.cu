@@ -907,6 +907,7 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
                                               " cell visits");
   }
   A->numeric_done = true;
+  A->qp_values = false;
   ++A->numeric_epoch;
   return GD_OK;
 }

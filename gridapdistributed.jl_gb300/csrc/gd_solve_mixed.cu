@@ -328,7 +328,7 @@ int mixed_setup(gd_asm* A) {
   const int64_t n = A->ngdofs;
   MixedState& M = A->mx;
   if (M.numeric_epoch == A->numeric_epoch && M.ready) return GD_OK;
-  M.matrix_free = A->fast_q1 && A->q1c_cube && g.dim == 3;
+  M.matrix_free = A->fast_q1 && A->q1c_cube && g.dim == 3 && !A->qp_values;
   int64_t ncells = 1, nnodes = 1;
   for (int d = 0; d < g.dim; ++d) {
     ncells *= g.n[d];

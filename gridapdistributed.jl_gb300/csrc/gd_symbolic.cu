@@ -610,6 +610,8 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->dred);
   dfreeb(A->dinv);
   A->sell.release();
+  gd::qp_release(A->qp);
+  A->qp = nullptr;
   dfreeb(A->row_pat);
   dfreeb(A->pat);
   dfreeb(A->w_cells);

@@ -574,6 +574,7 @@ extern "C" int gd_assemble_elasticity(gd_asm* A, const gd_elasticity* c) {
   if (hbad) return fail(GD_ERR_NUMERIC, "gd_assemble_elasticity: E is not finite and positive in " +
                                             std::to_string(hbad) + " cell visits");
   A->numeric_done = true;
+  A->qp_values = false;
   ++A->numeric_epoch;
   return GD_OK;
 }

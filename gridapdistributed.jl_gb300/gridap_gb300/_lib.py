@@ -20,6 +20,11 @@ GD_SOLVE_JACOBI_PCG = 1
 GD_SOLVE_MIXED_IR = 2
 GD_HOST = 0
 GD_DEVICE = 1
+GD_QP_FP64 = 0
+GD_QP_BF16 = 1
+GD_QP_BF16X3 = 2
+GD_QP_BF16X6 = 3
+QP_PRECISIONS = {"fp64": GD_QP_FP64, "bf16": GD_QP_BF16, "bf16x3": GD_QP_BF16X3, "bf16x6": GD_QP_BF16X6}
 
 STATUS_NAMES = {
     0: "GD_OK", 1: "GD_ERR_ARG", 2: "GD_ERR_OOM", 3: "GD_ERR_CUDA", 4: "GD_ERR_TIMEOUT",
@@ -42,6 +47,16 @@ class gd_coeffs(C.Structure):
 class gd_elasticity(C.Structure):
     _fields_ = [("E", C.c_void_p), ("nu", C.c_double), ("force", C.c_double * 3), ("degree", C.c_int),
                 ("where", C.c_int)]
+
+
+class gd_qp_coeffs(C.Structure):
+    _fields_ = [("kappa_qp", C.c_void_p), ("f_nodal", C.c_void_p), ("f_const", C.c_double), ("degree", C.c_int),
+                ("precision", C.c_int), ("where", C.c_int)]
+
+
+class gd_elasticity_qp(C.Structure):
+    _fields_ = [("E_qp", C.c_void_p), ("nu", C.c_double), ("force", C.c_double * 3), ("degree", C.c_int),
+                ("precision", C.c_int), ("where", C.c_int)]
 
 
 class gd_dg_form(C.Structure):
@@ -102,6 +117,9 @@ SIGNATURES = {
     "gd_solve_rhs": [P, C.c_int, C.c_double, C.c_int, P, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_solve_noalloc": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_assemble_elasticity": [P, P],
+    "gd_assemble_qp": [P, P],
+    "gd_assemble_elasticity_qp": [P, P],
+    "gd_qp_info": [P, I32P, I32P, I32P, I32P, DP, DP],
     "gd_l2_error": [P, P, P, C.c_int, C.c_int, DP],
     "gd_add_boundary_source": [P, I32P, P, C.c_int, C.c_int],
     "gd_batch_create": [P, P, C.c_int, PP],

@@ -369,10 +369,15 @@ def _lattice_values(V, u):
 # --------------------------------------------------------------------------------------
 @dataclass
 class GradGradForm:
-    """a(u,v) = ∫( κ ∇(v)⋅∇(u) )dΩ with κ per global cell (None = 1)."""
+    """a(u,v) = ∫( κ ∇(v)⋅∇(u) )dΩ with κ per global cell (None = 1), or -- a CellField
+    that varies inside the cells -- κ at the Gauss points of every cell (``kappa_qp``,
+    shape (cells, nq^dim), points x fastest), its element matrices formed in ``precision``
+    ("fp64", "bf16", "bf16x3", "bf16x6")."""
 
     kappa: np.ndarray | None
     measure: Measure
+    kappa_qp: np.ndarray | None = None
+    precision: str = "fp64"
 
 
 @dataclass
@@ -383,6 +388,8 @@ class ElasticityForm:
     E: np.ndarray | None
     nu: float
     measure: Measure
+    E_qp: np.ndarray | None = None
+    precision: str = "fp64"
 
 
 @dataclass
@@ -446,11 +453,34 @@ def boundary_quadrature_points(trian: BoundaryTriangulation, degree: int):
     return out
 
 
-def integral_grad_grad(kappa=None, measure: Measure = None):
+def _point_values(coef, measure):
+    """A coefficient given as a function of the coordinates (evaluated at the Gauss points
+    on the host, like the Dirichlet values of TrialFESpace) or as per-point values."""
+    if callable(coef):
+        model = measure.trian.model
+        ncells = int(np.prod(model.cells))
+        xq = quadrature_points(model, measure.degree).reshape(ncells, -1, model.dim)
+        v = coef(*[xq[:, :, d] for d in range(model.dim)])
+        return np.ascontiguousarray(np.broadcast_to(np.asarray(v, dtype=np.float64), xq.shape[:2]))
+    return np.ascontiguousarray(coef, dtype=np.float64)
+
+
+def integral_grad_grad(kappa=None, measure: Measure = None, precision: str = "fp64"):
+    """∫( κ ∇(v)⋅∇(u) )dΩ: κ per cell (1-D array), at the Gauss points (2-D array
+    (cells, nq^dim)) or a function of the coordinates (sampled at the Gauss points)."""
+    if callable(kappa) or (kappa is not None and np.ndim(kappa) == 2):
+        if precision not in L.QP_PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(L.QP_PRECISIONS)}")
+        return GradGradForm(None, measure, _point_values(kappa, measure), precision)
     return GradGradForm(None if kappa is None else np.ascontiguousarray(kappa, dtype=np.float64), measure)
 
 
-def integral_elasticity(E=None, nu=0.3, measure: Measure = None):
+def integral_elasticity(E=None, nu=0.3, measure: Measure = None, precision: str = "fp64"):
+    """∫( ε(v) ⊙ (σ∘ε(u)) )dΩ with E per cell, at the Gauss points, or a function of x."""
+    if callable(E) or (E is not None and np.ndim(E) == 2):
+        if precision not in L.QP_PRECISIONS:
+            raise ValueError(f"precision must be one of {sorted(L.QP_PRECISIONS)}")
+        return ElasticityForm(None, float(nu), measure, _point_values(E, measure), precision)
     return ElasticityForm(None if E is None else np.ascontiguousarray(E, dtype=np.float64), float(nu), measure)
 
 
@@ -510,6 +540,36 @@ class DistributedSparseMatrixAssembler:
                L.GD_HOST)
 
     def _numeric(self, a, l):
+        if isinstance(a, ElasticityForm) and a.E_qp is not None:
+            c = L.gd_elasticity_qp()
+            c.E_qp = a.E_qp.ctypes.data
+            c.nu = a.nu
+            f = l.f if l is not None else (0.0,) * self.V.model.dim
+            f = tuple(float(x) for x in (f if not np.isscalar(f) else (0.0,) * self.V.model.dim))
+            for i in range(3):
+                c.force[i] = f[i] if i < len(f) else 0.0
+            c.degree = int(a.measure.degree if a.measure is not None else 2 * self.V.order)
+            c.precision = L.QP_PRECISIONS[a.precision]
+            c.where = L.GD_HOST
+            L.call("gd_assemble_elasticity_qp", self.handle, C.byref(c))
+            return
+        if isinstance(a, GradGradForm) and a.kappa_qp is not None:
+            c = L.gd_qp_coeffs()
+            c.kappa_qp = a.kappa_qp.ctypes.data
+            f = l.f if l is not None else 0.0
+            keep = None
+            if np.isscalar(f):
+                c.f_nodal = None
+                c.f_const = float(f)
+            else:
+                keep = np.ascontiguousarray(f, dtype=np.float64)
+                c.f_nodal = keep.ctypes.data
+                c.f_const = 0.0
+            c.degree = int(a.measure.degree if a.measure is not None else 2 * self.V.order)
+            c.precision = L.QP_PRECISIONS[a.precision]
+            c.where = L.GD_HOST
+            L.call("gd_assemble_qp", self.handle, C.byref(c))
+            return
         if isinstance(a, ElasticityForm):
             c = L.gd_elasticity()
             c.E = None if a.E is None else a.E.ctypes.data

@@ -40,6 +40,37 @@ def lognormal_kappa(cells, sigma=1.0, corr_len=0.1, seed=0):
     return np.exp(gaussian_random_field(cells, sigma, corr_len, seed))
 
 
+def gaussian_random_field_at_points(cells, points, sigma=1.0, corr_len=0.1, seed=0, domain_len=1.0):
+    """g of gaussian_random_field (same seed, same cell-centre values) at arbitrary points
+    of the unit box, by multilinear interpolation between the cell centres (constant
+    beyond the outermost centres).  ``points``: array (..., dim).  The correlation length
+    spans several cells, so the interpolation changes the field by O((h / l)^2)."""
+    cells = tuple(int(c) for c in cells)
+    dim = len(cells)
+    g = gaussian_random_field(cells, sigma, corr_len, seed, domain_len).reshape(tuple(reversed(cells)))
+    pts = np.asarray(points, dtype=np.float64)
+    i0, t = [], []
+    for d in range(dim):
+        s = pts[..., d] / (domain_len / cells[d]) - 0.5
+        lo = np.clip(np.floor(s).astype(np.int64), 0, max(cells[d] - 2, 0))
+        i0.append(lo)
+        t.append(np.clip(s - lo, 0.0, 1.0) if cells[d] > 1 else np.zeros_like(s))
+    out = np.zeros(pts.shape[:-1])
+    for corner in range(1 << dim):
+        w = np.ones(pts.shape[:-1])
+        idx = []
+        for d in range(dim):
+            b = (corner >> d) & 1
+            w = w * (t[d] if b else 1.0 - t[d])
+            idx.append(np.minimum(i0[d] + b, cells[d] - 1))
+        out += w * g[tuple(reversed(idx))]
+    return out
+
+
+def lognormal_at_points(cells, points, sigma=1.0, corr_len=0.1, seed=0):
+    return np.exp(gaussian_random_field_at_points(cells, points, sigma, corr_len, seed))
+
+
 # The 3D variable-coefficient Poisson workload: 128^3 Q1 hex cells on the unit
 # cube, parts (2,2,2), kappa = exp(g) (sigma 1, correlation length 0.1), f = 1,
 # homogeneous Dirichlet on the whole boundary, quadrature degree 2.

@@ -176,6 +176,50 @@ typedef struct gd_elasticity {
  * vector-space assembler (dof = dim * node dof + component). */
 int gd_assemble_elasticity(gd_asm* a, const gd_elasticity* c);
 
+/* ---- A7 with coefficients that vary inside a cell --------------------------------------
+ * integrate of an integrand built from a CellField known at the quadrature points
+ * (src/CellData.jl:234-259, `*(Integrand, Measure)` at :255-259; a CellField from a
+ * function of x or from per-point data): a(u,v) = int kappa(x) grad(v).grad(u) with
+ * kappa given at the tensor Gauss points of every cell ((degree+2)/2 per direction,
+ * at most 64 per cell): kappa_qp[cell * nq^dim + q], cells lexicographic, points x
+ * fastest.  l(v) = int v f as in gd_coeffs.  Each element matrix is
+ * K_e = sum_q kappa_q H_q; `precision` chooses how it is formed:
+ *   GD_QP_FP64:   FP64 on the CUDA cores (matches an FP64 quadrature to rounding);
+ *   GD_QP_BF16:   tensor cores (tcgen05, BF16 operands, FP32 accumulation), relative
+ *                 error of the element entries about 1e-2 .. 1e-3;
+ *   GD_QP_BF16X3: the same with each operand split into two BF16 terms (3 products),
+ *                 about 1e-5;
+ *   GD_QP_BF16X6: three BF16 terms (6 products), about FP32 rounding (1e-7 .. 1e-6).
+ * The element matrices are kept in FP32 (FP64 for GD_QP_FP64) and summed into the
+ * symbolic pattern deterministically; the matrix values are stored in FP64 as usual. */
+enum { GD_QP_FP64 = 0, GD_QP_BF16 = 1, GD_QP_BF16X3 = 2, GD_QP_BF16X6 = 3 };
+typedef struct gd_qp_coeffs {
+  const double* kappa_qp; /* per global cell, nq^dim values at the Gauss points          */
+  const double* f_nodal;  /* per global lattice node (load M*f); NULL = f_const         */
+  double f_const;
+  int degree;             /* quadrature degree                                           */
+  int precision;          /* GD_QP_*                                                     */
+  int where;              /* GD_HOST or GD_DEVICE for kappa_qp and f_nodal               */
+} gd_qp_coeffs;
+int gd_assemble_qp(gd_asm* a, const gd_qp_coeffs* c);
+/* Linear elasticity (vector space, orders 1-2) with Young's modulus at the Gauss points
+ * (E_qp in the layout of kappa_qp), constant nu and body force; homogeneous or the trial
+ * space's Dirichlet values. */
+typedef struct gd_elasticity_qp {
+  const double* E_qp;
+  double nu;
+  double force[3];
+  int degree;
+  int precision;          /* GD_QP_*                                                     */
+  int where;
+} gd_elasticity_qp;
+int gd_assemble_elasticity_qp(gd_asm* a, const gd_elasticity_qp* c);
+/* Sizes of the last quadrature-point assembly: points per cell, element-matrix entries,
+ * points padded to the tensor-core K step, 128-entry tiles; with gd_assembler_set_profiling
+ * on, the event-timed ms of the element-matrix kernel and of the row kernel. */
+int gd_qp_info(const gd_asm* a, int32_t* points, int32_t* entries, int32_t* kpad, int32_t* etiles,
+               double* ms_element, double* ms_rows);
+
 /* l(v) += int(v g) dGamma over the boundary sides flagged in `sides` (2*dim flags in the
  * order of dirichlet_sides; the Neumann term of test/PoissonTests.jl:20-41), added to
  * the owned rows of the assembled rhs -- call after gd_assemble_numeric.  g_qp holds g at

@@ -494,6 +494,75 @@ def quad_points_per_dir(degree):
     return (degree + 2) // 2
 
 
+def reference_point_tables(dim, k, h, degree):
+    """Weights ``W[q] = w_q |J|``, values ``phi[q, i]`` and gradients ``grad[q, i, d]`` of
+    the cell's shape functions at the tensor Gauss points (points x fastest), in Gridap's
+    cell-local node order -- what Gridap's integrate evaluates per point
+    (CellData integrate, src/CellData.jl:234-259)."""
+    nq = quad_points_per_dir(degree)
+    xq, wq = gauss_legendre(nq)
+    V, D = lagrange_1d(k, xq)
+    lnodes = cell_local_nodes(dim, k)
+    nn = len(lnodes)
+    detJ = float(np.prod(h))
+    qidx = list(itertools.product(*[range(nq)] * dim))
+    nqt = len(qidx)
+    phi = np.zeros((nqt, nn))
+    grad = np.zeros((nqt, nn, dim))
+    W = np.zeros(nqt)
+    for iq, qi in enumerate(qidx):
+        qi = tuple(reversed(qi))
+        W[iq] = np.prod([wq[qi[d]] for d in range(dim)]) * detJ
+        for a, off in enumerate(lnodes):
+            vals = [V[qi[d], off[d]] for d in range(dim)]
+            phi[iq, a] = np.prod(vals)
+            for d in range(dim):
+                g = D[qi[d], off[d]] / h[d]
+                for e in range(dim):
+                    if e != d:
+                        g *= vals[e]
+                grad[iq, a, d] = g
+    return W, phi, grad
+
+
+def quadrature_points(pb, cells=None):
+    """Physical coordinates of the tensor Gauss points of the given global cells (all by
+    default): array (cells, nq^dim, dim), points x fastest."""
+    nq = quad_points_per_dir(pb.degree)
+    xq, _ = gauss_legendre(nq)
+    dim = pb.dim
+    cells = np.arange(int(np.prod(pb.n))) if cells is None else np.asarray(cells)
+    cc = np.stack(np.unravel_index(cells, tuple(reversed(pb.n)))[::-1], axis=1)   # (cells, dim), x first
+    qi = np.indices((nq,) * dim).reshape(dim, -1)[::-1].T                          # (nqt, dim), x fastest
+    out = np.empty((len(cells), len(qi), dim))
+    for d in range(dim):
+        out[:, :, d] = pb.domain[2 * d] + (cc[:, d][:, None] + xq[qi[:, d]][None, :]) * pb.h[d]
+    return out
+
+
+def stiffness_from_points(W, grad, c):
+    """``K[i,j] = sum_q c_q W_q grad(phi_i).grad(phi_j)`` for coefficient values c at the points."""
+    return np.einsum("q,qid,qjd->ij", W * c, grad, grad)
+
+
+def elasticity_from_points(W, grad, c, nu):
+    """Element matrix of ``int E C1 eps(u):eps(v)`` with E at the points (``c``), in the
+    component-major vector DOF order of reference_elasticity."""
+    nn, dim = grad.shape[1], grad.shape[2]
+    lam = nu / ((1 + nu) * (1 - 2 * nu))
+    mu = 1.0 / (2 * (1 + nu))
+    G = np.einsum("q,qic,qjd->icjd", W * c, grad, grad)
+    K = np.zeros((dim * nn, dim * nn))
+    lap = np.einsum("icjc->ij", G)
+    for a in range(dim):
+        for b in range(dim):
+            blk = lam * G[:, a, :, b] + mu * G[:, b, :, a]
+            if a == b:
+                blk = blk + mu * lap
+            K[a * nn:(a + 1) * nn, b * nn:(b + 1) * nn] = blk
+    return K
+
+
 def reference_matrices(dim, k, h, degree):
     """Element stiffness ``Kh[i,j] = sum_q w_q |J| grad(phi_i).grad(phi_j)``, mass
     ``Mh`` and load ``Fh[i] = sum_q w_q |J| phi_i`` for an axis-aligned cell of
@@ -586,6 +655,8 @@ class Problem:
     degree: int = 2
     dirichlet_sides: tuple = None   # 2*dim flags; default: whole boundary
     kappa: np.ndarray = None        # per global cell (lexicographic); default 1
+    kappa_qp: np.ndarray = None     # or per global cell and Gauss point (cells, nq^dim), points x
+                                    # fastest: a coefficient that varies inside the cells (E for elasticity)
     f_const: float = 0.0            # constant source
     f_nodal: np.ndarray = None      # or nodal source values on the global lattice (b = M f)
     u_dir: np.ndarray = None        # Dirichlet values on the global lattice (dense), default 0;
@@ -667,11 +738,16 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
         # element DOFs component-major (c * nnode + a), as Kel; u_dir: (lattice nodes, dim)
         assert pb.f_nodal is None, "elasticity: constant body force"
         Kel = reference_elasticity(dim, pb.order, pb.h, pb.degree, pb.nu)
+        if pb.kappa_qp is not None:
+            Wq, _, Gq = reference_point_tables(dim, pb.order, pb.h, pb.degree)
         force = pb.force if pb.force is not None else (0.0,) * dim
         be = np.concatenate([force[c] * Fh for c in range(dim)])
         ud_all = None if pb.u_dir is None else np.asarray(pb.u_dir, dtype=np.float64).reshape(-1, dim)
         for ic, g in enumerate(sp.cells):
-            Ke = pb.kappa[g] * Kel
+            if pb.kappa_qp is not None:
+                Ke = elasticity_from_points(Wq, Gq, pb.kappa_qp[g], pb.nu)
+            else:
+                Ke = pb.kappa[g] * Kel
             bv = be.copy()
             if ud_all is not None:
                 ci = np.array(P_cell_coords(pb.n, int(g)))
@@ -682,9 +758,15 @@ def cell_contributions(pb: Problem, sp: LocalSpace, Kh, Mh, Fh):
             vecs.append(bv)
         return mats, vecs
     nbt = neumann_tables(pb) if pb.neumann else None
+    if pb.kappa_qp is not None:
+        assert pb.stiff == 1.0 and pb.mass == 0.0, "point coefficients: stiffness form"
+        Wq, _, Gq = reference_point_tables(dim, pb.order, pb.h, pb.degree)
     for ic, g in enumerate(sp.cells):
-        kap = pb.kappa[g]
-        Ke = kap * Kh if (pb.stiff == 1.0 and pb.mass == 0.0) else kap * (pb.stiff * Kh + pb.mass * Mh)
+        if pb.kappa_qp is not None:
+            Ke = stiffness_from_points(Wq, Gq, pb.kappa_qp[g])
+        else:
+            kap = pb.kappa[g]
+            Ke = kap * Kh if (pb.stiff == 1.0 and pb.mass == 0.0) else kap * (pb.stiff * Kh + pb.mass * Mh)
         ci = np.array(P_cell_coords(pb.n, int(g)))
         X = pb.order * ci[None, :] + lnodes
         if pb.f_nodal is not None:
