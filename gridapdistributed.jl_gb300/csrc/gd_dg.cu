@@ -18,10 +18,22 @@
 // evaluated at the same face points), plus the face value / normal-derivative rows for
 // the right-hand side.  The tables are built once in FP64 on the host; a row of the
 // matrix (owned dof a of cell X) is table entries for X's own dofs (volume + its faces)
-// and for each face neighbour's dofs.  Assembly follows FullyAssembledRows: every owned
-// row is summed completely by its part (the global operator the reference assembles);
-// local columns are the owned dofs, then the touched ghost dofs (neighbour cells in the
-// ghost layer) in local-id order.
+// and for each face neighbour's dofs.  Every owned row is summed completely (the global
+// operator the reference assembles, whichever the strategy).  The local parts follow the
+// strategy:
+//  * FullyAssembledRows: owned rows only; columns: the owned dofs, then the touched ghost
+//    dofs (the face-neighbour cells in the ghost layer) in local-id order;
+//  * SubAssembledRows (the reference's default): a part integrates the interior faces
+//    whose cell with the larger global id it owns (src/Geometry.jl:864-882) -- with
+//    lexicographic cell ids those are the faces to the ghost cells just below its owned
+//    box -- so the dofs of those ghost cells are touched ghost rows (local-id order, their
+//    entries explicit zeros: the triplets went to their owners, Algebra.jl:1048-1131);
+//    ghost columns come in order of first appearance in the local COO and then the
+//    received triplets (Algebra.jl:1210-1238): the cells below the owned box by local id
+//    (each meets its one owned neighbour at a face that Gridap's face numbering reaches
+//    at the lower cell, plus side = lower local id, block columns walked plus first),
+//    then the cells just above it, owner by owner (receives in ascending sender order),
+//    lexicographic within an owner.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -40,6 +52,7 @@ struct DgPart {
   int64_t ncell_own;
   int64_t nloc_cells;
   int64_t gc_off, n_gc;   // touched ghost cells (local-box lexicographic ids, sorted)
+  int64_t gr_off, n_gr;   // ghost-row cells (SubAssembledRows: the cells just below the owned box)
 };
 
 struct DgGeo {
@@ -102,8 +115,8 @@ struct RowCell {
 };
 
 // the row cell and its face neighbours, in local column order
-__device__ inline int dg_row_cells(const DgGeo& G, const DgPart* parts, const int64_t* __restrict__ gcells, int p,
-                                   const int64_t* X, RowCell* rc) {
+__device__ inline int dg_row_cells(const DgGeo& G, const DgPart* parts, const int64_t* __restrict__ gcells,
+                                   const int32_t* __restrict__ gperm, int p, const int64_t* X, RowCell* rc) {
   const DgPart& P = parts[p];
   int m = 0;
   for (int f = -1; f < 2 * G.dim; ++f) {
@@ -126,7 +139,7 @@ __device__ inline int dg_row_cells(const DgGeo& G, const DgPart* parts, const in
         if (gcells[P.gc_off + mid] < key) lo = mid + 1;
         else hi = mid;
       }
-      c.colbase = (int64_t)G.nn * (P.ncell_own + lo);
+      c.colbase = (int64_t)G.nn * (P.ncell_own + gperm[P.gc_off + lo]);
     }
     int j = m++;
     while (j > 0 && rc[j - 1].colbase > c.colbase) {
@@ -159,9 +172,10 @@ struct DgTabs {
 
 // warp per owned row; lanes over the row's entries
 __global__ void __launch_bounds__(256)
-k_dg_fill(DgGeo G, DgTabs T, const DgPart* __restrict__ parts, const int64_t* __restrict__ gcells, int64_t nrows,
-          int dmask, const double* __restrict__ tab, const int64_t* __restrict__ rowptr, int32_t* __restrict__ colidx,
-          int32_t* __restrict__ colgid, double* __restrict__ vals) {
+k_dg_fill(DgGeo G, DgTabs T, const DgPart* __restrict__ parts, const int64_t* __restrict__ gcells,
+          const int32_t* __restrict__ gperm, int64_t nrows, int dmask, const double* __restrict__ tab,
+          const int64_t* __restrict__ rowptr, int32_t* __restrict__ colidx, int32_t* __restrict__ colgid,
+          double* __restrict__ vals) {
   const int lane = threadIdx.x & 31;
   const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
@@ -171,7 +185,7 @@ k_dg_fill(DgGeo G, DgTabs T, const DgPart* __restrict__ parts, const int64_t* __
     int64_t X[kMaxDim];
     dg_row(G, parts, r, p, X, a);
     RowCell rc[2 * kMaxDim + 1];
-    const int m = dg_row_cells(G, parts, gcells, p, X, rc);
+    const int m = dg_row_cells(G, parts, gcells, gperm, p, X, rc);
     // which faces of X are interior / Dirichlet boundary
     int interior = 0, dir = 0;
     for (int f = 0; f < 2 * G.dim; ++f) {
@@ -198,6 +212,54 @@ k_dg_fill(DgGeo G, DgTabs T, const DgPart* __restrict__ parts, const int64_t* __
       colidx[e0 + e] = (int32_t)(c.colbase + b);
       colgid[e0 + e] = (int32_t)(c.gid0 + b);
       vals[e0 + e] = v;
+    }
+  }
+}
+
+// SubAssembledRows ghost rows (rows nown_total + i): the dofs of a ghost cell X' just below
+// the owned box, whose one owned neighbour is X' + e_d.  Columns sorted by local id: the
+// neighbour's dofs (owned), then X''s dofs (a ghost column); values explicit zeros.
+// Mode 0: row lengths; mode 1: columns and values.
+__global__ void k_dg_ghost_rows(DgGeo G, const DgPart* __restrict__ parts, const int64_t* __restrict__ grcells,
+                                const int64_t* __restrict__ gcells, const int32_t* __restrict__ gperm, int64_t n_own,
+                                int64_t nghost, int mode, int32_t* __restrict__ len,
+                                const int64_t* __restrict__ rowptr, int32_t* __restrict__ colidx,
+                                int32_t* __restrict__ colgid, double* __restrict__ vals) {
+  const int nn = G.nn;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nghost; i += (int64_t)gridDim.x * blockDim.x) {
+    if (mode == 0) {
+      len[n_own + i] = 2 * nn;
+      continue;
+    }
+    const int64_t gc = i / nn;   // ghost-row cell (all parts concatenated)
+    int p = 0;
+    while (p + 1 < G.np && parts[p + 1].gr_off <= gc) ++p;
+    const DgPart& P = parts[p];
+    const int64_t key = grcells[gc];
+    int64_t X[kMaxDim] = {0, 0, 0}, Y[kMaxDim] = {0, 0, 0}, rest = key;
+    for (int d = 0; d < G.dim; ++d) {
+      const int64_t w = P.loc_hi[d] - P.loc_lo[d];
+      X[d] = P.loc_lo[d] + rest % w;
+      rest /= w;
+    }
+    for (int d = 0; d < G.dim; ++d) Y[d] = X[d] + (X[d] == P.own_lo[d] - 1 ? 1 : 0);
+    int64_t lo = 0, hi = P.n_gc - 1;   // X' among the part's ghost columns
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (gcells[P.gc_off + mid] < key) lo = mid + 1;
+      else hi = mid;
+    }
+    const int64_t cown = (int64_t)nn * box_lex(P.own_lo, P.own_hi, Y, G.dim);
+    const int64_t cgh = (int64_t)nn * (P.ncell_own + gperm[P.gc_off + lo]);
+    const int64_t gY = dg_cell_gid0(G, parts, Y), gX = dg_cell_gid0(G, parts, X);
+    const int64_t e0 = rowptr[n_own + i];
+    for (int b = 0; b < nn; ++b) {
+      colidx[e0 + b] = (int32_t)(cown + b);
+      colgid[e0 + b] = (int32_t)(gY + b);
+      vals[e0 + b] = 0.0;
+      colidx[e0 + nn + b] = (int32_t)(cgh + b);
+      colgid[e0 + nn + b] = (int32_t)(gX + b);
+      vals[e0 + nn + b] = 0.0;
     }
   }
 }
@@ -308,6 +370,12 @@ struct gd_dgspace {
   gd::DBuf<gd::DgPart> d_parts;
   std::vector<int64_t> h_gcells;
   gd::DBuf<int64_t> gcells;
+  int strategy = GD_SUB_ASSEMBLED_ROWS;
+  std::vector<int32_t> h_gperm;    // per ghost column (sorted by local id): its position in the column order
+  gd::DBuf<int32_t> gperm;
+  std::vector<int64_t> h_grcells;  // ghost-row cells per part (local-box ids, sorted)
+  gd::DBuf<int64_t> grcells;
+  int64_t nghost_rows = 0;         // ghost rows of all parts (dofs)
   std::vector<int> dofpos;   // 3 per local dof
   int64_t ndofs = 0, nnz = 0;
   bool assembled = false;
@@ -318,6 +386,8 @@ struct gd_dgspace {
   ~gd_dgspace() {
     gd::dfreeb(d_parts);
     gd::dfreeb(gcells);
+    gd::dfreeb(gperm);
+    gd::dfreeb(grcells);
     gd::dfreeb(rowptr);
     gd::dfreeb(colidx);
     gd::dfreeb(colgid);
@@ -451,6 +521,71 @@ extern "C" int gd_dg_get_gids(const gd_dgspace* S, int part, int64_t* gid, int32
       if (owner) owner[l * S->nn + a] = q;
     }
   }
+  return GD_OK;
+}
+
+// Ghost-column order and ghost-row cells of every part for the space's strategy (see the
+// file comment), uploaded with the part table.
+static int dg_layout(gd_dgspace* S) {
+  const Geom& g = S->model->geom;
+  S->h_gperm.assign(std::max<size_t>(S->h_gcells.size(), 1), 0);
+  S->h_grcells.clear();
+  for (DgPart& P : S->parts) {
+    struct Item {
+      int cls, owner;
+      int64_t key;
+      int64_t idx;
+    };
+    std::vector<Item> items;
+    P.gr_off = (int64_t)S->h_grcells.size();
+    for (int64_t i = 0; i < P.n_gc; ++i) {
+      const int64_t key = S->h_gcells[P.gc_off + i];
+      int64_t X[kMaxDim] = {0, 0, 0}, rest = key;
+      for (int d = 0; d < S->dim; ++d) {
+        const int64_t w = P.loc_hi[d] - P.loc_lo[d];
+        X[d] = P.loc_lo[d] + rest % w;
+        rest /= w;
+      }
+      bool lower = false;
+      for (int d = 0; d < S->dim; ++d) lower = lower || X[d] == P.own_lo[d] - 1;
+      if (S->strategy == GD_FULLY_ASSEMBLED_ROWS) {
+        items.push_back({0, 0, key, i});
+      } else if (lower) {
+        items.push_back({0, 0, key, i});
+        S->h_grcells.push_back(key);
+      } else {
+        items.push_back({1, cell_owner(g, X), cell_lin(g, X), i});
+      }
+    }
+    std::stable_sort(items.begin(), items.end(), [](const Item& a, const Item& b) {
+      if (a.cls != b.cls) return a.cls < b.cls;
+      if (a.owner != b.owner) return a.owner < b.owner;
+      return a.key < b.key;
+    });
+    for (size_t pos = 0; pos < items.size(); ++pos) S->h_gperm[P.gc_off + items[pos].idx] = (int32_t)pos;
+    P.n_gr = (int64_t)S->h_grcells.size() - P.gr_off;
+  }
+  S->nghost_rows = (int64_t)S->nn * (int64_t)S->h_grcells.size();
+  cudaStream_t st = S->model->ctx->stream;
+  GD_TRY(dalloc(S->gperm, S->h_gperm.size()));
+  GD_TRY(dalloc(S->grcells, std::max<size_t>(S->h_grcells.size(), 1)));
+  GD_CUDA_TRY(cudaMemcpyAsync(S->d_parts.p, S->parts.data(), sizeof(DgPart) * S->parts.size(), cudaMemcpyHostToDevice, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(S->gperm.p, S->h_gperm.data(), sizeof(int32_t) * S->h_gperm.size(),
+                              cudaMemcpyHostToDevice, st));
+  if (!S->h_grcells.empty())
+    GD_CUDA_TRY(cudaMemcpyAsync(S->grcells.p, S->h_grcells.data(), sizeof(int64_t) * S->h_grcells.size(),
+                                cudaMemcpyHostToDevice, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return GD_OK;
+}
+
+extern "C" int gd_dg_set_strategy(gd_dgspace* S, int strategy) {
+  if (!S) return fail(GD_ERR_ARG, "gd_dg_set_strategy: null space");
+  if (strategy != GD_SUB_ASSEMBLED_ROWS && strategy != GD_FULLY_ASSEMBLED_ROWS)
+    return fail(GD_ERR_ARG, "gd_dg_set_strategy: unknown strategy");
+  if (S->rowptr.p && strategy != S->strategy)
+    return fail(GD_ERR_STATE, "gd_dg_set_strategy: the pattern of the other strategy is built already");
+  S->strategy = strategy;
   return GD_OK;
 }
 
@@ -637,25 +772,41 @@ extern "C" int gd_dg_assemble(gd_dgspace* S, const gd_dg_form* F) {
     }
   }
   if (e != cudaSuccess) return done(fail(GD_ERR_CUDA, "gd_dg_assemble: copy"));
-  // pattern (once): row lengths, offsets
+  // pattern (once): ghost layout of the strategy, row lengths of the owned rows and then of
+  // the ghost rows (SubAssembledRows), offsets; the ghost rows' columns and their explicit
+  // zeros are written here once
   if (!S->rowptr.p) {
-    if ((s = dalloc(len, std::max<int64_t>(n, 1))) != GD_OK) return done(s);
-    if ((s = dalloc(S->rowptr, n + 1)) != GD_OK) return done(s);
+    if ((s = dg_layout(S)) != GD_OK) return done(s);
+    const int64_t nt = n + S->nghost_rows;
+    if ((s = dalloc(len, std::max<int64_t>(nt, 1))) != GD_OK) return done(s);
+    if ((s = dalloc(S->rowptr, nt + 1)) != GD_OK) return done(s);
     if (n) k_dg_rowlen<<<dg_grid(n, 256), 256, 0, st>>>(G, S->d_parts.p, n, len.p);
+    if (S->nghost_rows)
+      k_dg_ghost_rows<<<dg_grid(S->nghost_rows, 256), 256, 0, st>>>(G, S->d_parts.p, S->grcells.p, S->gcells.p,
+                                                                     S->gperm.p, n, S->nghost_rows, 0, len.p,
+                                                                     nullptr, nullptr, nullptr, nullptr);
     if (cudaGetLastError() != cudaSuccess) return done(fail(GD_ERR_CUDA, "gd_dg_assemble: row lengths"));
-    if ((s = exclusive_scan_i32(len.p, S->rowptr.p, n, st)) != GD_OK) return done(s);
+    if ((s = exclusive_scan_i32(len.p, S->rowptr.p, nt, st)) != GD_OK) return done(s);
+    int64_t nz_all = 0;
     if (cudaMemcpyAsync(&S->nnz, S->rowptr.p + n, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+        cudaMemcpyAsync(&nz_all, S->rowptr.p + nt, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
         cudaStreamSynchronize(st) != cudaSuccess)
       return done(fail(GD_ERR_CUDA, "gd_dg_assemble: entry count"));
-    if (S->nnz >= ((int64_t)1 << 31) || n >= ((int64_t)1 << 31))
+    if (nz_all >= ((int64_t)1 << 31) || nt >= ((int64_t)1 << 31))
       return done(fail(GD_ERR_UNSUPPORTED, "gd_dg_assemble: more than 2^31 entries"));
-    const size_t nz = (size_t)std::max<int64_t>(S->nnz, 1);
+    const size_t nz = (size_t)std::max<int64_t>(nz_all, 1);
     if ((s = dalloc(S->colidx, nz)) != GD_OK || (s = dalloc(S->colgid, nz)) != GD_OK ||
         (s = dalloc(S->vals, nz)) != GD_OK || (s = dalloc(S->rhs, std::max<int64_t>(n, 1))) != GD_OK)
       return done(s);
+    if (S->nghost_rows) {
+      k_dg_ghost_rows<<<dg_grid(S->nghost_rows, 256), 256, 0, st>>>(G, S->d_parts.p, S->grcells.p, S->gcells.p,
+                                                                     S->gperm.p, n, S->nghost_rows, 1, nullptr,
+                                                                     S->rowptr.p, S->colidx.p, S->colgid.p, S->vals.p);
+      if (cudaGetLastError() != cudaSuccess) return done(fail(GD_ERR_CUDA, "gd_dg_assemble: ghost rows"));
+    }
   }
   if (n) {
-    k_dg_fill<<<dg_grid(n * 32, 256), 256, 0, st>>>(G, T, S->d_parts.p, S->gcells.p, n, dmask, S->tabs.p,
+    k_dg_fill<<<dg_grid(n * 32, 256), 256, 0, st>>>(G, T, S->d_parts.p, S->gcells.p, S->gperm.p, n, dmask, S->tabs.p,
                                                      S->rowptr.p, S->colidx.p, S->colgid.p, S->vals.p);
     k_dg_rhs<<<dg_grid(n, 128), 128, 0, st>>>(G, T, S->d_parts.p, n, S->tabs.p, F->f_const, fq, dvt.p, nqt, dmask,
                                               ddoff.p, ud, nmask, dnoff.p, gq, S->rhs.p);
@@ -668,55 +819,90 @@ extern "C" int gd_dg_assemble(gd_dgspace* S, const gd_dg_form* F) {
 }
 
 extern "C" int gd_dg_matrix_sizes(const gd_dgspace* S, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
-                                  int64_t* n_ghost_cols) {
+                                  int64_t* n_ghost_rows, int64_t* n_ghost_cols) {
   if (!S || !S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_sizes: assemble first");
   if (part < 0 || part >= (int)S->parts.size()) return fail(GD_ERR_ARG, "gd_dg_matrix_sizes: bad part");
   const DgPart& P = S->parts[part];
   cudaStream_t st = S->model->ctx->stream;
   const int64_t r0 = P.first, r1 = P.first + (int64_t)S->nn * P.ncell_own;
-  int64_t b[2];
+  const int64_t g0 = S->ndofs + (int64_t)S->nn * P.gr_off, g1 = g0 + (int64_t)S->nn * P.n_gr;
+  int64_t b[4];
   GD_CUDA_TRY(cudaMemcpyAsync(&b[0], S->rowptr.p + r0, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaMemcpyAsync(&b[1], S->rowptr.p + r1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&b[2], S->rowptr.p + g0, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&b[3], S->rowptr.p + g1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
-  if (nrows) *nrows = r1 - r0;
+  if (nrows) *nrows = (r1 - r0) + (g1 - g0);
   if (ncols) *ncols = (int64_t)S->nn * (P.ncell_own + P.n_gc);
-  if (nnz) *nnz = b[1] - b[0];
+  if (nnz) *nnz = (b[1] - b[0]) + (b[3] - b[2]);
+  if (n_ghost_rows) *n_ghost_rows = g1 - g0;
   if (n_ghost_cols) *n_ghost_cols = (int64_t)S->nn * P.n_gc;
   return GD_OK;
 }
 
-// The part's owned rows: local CSR, ghost column gids / owners, right-hand side.
+// gid and owner of dof a of the cell with local-box id `key` of part P
+static void dg_local_cell_gid(const gd_dgspace* S, const DgPart& P, int64_t key, int64_t* gid0, int32_t* owner) {
+  const Geom& g = S->model->geom;
+  int64_t X[kMaxDim] = {0, 0, 0}, rest = key;
+  for (int d = 0; d < S->dim; ++d) {
+    const int64_t w = P.loc_hi[d] - P.loc_lo[d];
+    X[d] = P.loc_lo[d] + rest % w;
+    rest /= w;
+  }
+  const int q = cell_owner(g, X);
+  const DgPart& Q = S->parts[q];
+  *gid0 = Q.first + (int64_t)S->nn * box_lex(Q.own_lo, Q.own_hi, X, S->dim);
+  *owner = q;
+}
+
+// One part: local CSR over the owned rows and then the ghost rows, the ghost rows' and
+// ghost columns' gids / owners (in the strategy's order), the right-hand side (ghost rows 0).
 extern "C" int gd_dg_matrix_export(const gd_dgspace* S, int part, int64_t* rowptr, int32_t* colidx, double* vals,
-                                   int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs) {
+                                   int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
+                                   int32_t* ghost_col_owners, double* rhs) {
   if (!S || !S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_export: assemble first");
   if (part < 0 || part >= (int)S->parts.size()) return fail(GD_ERR_ARG, "gd_dg_matrix_export: bad part");
   const DgPart& P = S->parts[part];
   cudaStream_t st = S->model->ctx->stream;
-  const int64_t r0 = P.first, nr = (int64_t)S->nn * P.ncell_own;
-  std::vector<int64_t> rp(nr + 1);
+  const int nn = S->nn;
+  const int64_t r0 = P.first, nr = (int64_t)nn * P.ncell_own;
+  const int64_t g0 = S->ndofs + (int64_t)nn * P.gr_off, ng = (int64_t)nn * P.n_gr;
+  std::vector<int64_t> rp(nr + 1), gp(ng + 1);
   GD_CUDA_TRY(cudaMemcpyAsync(rp.data(), S->rowptr.p + r0, sizeof(int64_t) * (nr + 1), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(gp.data(), S->rowptr.p + g0, sizeof(int64_t) * (ng + 1), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
-  const int64_t nz = rp[nr] - rp[0];
-  if (rowptr)
+  const int64_t nz = rp[nr] - rp[0], nzg = gp[ng] - gp[0];
+  if (rowptr) {
     for (int64_t i = 0; i <= nr; ++i) rowptr[i] = rp[i] - rp[0];
+    for (int64_t i = 1; i <= ng; ++i) rowptr[nr + i] = nz + gp[i] - gp[0];
+  }
   if (colidx && nz) GD_CUDA_TRY(cudaMemcpyAsync(colidx, S->colidx.p + rp[0], sizeof(int32_t) * nz, cudaMemcpyDeviceToHost, st));
+  if (colidx && nzg)
+    GD_CUDA_TRY(cudaMemcpyAsync(colidx + nz, S->colidx.p + gp[0], sizeof(int32_t) * nzg, cudaMemcpyDeviceToHost, st));
   if (vals && nz) GD_CUDA_TRY(cudaMemcpyAsync(vals, S->vals.p + rp[0], sizeof(double) * nz, cudaMemcpyDeviceToHost, st));
+  if (vals && nzg)
+    GD_CUDA_TRY(cudaMemcpyAsync(vals + nz, S->vals.p + gp[0], sizeof(double) * nzg, cudaMemcpyDeviceToHost, st));
   if (rhs && nr) GD_CUDA_TRY(cudaMemcpyAsync(rhs, S->rhs.p + r0, sizeof(double) * nr, cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
-  const Geom& g = S->model->geom;
-  for (int64_t i = 0; i < P.n_gc; ++i) {
-    int64_t X[kMaxDim] = {0, 0, 0}, rest = S->h_gcells[P.gc_off + i];
-    for (int d = 0; d < S->dim; ++d) {
-      const int64_t w = P.loc_hi[d] - P.loc_lo[d];
-      X[d] = P.loc_lo[d] + rest % w;
-      rest /= w;
+  if (rhs)
+    for (int64_t i = 0; i < ng; ++i) rhs[nr + i] = 0.0;
+  for (int64_t i = 0; i < P.n_gr; ++i) {
+    int64_t gid0;
+    int32_t q;
+    dg_local_cell_gid(S, P, S->h_grcells[P.gr_off + i], &gid0, &q);
+    for (int a = 0; a < nn; ++a) {
+      if (ghost_row_gids) ghost_row_gids[i * nn + a] = gid0 + a;
+      if (ghost_row_owners) ghost_row_owners[i * nn + a] = q;
     }
-    const int q = cell_owner(g, X);
-    const DgPart& Q = S->parts[q];
-    const int64_t g0 = Q.first + (int64_t)S->nn * box_lex(Q.own_lo, Q.own_hi, X, S->dim);
-    for (int a = 0; a < S->nn; ++a) {
-      if (ghost_col_gids) ghost_col_gids[i * S->nn + a] = g0 + a;
-      if (ghost_col_owners) ghost_col_owners[i * S->nn + a] = q;
+  }
+  for (int64_t i = 0; i < P.n_gc; ++i) {
+    int64_t gid0;
+    int32_t q;
+    dg_local_cell_gid(S, P, S->h_gcells[P.gc_off + i], &gid0, &q);
+    const int64_t pos = S->h_gperm[P.gc_off + i];
+    for (int a = 0; a < nn; ++a) {
+      if (ghost_col_gids) ghost_col_gids[pos * nn + a] = gid0 + a;
+      if (ghost_col_owners) ghost_col_owners[pos * nn + a] = q;
     }
   }
   return GD_OK;

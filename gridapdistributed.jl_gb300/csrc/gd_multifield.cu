@@ -15,10 +15,21 @@
 // by field in the fields' own order, numbered part by part; because every field shares
 // one part-contiguous scalar numbering, the gid of a field-jj dof with scalar gid g owned
 // by part q is |G| first(q) + jj n_own(q) + (g - first(q)).  A part's local columns are
-// the group's owned columns (field-major) followed by the touched ghost columns of each
-// touched field in field order (each sorted by local id, as the scalar
-// FullyAssembledRows columns are: src/Algebra.jl:1245-1257), so a merged row is the
-// owned-column prefixes of its touched blocks' scalar rows, then their ghost suffixes.
+// the group's owned columns (field-major) followed by the ghost columns; a merged row is
+// the owned-column prefixes of its touched blocks' scalar rows, then their ghost parts.
+//  * FullyAssembledRows: the touched ghost columns of each touched field in field order
+//    (each sorted by local id, as the scalar FullyAssembledRows columns are:
+//    src/Algebra.jl:1245-1257); owned rows only.
+//  * SubAssembledRows (the default of the reference's multi-field assemblers,
+//    src/MultiField.jl:473-479): only owned cells are integrated; Gridap walks a cell's
+//    block matrix column-major with the block columns outer, so a ghost column (field j,
+//    node y) first appears at the scalar column's first-appearance cell, and among the
+//    columns first met in one cell field j's come before field j+1's.  The ghost columns
+//    are therefore the scalar SubAssembledRows ghost columns grouped by first cell (the
+//    groups the vector expansion uses), field-major inside a group.  Rows: the owned
+//    rows, then per part the touched ghost rows -- each row field with a touched block
+//    times the scalar ghost rows, by local id (field-major) -- holding explicit zeros
+//    (their triplets went to the owners, src/Algebra.jl:1048-1131).
 #include <algorithm>
 #include <string>
 #include <vector>
@@ -47,8 +58,10 @@ struct gd_mfmat {
   gd_mfield* M = nullptr;
   std::vector<int> rf, cf;       // row and column fields
   std::vector<int> ctouched;     // per column field: touched by some row field
+  std::vector<int> rtouched;     // per row field: touching some column field
   std::vector<int> btouched;     // nr * nc: block touched when the pattern was built
-  int64_t nrows = 0, nnz = 0;
+  int64_t nrows = 0, nnz = 0;    // owned rows (group gid order) and all stored entries
+  int64_t nrows_total = 0;       // owned rows, then the ghost rows of every part (SubAssembledRows)
   int64_t epoch = -1;            // assembly epoch the values were gathered from
   gd::DBuf<int64_t> rowptr;      // nrows + 1 (rows in group gid order)
   gd::DBuf<int32_t> colidx;      // local column id (per part)
@@ -75,6 +88,9 @@ struct MfPartInfo {
   int64_t first;   // first scalar gid of the part
   int64_t n_own;
   int64_t n_gcol;
+  int64_t gcol_off;   // scalar ghost columns of the part in the concatenated list
+  int64_t grow_off;   // scalar ghost rows of the part (concatenated, after the owned rows)
+  int64_t n_grow;
 };
 
 // group gid of the field-jj dof with scalar gid g (owner found by bisection over the
@@ -109,15 +125,45 @@ struct MfGroups {
   int nr, nc, nf;
   int rf[8], cf[8];
   int blk[8][8];      // block index rf[ii] * nf + cf[jj], -1 when not touched
-  int gofs[8];        // ghost-column offset (in units of n_gcol) of column field jj, -1 when untouched
+  int gofs[8];        // index of column field jj among the touched ones, -1 when untouched
+  int ntc;            // touched column fields
+  int rt[8];          // row field index of the t-th touched row field
+  int nrt;            // touched row fields
+  int sub;            // SubAssembledRows
+  int64_t nrows_own;  // nr * ngdofs
+  int64_t ngdofs;
 };
+
+// merged row m -> (part, row field index, scalar row in the scalar row space); ghost rows
+// (m >= nrows_own) of part p are nrt * n_grow rows, row field outer
+__device__ __forceinline__ void mf_any_row(const MfGroups& G, const MfPartInfo* parts, int np, int64_t m, int& p,
+                                           int& ii, int64_t& r, bool& ghost) {
+  ghost = m >= G.nrows_own;
+  if (!ghost) {
+    mf_row(parts, np, G.nr, m, p, ii, r);
+    return;
+  }
+  const int64_t gm = m - G.nrows_own;
+  int lo = 0, hi = np - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if ((int64_t)G.nrt * parts[mid].grow_off <= gm) lo = mid;
+    else hi = mid - 1;
+  }
+  p = lo;
+  const int64_t off = gm - (int64_t)G.nrt * parts[lo].grow_off;
+  const int t = parts[lo].n_grow ? (int)(off / parts[lo].n_grow) : 0;
+  ii = G.rt[t];
+  r = G.ngdofs + parts[lo].grow_off + (off - (int64_t)t * parts[lo].n_grow);
+}
 
 __global__ void k_mf_rowlen(MfGroups G, const MfPartInfo* __restrict__ parts, int np, int64_t nrows,
                             const int64_t* __restrict__ rowptr, int32_t* __restrict__ len) {
   for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < nrows; m += (int64_t)gridDim.x * blockDim.x) {
     int p, ii;
     int64_t r;
-    mf_row(parts, np, G.nr, m, p, ii, r);
+    bool ghost;
+    mf_any_row(G, parts, np, m, p, ii, r, ghost);
     const int64_t l = rowptr[r + 1] - rowptr[r];
     int k = 0;
     for (int jj = 0; jj < G.nc; ++jj) k += G.blk[ii][jj] >= 0;
@@ -127,39 +173,65 @@ __global__ void k_mf_rowlen(MfGroups G, const MfPartInfo* __restrict__ parts, in
 
 __global__ void k_mf_fill(MfGroups G, const MfPartInfo* __restrict__ parts, int np, int64_t nrows, int64_t nnz_blk,
                           const int64_t* __restrict__ rowptr, const int32_t* __restrict__ colidx,
-                          const int32_t* __restrict__ colgid, const int64_t* __restrict__ mrowptr,
+                          const int32_t* __restrict__ colgid, const int32_t* __restrict__ gstart,
+                          const int32_t* __restrict__ gsize, const int64_t* __restrict__ mrowptr,
                           int32_t* __restrict__ mcol, int64_t* __restrict__ mgid, int64_t* __restrict__ msrc) {
   for (int64_t m = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; m < nrows; m += (int64_t)gridDim.x * blockDim.x) {
     int p, ii;
     int64_t r;
-    mf_row(parts, np, G.nr, m, p, ii, r);
+    bool ghost;
+    mf_any_row(G, parts, np, m, p, ii, r, ghost);
     const MfPartInfo P = parts[p];
     const int64_t e0 = rowptr[r], e1 = rowptr[r + 1];
     int64_t eo = e0;   // end of the owned-column prefix (columns are sorted: owned first)
     while (eo < e1 && colidx[eo] < P.n_own) ++eo;
     int64_t o = mrowptr[m];
-    for (int pass = 0; pass < 2; ++pass) {
+    auto emit = [&](int jj, int b, int64_t e, int32_t col) {
+      mcol[o] = col;
+      mgid[o] = ghost ? -1 : mf_gid(parts, np, G.nc, jj, (int64_t)colgid[e]);
+      msrc[o] = ghost ? -1 : (int64_t)b * nnz_blk + e;   // ghost rows: explicit zeros
+      ++o;
+    };
+    for (int jj = 0; jj < G.nc; ++jj) {   // owned columns, field-major
+      const int b = G.blk[ii][jj];
+      if (b < 0) continue;
+      for (int64_t e = e0; e < eo; ++e) emit(jj, b, e, (int32_t)(jj * P.n_own + colidx[e]));
+    }
+    if (!G.sub) {   // ghost columns of each touched field in turn
       for (int jj = 0; jj < G.nc; ++jj) {
         const int b = G.blk[ii][jj];
         if (b < 0) continue;
-        const int64_t a0 = pass == 0 ? e0 : eo, a1 = pass == 0 ? eo : e1;
-        for (int64_t e = a0; e < a1; ++e) {
-          const int c = colidx[e];
-          mcol[o] = pass == 0 ? (int32_t)(jj * P.n_own + c)
-                              : (int32_t)(G.nc * P.n_own + G.gofs[jj] * P.n_gcol + (c - P.n_own));
-          mgid[o] = mf_gid(parts, np, G.nc, jj, (int64_t)colgid[e]);
-          msrc[o] = (int64_t)b * nnz_blk + e;
-          ++o;
+        for (int64_t e = eo; e < e1; ++e)
+          emit(jj, b, e, (int32_t)(G.nc * P.n_own + G.gofs[jj] * P.n_gcol + (colidx[e] - P.n_own)));
+      }
+      continue;
+    }
+    // SubAssembledRows: first-appearance groups, field-major inside a group
+    int64_t e = eo;
+    while (e < e1) {
+      const int64_t g0 = colidx[e] - P.n_own;
+      const int64_t s0 = gstart[P.gcol_off + g0], mg = gsize[P.gcol_off + g0];
+      int64_t f = e;
+      while (f < e1 && gstart[P.gcol_off + (colidx[f] - P.n_own)] == s0) ++f;
+      for (int jj = 0; jj < G.nc; ++jj) {
+        const int b = G.blk[ii][jj];
+        if (b < 0) continue;
+        for (int64_t x = e; x < f; ++x) {
+          const int64_t g = colidx[x] - P.n_own;
+          emit(jj, b, x, (int32_t)(G.nc * P.n_own + G.ntc * s0 + G.gofs[jj] * mg + (g - s0)));
         }
       }
+      e = f;
     }
   }
 }
 
 __global__ void k_mf_gather(int64_t n, const int64_t* __restrict__ src, const double* __restrict__ bvals,
                             double* __restrict__ out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = bvals[src[i]];
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t k = src[i];
+    out[i] = k >= 0 ? bvals[k] : 0.0;
+  }
 }
 
 __global__ void k_mf_rhs(MfGroups G, const MfPartInfo* __restrict__ parts, int np, int64_t nrows, int64_t ngdofs,
@@ -206,7 +278,10 @@ unsigned mf_grid(int64_t n) {
 
 std::vector<MfPartInfo> part_info(const gd_asm* A) {
   std::vector<MfPartInfo> v(A->parts.size());
-  for (size_t p = 0; p < A->parts.size(); ++p) v[p] = {A->parts[p].first_gdof, A->parts[p].n_own, A->parts[p].n_gcol};
+  for (size_t p = 0; p < A->parts.size(); ++p) {
+    const DevPart& P = A->parts[p];
+    v[p] = {P.first_gdof, P.n_own, P.n_gcol, P.gcol_off, P.grow_off, P.n_grow};
+  }
   return v;
 }
 
@@ -226,9 +301,9 @@ extern "C" int gd_mfield_create(gd_asm* A, int nfields, gd_mfield** out) {
   if (!A || !out) return fail(GD_ERR_ARG, "gd_mfield_create: null argument");
   if (nfields < 1 || nfields > 8) return fail(GD_ERR_ARG, "gd_mfield_create: 1 to 8 fields");
   if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_mfield_create: run gd_assemble_symbolic first");
-  if (A->strategy != GD_FULLY_ASSEMBLED_ROWS)
-    return fail(GD_ERR_UNSUPPORTED, "gd_mfield_create: multi-field assembly is built for FullyAssembledRows");
   if (A->bs != 1) return fail(GD_ERR_UNSUPPORTED, "gd_mfield_create: fields must be scalar");
+  if (A->strategy == GD_SUB_ASSEMBLED_ROWS && A->total_gcols > 0 && !A->gcol_gstart.p)
+    return fail(GD_ERR_STATE, "gd_mfield_create: the assembler has no ghost-column groups");
   gd_mfield* M = new gd_mfield();
   M->A = A;
   M->nf = nfields;
@@ -386,9 +461,16 @@ static MfGroups make_groups(const gd_mfmat* X) {
   for (int jj = 0; jj < G.nc; ++jj) G.cf[jj] = X->cf[jj];
   int k = 0;
   for (int jj = 0; jj < G.nc; ++jj) G.gofs[jj] = X->ctouched[jj] ? k++ : -1;
+  G.ntc = k;
+  G.nrt = 0;
+  for (int ii = 0; ii < G.nr; ++ii)
+    if (X->rtouched[ii]) G.rt[G.nrt++] = ii;
   for (int ii = 0; ii < G.nr; ++ii)
     for (int jj = 0; jj < G.nc; ++jj)
       G.blk[ii][jj] = X->btouched[ii * G.nc + jj] ? X->rf[ii] * M->nf + X->cf[jj] : -1;
+  G.sub = M->A->strategy == GD_SUB_ASSEMBLED_ROWS;
+  G.ngdofs = M->A->ngdofs;
+  G.nrows_own = X->nrows;
   return G;
 }
 
@@ -408,13 +490,21 @@ extern "C" int gd_mfmat_create(gd_mfield* M, int nr, const int* rf, int nc, cons
   X->rf.assign(rf, rf + nr);
   X->cf.assign(cf, cf + nc);
   X->ctouched.assign(nc, 0);
+  X->rtouched.assign(nr, 0);
   X->btouched.assign(nr * nc, 0);
   for (int jj = 0; jj < nc; ++jj)
     for (int ii = 0; ii < nr; ++ii) {
       X->btouched[ii * nc + jj] = M->touched[rf[ii] * M->nf + cf[jj]];
       X->ctouched[jj] |= X->btouched[ii * nc + jj];
+      X->rtouched[ii] |= X->btouched[ii * nc + jj];
     }
   X->nrows = (int64_t)nr * A->ngdofs;
+  int nrt = 0;
+  for (int t : X->rtouched) nrt += t;
+  int64_t ngrow = 0;
+  if (A->strategy == GD_SUB_ASSEMBLED_ROWS)
+    for (const DevPart& P : A->parts) ngrow += P.n_grow;
+  X->nrows_total = X->nrows + (int64_t)nrt * ngrow;
   const std::vector<MfPartInfo> pi = part_info(A);
   const int np = (int)pi.size();
   DBuf<MfPartInfo> dparts;
@@ -425,17 +515,18 @@ extern "C" int gd_mfmat_create(gd_mfield* M, int nr, const int* rf, int nc, cons
     delete X;
     return s;
   };
+  const int64_t NT = X->nrows_total;
   int s = dalloc(dparts, pi.size());
-  if (s == GD_OK) s = dalloc(len, std::max<int64_t>(X->nrows, 1));
-  if (s == GD_OK) s = dalloc(X->rowptr, X->nrows + 1);
+  if (s == GD_OK) s = dalloc(len, std::max<int64_t>(NT, 1));
+  if (s == GD_OK) s = dalloc(X->rowptr, NT + 1);
   if (s != GD_OK) return cleanup(s);
   if (cudaMemcpyAsync(dparts.p, pi.data(), sizeof(MfPartInfo) * pi.size(), cudaMemcpyHostToDevice, st) != cudaSuccess)
     return cleanup(fail(GD_ERR_CUDA, "gd_mfmat_create: copy"));
   const MfGroups G = make_groups(X);
-  if (X->nrows) k_mf_rowlen<<<mf_grid(X->nrows), kMfThreads, 0, st>>>(G, dparts.p, np, X->nrows, A->rowptr.p, len.p);
+  if (NT) k_mf_rowlen<<<mf_grid(NT), kMfThreads, 0, st>>>(G, dparts.p, np, NT, A->rowptr.p, len.p);
   if (cudaGetLastError() != cudaSuccess) return cleanup(fail(GD_ERR_CUDA, "gd_mfmat_create: row lengths"));
-  if ((s = exclusive_scan_i32(len.p, X->rowptr.p, X->nrows, st)) != GD_OK) return cleanup(s);
-  if (cudaMemcpyAsync(&X->nnz, X->rowptr.p + X->nrows, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
+  if ((s = exclusive_scan_i32(len.p, X->rowptr.p, NT, st)) != GD_OK) return cleanup(s);
+  if (cudaMemcpyAsync(&X->nnz, X->rowptr.p + NT, sizeof(int64_t), cudaMemcpyDeviceToHost, st) != cudaSuccess ||
       cudaStreamSynchronize(st) != cudaSuccess)
     return cleanup(fail(GD_ERR_CUDA, "gd_mfmat_create: entry count"));
   const size_t nz = (size_t)std::max<int64_t>(X->nnz, 1);
@@ -445,10 +536,12 @@ extern "C" int gd_mfmat_create(gd_mfield* M, int nr, const int* rf, int nc, cons
   if (s == GD_OK) s = dalloc(X->vals, nz);
   if (s == GD_OK) s = dalloc(X->rhs, std::max<int64_t>(X->nrows, 1));
   if (s != GD_OK) return cleanup(s);
+  if (NT) {
+    k_mf_fill<<<mf_grid(NT), kMfThreads, 0, st>>>(G, dparts.p, np, NT, std::max<int64_t>(A->nnz_own, 1), A->rowptr.p,
+                                                 A->colidx.p, A->colgid.p, A->gcol_gstart.p, A->gcol_gsize.p,
+                                                 X->rowptr.p, X->colidx.p, X->colgid.p, X->src.p);
+  }
   if (X->nrows) {
-    k_mf_fill<<<mf_grid(X->nrows), kMfThreads, 0, st>>>(G, dparts.p, np, X->nrows, std::max<int64_t>(A->nnz_own, 1),
-                                                       A->rowptr.p, A->colidx.p, A->colgid.p, X->rowptr.p,
-                                                       X->colidx.p, X->colgid.p, X->src.p);
     k_mf_rhs<<<mf_grid(X->nrows), kMfThreads, 0, st>>>(G, dparts.p, np, X->nrows, std::max<int64_t>(A->ngdofs, 1),
                                                       M->brhs.p, X->rhs.p);
   }
@@ -495,31 +588,39 @@ extern "C" int gd_mfmat_refresh(gd_mfmat* X) {
 }
 
 extern "C" int gd_mfmat_sizes(const gd_mfmat* X, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
-                              int64_t* n_ghost_cols) {
+                              int64_t* n_ghost_rows, int64_t* n_ghost_cols) {
   if (!X) return fail(GD_ERR_ARG, "gd_mfmat_sizes: null argument");
   const gd_asm* A = X->M->A;
   if (part < 0 || part >= (int)A->parts.size()) return fail(GD_ERR_ARG, "gd_mfmat_sizes: bad part");
   const DevPart& P = A->parts[part];
   const int nr = (int)X->rf.size(), nc = (int)X->cf.size();
-  int ntc = 0;
+  int ntc = 0, nrt = 0;
   for (int t : X->ctouched) ntc += t;
+  for (int t : X->rtouched) nrt += t;
+  const int64_t ngr = A->strategy == GD_SUB_ASSEMBLED_ROWS ? (int64_t)nrt * P.n_grow : 0;
   cudaStream_t st = A->test->model->ctx->stream;
-  int64_t b[2];
+  int64_t b[4];
   const int64_t r0 = (int64_t)nr * P.first_gdof, r1 = r0 + (int64_t)nr * P.n_own;
+  const int64_t g0 = X->nrows + (int64_t)nrt * P.grow_off, g1 = g0 + ngr;
   GD_CUDA_TRY(cudaMemcpyAsync(&b[0], X->rowptr.p + r0, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaMemcpyAsync(&b[1], X->rowptr.p + r1, sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&b[2], X->rowptr.p + (ngr ? g0 : 0), sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(&b[3], X->rowptr.p + (ngr ? g1 : 0), sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
-  if (nrows) *nrows = (int64_t)nr * P.n_own;
+  if (nrows) *nrows = (int64_t)nr * P.n_own + ngr;
   if (ncols) *ncols = (int64_t)nc * P.n_own + (int64_t)ntc * P.n_gcol;
-  if (nnz) *nnz = b[1] - b[0];
+  if (nnz) *nnz = (b[1] - b[0]) + (b[3] - b[2]);
+  if (n_ghost_rows) *n_ghost_rows = ngr;
   if (n_ghost_cols) *n_ghost_cols = (int64_t)ntc * P.n_gcol;
   return GD_OK;
 }
 
-// The part's rows: local CSR (columns: the group's owned columns, then the ghost columns),
-// ghost column gids and owners (group numbering) and the right-hand side.
+// The part's rows (owned rows, then its ghost rows): local CSR (columns: the group's owned
+// columns, then the ghost columns), ghost row and ghost column gids and owners (group
+// numberings) and the right-hand side (ghost rows 0).
 extern "C" int gd_mfmat_export(const gd_mfmat* X, int part, int64_t* rowptr, int32_t* colidx, double* vals,
-                               int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs) {
+                               int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
+                               int32_t* ghost_col_owners, double* rhs) {
   if (!X) return fail(GD_ERR_ARG, "gd_mfmat_export: null argument");
   const gd_mfield* M = X->M;
   const gd_asm* A = M->A;
@@ -527,40 +628,70 @@ extern "C" int gd_mfmat_export(const gd_mfmat* X, int part, int64_t* rowptr, int
   const DevPart& P = A->parts[part];
   const gd_space* S = A->test;
   cudaStream_t st = S->model->ctx->stream;
+  const bool sub = A->strategy == GD_SUB_ASSEMBLED_ROWS;
   const int nr = (int)X->rf.size(), nc = (int)X->cf.size();
+  int ntc = 0, nrt = 0;
+  for (int t : X->ctouched) ntc += t;
+  for (int t : X->rtouched) nrt += t;
   const int64_t r0 = (int64_t)nr * P.first_gdof, nrow = (int64_t)nr * P.n_own;
-  std::vector<int64_t> rp(nrow + 1);
+  const int64_t ngr = sub ? (int64_t)nrt * P.n_grow : 0;
+  const int64_t g0 = X->nrows + (int64_t)nrt * P.grow_off;
+  std::vector<int64_t> rp(nrow + 1), gp(ngr + 1);
   GD_CUDA_TRY(cudaMemcpyAsync(rp.data(), X->rowptr.p + r0, sizeof(int64_t) * (nrow + 1), cudaMemcpyDeviceToHost, st));
+  if (ngr) GD_CUDA_TRY(cudaMemcpyAsync(gp.data(), X->rowptr.p + g0, sizeof(int64_t) * (ngr + 1), cudaMemcpyDeviceToHost, st));
   GD_CUDA_TRY(cudaStreamSynchronize(st));
-  const int64_t n = rp[nrow] - rp[0];
-  if (rowptr)
+  const int64_t n = rp[nrow] - rp[0], ng = ngr ? gp[ngr] - gp[0] : 0;
+  if (rowptr) {
     for (int64_t i = 0; i <= nrow; ++i) rowptr[i] = rp[i] - rp[0];
+    for (int64_t i = 1; i <= ngr; ++i) rowptr[nrow + i] = n + gp[i] - gp[0];
+  }
   if (colidx && n) GD_CUDA_TRY(cudaMemcpyAsync(colidx, X->colidx.p + rp[0], sizeof(int32_t) * n, cudaMemcpyDeviceToHost, st));
+  if (colidx && ng) GD_CUDA_TRY(cudaMemcpyAsync(colidx + n, X->colidx.p + gp[0], sizeof(int32_t) * ng, cudaMemcpyDeviceToHost, st));
   if (vals && n) GD_CUDA_TRY(cudaMemcpyAsync(vals, X->vals.p + rp[0], sizeof(double) * n, cudaMemcpyDeviceToHost, st));
+  if (vals && ng) GD_CUDA_TRY(cudaMemcpyAsync(vals + n, X->vals.p + gp[0], sizeof(double) * ng, cudaMemcpyDeviceToHost, st));
   if (rhs && nrow) GD_CUDA_TRY(cudaMemcpyAsync(rhs, X->rhs.p + r0, sizeof(double) * nrow, cudaMemcpyDeviceToHost, st));
-  if (ghost_col_gids || ghost_col_owners) {
-    std::vector<int64_t> gid(P.nfree);
-    std::vector<int32_t> own(P.nfree), gcl(P.n_gcol);
-    if (P.nfree) {
-      GD_CUDA_TRY(cudaMemcpyAsync(gid.data(), S->lid_gid.p + P.lid_off, sizeof(int64_t) * P.nfree, cudaMemcpyDeviceToHost, st));
-      GD_CUDA_TRY(cudaMemcpyAsync(own.data(), S->lid_owner.p + P.lid_off, sizeof(int32_t) * P.nfree, cudaMemcpyDeviceToHost, st));
-    }
-    if (P.n_gcol)
-      GD_CUDA_TRY(cudaMemcpyAsync(gcl.data(), A->gcol_lid.p + P.gcol_off, sizeof(int32_t) * P.n_gcol, cudaMemcpyDeviceToHost, st));
-    GD_CUDA_TRY(cudaStreamSynchronize(st));
+  std::vector<int64_t> gid(P.nfree);
+  std::vector<int32_t> own(P.nfree), gcl(P.n_gcol), grl(sub ? P.n_grow : 0), gst(sub ? P.n_gcol : 0),
+      gsz(sub ? P.n_gcol : 0);
+  if (P.nfree) {
+    GD_CUDA_TRY(cudaMemcpyAsync(gid.data(), S->lid_gid.p + P.lid_off, sizeof(int64_t) * P.nfree, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaMemcpyAsync(own.data(), S->lid_owner.p + P.lid_off, sizeof(int32_t) * P.nfree, cudaMemcpyDeviceToHost, st));
+  }
+  if (P.n_gcol)
+    GD_CUDA_TRY(cudaMemcpyAsync(gcl.data(), A->gcol_lid.p + P.gcol_off, sizeof(int32_t) * P.n_gcol, cudaMemcpyDeviceToHost, st));
+  if (sub && P.n_grow)
+    GD_CUDA_TRY(cudaMemcpyAsync(grl.data(), A->grow_lid.p + P.grow_off, sizeof(int32_t) * P.n_grow, cudaMemcpyDeviceToHost, st));
+  if (sub && P.n_gcol) {
+    GD_CUDA_TRY(cudaMemcpyAsync(gst.data(), A->gcol_gstart.p + P.gcol_off, sizeof(int32_t) * P.n_gcol, cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaMemcpyAsync(gsz.data(), A->gcol_gsize.p + P.gcol_off, sizeof(int32_t) * P.n_gcol, cudaMemcpyDeviceToHost, st));
+  }
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (rhs)
+    for (int64_t i = 0; i < ngr; ++i) rhs[nrow + i] = 0.0;
+  auto group_gid = [&](int ng_, int jj, int lid) {
+    const DevPart& Q = A->parts[own[lid]];
+    return (int64_t)ng_ * Q.first_gdof + (int64_t)jj * Q.n_own + (gid[lid] - Q.first_gdof);
+  };
+  if (sub) {   // ghost rows: touched row fields in order, each the scalar ghost rows
     int64_t k = 0;
-    for (int jj = 0; jj < nc; ++jj) {
-      if (!X->ctouched[jj]) continue;
-      for (int64_t i = 0; i < P.n_gcol; ++i, ++k) {
-        const int64_t g = gid[gcl[i]];
-        const int q = own[gcl[i]];
-        const DevPart& Q = A->parts[q];
-        if (ghost_col_gids) ghost_col_gids[k] = (int64_t)nc * Q.first_gdof + (int64_t)jj * Q.n_own + (g - Q.first_gdof);
-        if (ghost_col_owners) ghost_col_owners[k] = q;
+    for (int ii = 0; ii < nr; ++ii) {
+      if (!X->rtouched[ii]) continue;
+      for (int64_t x = 0; x < P.n_grow; ++x, ++k) {
+        if (ghost_row_gids) ghost_row_gids[k] = group_gid(nr, ii, grl[x]);
+        if (ghost_row_owners) ghost_row_owners[k] = own[grl[x]];
       }
     }
   }
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  int kt = 0;
+  for (int jj = 0; jj < nc; ++jj) {
+    if (!X->ctouched[jj]) continue;
+    for (int64_t g = 0; g < P.n_gcol; ++g) {
+      const int64_t pos = sub ? (int64_t)ntc * gst[g] + (int64_t)kt * gsz[g] + (g - gst[g]) : (int64_t)kt * P.n_gcol + g;
+      if (ghost_col_gids) ghost_col_gids[pos] = group_gid(nc, jj, gcl[g]);
+      if (ghost_col_owners) ghost_col_owners[pos] = own[gcl[g]];
+    }
+    ++kt;
+  }
   return GD_OK;
 }
 

@@ -791,6 +791,144 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   return GD_OK;
 }
 
+// ---- 2D Q_k (k = 2, 3): values and right-hand side in one kernel, one thread per row ----
+// A 2D row has at most (2k+1)^2 entries (25 for Q2), so one thread forms its whole row:
+// it decodes its node's (at most 4) cells once, then walks its CSR entries (the stencil
+// code of each entry gives the offset and the cells that hold both nodes through the
+// shared-memory entry table, as in qk_matrix_rows) and finally the right-hand side (source
+// term and Dirichlet lifting with the same cells).  Consecutive threads own consecutive
+// rows, so a warp's values are one contiguous range of the CSR value array.
+template <int K, typename CodeT, bool FN, bool UD>
+__global__ void __launch_bounds__(128)
+k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
+               const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
+               const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
+               const double* __restrict__ f_nodal, const double* __restrict__ u_dir, double* __restrict__ vals,
+               double* __restrict__ rhs, int32_t* __restrict__ bad) {
+  using L = Lat<2, K>;
+  constexpr int NN = L::NN;
+  __shared__ double s_K[NN * NN];
+  __shared__ double s_M[FN ? NN * NN : 1];
+  __shared__ double s_F[NN];
+  __shared__ uint16_t s_tab[EntryTab<2, K>::SIZE];
+  __shared__ double s_kap[4][128];   // per thread: coefficient and local index of its 4 slots
+  __shared__ int s_lx[4][128];       // (shared, not local, memory: they are indexed at run time)
+  for (int i = threadIdx.x; i < NN * NN; i += blockDim.x) {
+    s_K[i] = Khat[i];
+    if (FN) s_M[i] = Mhat[i];
+  }
+  for (int i = threadIdx.x; i < NN; i += blockDim.x) s_F[i] = Fhat[i];
+  build_entry_tab<2, K>(s_tab);
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows_own) return;
+  const uint32_t N0 = (uint32_t)g.N[0];
+  const uint32_t lin = (uint32_t)row_node[r];
+  const int X0 = (int)(lin % N0), X1 = (int)(lin / N0);
+  const int rm0 = X0 % K, rm1 = X1 % K;
+  const int onb = (rm0 == 0 ? 1 : 0) | (rm1 == 0 ? 2 : 0);
+  const int t = threadIdx.x;
+  uint32_t vmask = 0;
+  int nbad = 0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    const int s0 = a & 1, s1 = (a >> 1) & 1;
+    const int c0 = s0 ? X0 / K : X0 / K - 1, c1 = s1 ? X1 / K : X1 / K - 1;
+    const bool ok = (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
+                    c1 < (int)g.n[1];
+    const double k = ok ? __ldg(kappa + (int64_t)c1 * g.n[0] + c0) : 0.0;
+    if (ok) nbad += !(k > 0.0) || !isfinite(k);
+    s_kap[a][t] = k;
+    s_lx[a][t] = (s0 ? rm0 : K) + L::KP1 * (s1 ? rm1 : K);
+    vmask |= (uint32_t)ok << a;
+  }
+  const uint16_t* et = s_tab + onb * EntryTab<2, K>::E;
+  const int64_t e0 = rowptr[r];
+  const int len = (int)(rowptr[r + 1] - e0);
+  // all stencil codes of the row first (independent loads, one memory latency), then the
+  // entries; a 2D row has at most MAXE of them
+  constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
+  int cv[MAXE];
+#pragma unroll
+  for (int i = 0; i < MAXE; ++i) cv[i] = i < len ? (int)__ldg(code + e0 + i) : 0;
+#pragma unroll
+  for (int i = 0; i < MAXE; ++i) {
+    if (i >= len) break;
+    const int info = et[cv[i]];
+    const int off = (info & 255) - 128;
+    const int fixed = (info >> 8) & 7, both = (info >> 11) & 7;
+    double v = 0.0;
+    int sb = both;
+    while (true) {
+      const int a = fixed | sb;
+      if ((vmask >> a) & 1u) v = fma(s_kap[a][t], s_K[s_lx[a][t] * (NN + 1) + off], v);
+      if (sb == 0) break;
+      sb = (sb - 1) & both;
+    }
+    vals[e0 + i] = v;
+  }
+  // right-hand side: source over the node's cells minus the lifting of the Dirichlet values
+  double b = 0.0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    if (!((vmask >> a) & 1u)) continue;
+    const int la = s_lx[a][t];
+    if (!FN) b += f_const * s_F[la];
+    if (FN || UD) {
+      const double ka = s_kap[a][t];
+      const int64_t c0 = (a & 1) ? X0 / K : X0 / K - 1, c1 = (a & 2) ? X1 / K : X1 / K - 1;
+      for (int lj = 0; lj < NN; ++lj) {
+        const int64_t Y0 = (int64_t)K * c0 + lj % L::KP1, Y1 = (int64_t)K * c1 + lj / L::KP1;
+        const int64_t ylin = Y1 * g.N[0] + Y0;
+        if (FN) b += s_M[la * NN + lj] * __ldg(f_nodal + ylin);
+        if (UD) {
+          const bool dir = (g.dsides[0] && Y0 == 0) || (g.dsides[1] && Y0 == g.N[0] - 1) ||
+                           (g.dsides[2] && Y1 == 0) || (g.dsides[3] && Y1 == g.N[1] - 1);
+          if (dir) b -= ka * s_K[la * NN + lj] * __ldg(u_dir + ylin);
+        }
+      }
+    }
+  }
+  rhs[r] = b;
+  if (nbad) atomicAdd(bad, nbad);
+}
+
+template <int K, typename CodeT>
+static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, int32_t* bad,
+                              cudaStream_t st) {
+  const Geom& g = A->test->geom;
+  const int64_t R = A->ngdofs;
+  const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
+  const unsigned nb = (unsigned)((R + 127) / 128);
+  const CodeT* code = reinterpret_cast<const CodeT*>(A->code.p);
+#define GD_R2D(FNV, UDV)                                                                                          \
+  k_rows2d_fused<K, CodeT, FNV, UDV><<<nb, 128, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa, A->Khat.p, \
+                                                         A->Mhat.p, A->Fhat.p, f_const, f_nodal, udir, A->vals.p,  \
+                                                         A->rhs.p, bad)
+  if (f_nodal && udir) GD_R2D(true, true);
+  else if (f_nodal) GD_R2D(true, false);
+  else if (udir) GD_R2D(false, true);
+  else GD_R2D(false, false);
+#undef GD_R2D
+  GD_CUDA_TRY(cudaGetLastError());
+  return GD_OK;
+}
+
+template <int K>
+static int launch_rows2d(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, int32_t* bad,
+                         cudaStream_t st) {
+  if (A->ngdofs == 0) return GD_OK;
+  if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
+  const int s = A->code_bytes == 1 ? launch_rows2d_code<K, uint8_t>(A, kappa, f_nodal, f_const, bad, st)
+                                   : launch_rows2d_code<K, uint16_t>(A, kappa, f_nodal, f_const, bad, st);
+  if (s != GD_OK) return s;
+  if (A->profiling) {   // one fused kernel: the rhs phase is empty
+    GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
+    GD_CUDA_TRY(cudaEventRecord(A->ev[3], st));
+  }
+  return GD_OK;
+}
+
 // Values of the owned rows with an arbitrary reference element table (a linear
 // combination of the stiffness and mass tables), kappa per cell: the generic row
 // kernel over the assembler's pattern, into `vals` (multi-field blocks).
@@ -893,8 +1031,8 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   if (A->fast_q1 && g.dim == 3) s = launch_q1<3>(A, kappa, fn, c->f_const, bad, st);
   else if (A->fast_q1 && g.dim == 2) s = launch_q1<2>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 2 && g.k == 1) s = launch_numeric<2, 1>(A, kappa, fn, c->f_const, bad, st);
-  else if (g.dim == 2 && g.k == 2) s = launch_numeric<2, 2>(A, kappa, fn, c->f_const, bad, st);
-  else if (g.dim == 2 && g.k == 3) s = launch_numeric<2, 3>(A, kappa, fn, c->f_const, bad, st);
+  else if (g.dim == 2 && g.k == 2) s = launch_rows2d<2>(A, kappa, fn, c->f_const, bad, st);
+  else if (g.dim == 2 && g.k == 3) s = launch_rows2d<3>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 3 && g.k == 1) s = launch_numeric<3, 1>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 3 && g.k == 2) s = launch_numeric<3, 2>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 3 && g.k == 3) s = launch_numeric<3, 3>(A, kappa, fn, c->f_const, bad, st);
@@ -960,8 +1098,10 @@ extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nn
   if (ngdofs) *ngdofs = A->ngdofs;
   if (nnz_owned) *nnz_owned = A->nnz_own;
   if (nnz_total) *nnz_total = A->nnz_total;
-  // cube Q1: k_prescale + k_numeric_q1; other Q1: k_numeric_q1; Q_k: k_numeric_qk_rows + k_numeric_rhs
-  if (kernels) *kernels = A->fast_q1 ? (A->q1c_cube ? 2 : 1) : 2;
+  // cube Q1: k_prescale + k_numeric_q1; other Q1: k_numeric_q1; 2D Q2/Q3: k_rows2d_fused;
+  // 3D Q_k: k_numeric_qk_rows + k_numeric_rhs
+  const bool fused2d = !A->fast_q1 && A->test->geom.dim == 2 && A->test->geom.k >= 2 && A->bs == 1;
+  if (kernels) *kernels = A->fast_q1 ? (A->q1c_cube ? 2 : 1) : (fused2d ? 1 : 2);
   return GD_OK;
 }
 

@@ -612,6 +612,8 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   A->sell.release();
   gd::qp_release(A->qp);
   A->qp = nullptr;
+  dfreeb(A->gcol_gstart);
+  dfreeb(A->gcol_gsize);
   dfreeb(A->row_pat);
   dfreeb(A->pat);
   dfreeb(A->w_cells);
@@ -732,7 +734,9 @@ static int symbolic_impl(gd_asm* A) {
       GD_TRY(launch_ok("k_assign_ghost_cols"));
     }
   }
-  if (S->ncomp > 1) GD_TRY(gcol_groups(A, ckey.p, rank.p, ncand));
+  // first-appearance groups of the ghost columns: the vector expansion and the
+  // multi-field matrices (SubAssembledRows) order columns group by group
+  if (S->ncomp > 1 || A->strategy == GD_SUB_ASSEMBLED_ROWS) GD_TRY(gcol_groups(A, ckey.p, rank.p, ncand));
   dfreeb(key);
   dfreeb(ckey);
   dfreeb(clid);

@@ -151,8 +151,8 @@ SIGNATURES = {
     "gd_mfmat_destroy": [P],
     "gd_mfmat_refresh": [P],
     "gd_mfmat_counts": [P, I64P, I64P],
-    "gd_mfmat_sizes": [P, C.c_int, I64P, I64P, I64P, I64P],
-    "gd_mfmat_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, DP],
+    "gd_mfmat_sizes": [P, C.c_int, I64P, I64P, I64P, I64P, I64P],
+    "gd_mfmat_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, I64P, I32P, DP],
     "gd_mfmat_spmv": [P, P, P, C.c_int],
     "gd_dg_space_create": [P, C.c_int, PP],
     "gd_dg_space_destroy": [P],
@@ -160,8 +160,9 @@ SIGNATURES = {
     "gd_dg_local_sizes": [P, C.c_int, I64P, I64P, I64P],
     "gd_dg_get_gids": [P, C.c_int, I64P, I32P],
     "gd_dg_assemble": [P, C.POINTER(gd_dg_form)],
-    "gd_dg_matrix_sizes": [P, C.c_int, I64P, I64P, I64P, I64P],
-    "gd_dg_matrix_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, DP],
+    "gd_dg_set_strategy": [P, C.c_int],
+    "gd_dg_matrix_sizes": [P, C.c_int, I64P, I64P, I64P, I64P, I64P],
+    "gd_dg_matrix_export": [P, C.c_int, I64P, I32P, DP, I64P, I32P, I64P, I32P, DP],
     "gd_dg_spmv": [P, P, P, C.c_int],
     "gd_dg_solve": [P, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],
     "gd_dg_l2_error": [P, P, P, C.c_int, C.c_int, DP],

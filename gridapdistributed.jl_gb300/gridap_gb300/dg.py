@@ -132,8 +132,9 @@ def _face_values(fn, trian: BoundaryTriangulation, degree, with_normal):
 
 
 class DGMatrix:
-    """The assembled SIPG operator: a PSparseMatrix over the DG dofs (owned rows per part,
-    FullyAssembledRows columns) with its right-hand side; parts live on the device."""
+    """The assembled SIPG operator: a PSparseMatrix over the DG dofs (per part the owned
+    rows, and the touched ghost rows under SubAssembledRows) with its right-hand side;
+    parts live on the device."""
 
     def __init__(self, V: DistributedDGFESpace):
         self.V = V
@@ -149,19 +150,23 @@ class DGMatrix:
         import scipy.sparse as sps
         out = []
         for p in range(self.V.model.num_parts):
-            a, b, n, g = (C.c_int64() for _ in range(4))
-            L.call("gd_dg_matrix_sizes", self.V.handle, p, C.byref(a), C.byref(b), C.byref(n), C.byref(g))
+            a, b, n, gr, g = (C.c_int64() for _ in range(5))
+            L.call("gd_dg_matrix_sizes", self.V.handle, p, C.byref(a), C.byref(b), C.byref(n), C.byref(gr),
+                   C.byref(g))
             rp = np.zeros(a.value + 1, dtype=np.int64)
             ci = np.zeros(n.value, dtype=np.int32)
             vv = np.zeros(n.value, dtype=np.float64)
+            rg = np.zeros(gr.value, dtype=np.int64)
+            ro = np.zeros(gr.value, dtype=np.int32)
             gg = np.zeros(g.value, dtype=np.int64)
             go = np.zeros(g.value, dtype=np.int32)
             bb = np.zeros(a.value, dtype=np.float64)
             L.call("gd_dg_matrix_export", self.V.handle, p, L.ptr(rp, C.c_int64), L.ptr(ci, C.c_int32),
-                   L.ptr(vv, C.c_double), L.ptr(gg, C.c_int64), L.ptr(go, C.c_int32), L.ptr(bb, C.c_double))
+                   L.ptr(vv, C.c_double), L.ptr(rg, C.c_int64), L.ptr(ro, C.c_int32), L.ptr(gg, C.c_int64),
+                   L.ptr(go, C.c_int32), L.ptr(bb, C.c_double))
             _, nown, first = self.V.local_sizes(p)
             own = np.arange(first, first + nown, dtype=np.int64)
-            rows = OwnAndGhostIndices(self.n_global, p, own, np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32))
+            rows = OwnAndGhostIndices(self.n_global, p, own, rg, ro)
             cols = OwnAndGhostIndices(self.n_global, p, own, gg, go)
             out.append((sps.csr_matrix((vv, ci, rp), shape=(a.value, b.value)), rows, cols, (rp, ci, vv), bb))
         self._parts = out
@@ -212,8 +217,12 @@ class DGVector:
         return np.concatenate(self.matrix.rhs_parts())
 
 
-def assemble_dg(V: DistributedDGFESpace, a: SIPGForm, l: SIPGSource):
-    """``assemble_matrix_and_vector`` for the SIPG forms on a DG space."""
+def assemble_dg(V: DistributedDGFESpace, a: SIPGForm, l: SIPGSource, strategy=None):
+    """``assemble_matrix_and_vector`` for the SIPG forms on a DG space; ``strategy`` is
+    SubAssembledRows() (the reference's default) or FullyAssembledRows()."""
+    from .distributed import SubAssembledRows
+    strategy = strategy if strategy is not None else SubAssembledRows()
+    L.call("gd_dg_set_strategy", V.handle, strategy.code)
     model = V.model
     dim = model.dim
     deg = int(a.measure.degree)

@@ -488,11 +488,19 @@ def integral_source(f=0.0, measure: Measure = None):
     return SourceForm(f, measure)
 
 
+class DGAssembler:
+    """``SparseMatrixAssembler(V, V, strategy)`` on a DG space: the strategy of its system."""
+
+    def __init__(self, V, strategy):
+        self.V, self.strategy = V, strategy
+
+
 def SparseMatrixAssembler(U, V, strategy=None):
+    from .dg import DistributedDGFESpace
     from .multifield import DistributedMultiFieldFESpace, MultiFieldAssembler
+    if isinstance(V, DistributedDGFESpace):
+        return DGAssembler(V, strategy or SubAssembledRows())
     if isinstance(U, DistributedMultiFieldFESpace) or isinstance(V, DistributedMultiFieldFESpace):
-        if not isinstance(strategy, FullyAssembledRows):
-            raise NotImplementedError("multi-field assembly is built for FullyAssembledRows")
         return MultiFieldAssembler(U, V, strategy)
     return DistributedSparseMatrixAssembler(U, V, strategy or SubAssembledRows())
 
@@ -868,10 +876,11 @@ class AffineFEOperator:
         self.U, self.V = U, V
         self.a, self.l = a, l
         if isinstance(V, DistributedDGFESpace):
-            if U is not V or assem is not None:
-                raise NotImplementedError("DG: trial space = test space, the built-in assembly")
-            self.assem = None
-            self.matrix, self.vector = assemble_dg(V, a, l)
+            if U is not V:
+                raise NotImplementedError("DG: trial space = test space")
+            strategy = getattr(assem, "strategy", None)
+            self.assem = assem
+            self.matrix, self.vector = assemble_dg(V, a, l, strategy)
             return
         self.assem = assem if assem is not None else SparseMatrixAssembler(U, V)
         if isinstance(self.assem, MultiFieldAssembler):

@@ -12,8 +12,9 @@
 The fields share one scalar test space (and one trial space); the bilinear form is
 ``sum_ij ∫(κ (stiffness[i][j] ∇(u_j)⋅∇(v_i) + mass[i][j] u_j v_i))dΩ``, the linear form
 ``sum_i ∫(src[i] v_i)dΩ`` — the vocabulary of the reference's block-assembler test
-(test/BlockSparseMatrixAssemblersTests.jl:111-114).  Assembly strategy:
-FullyAssembledRows (the strategy that test uses).
+(test/BlockSparseMatrixAssemblersTests.jl:111-114).  Assembly strategy: SubAssembledRows
+(the default of the reference's multi-field assemblers) or FullyAssembledRows (the strategy
+that test passes to its assemblers).
 """
 from __future__ import annotations
 
@@ -23,8 +24,8 @@ from dataclasses import dataclass
 import numpy as np
 
 from . import _lib as L
-from .distributed import (DistributedSingleFieldFESpace, FullyAssembledRows, LocalIndices, Measure,
-                          OwnAndGhostIndices, PRange)
+from .distributed import (DistributedSingleFieldFESpace, LocalIndices, Measure, OwnAndGhostIndices, PRange,
+                          SubAssembledRows)
 
 
 class ConsecutiveMultiFieldStyle:
@@ -126,13 +127,12 @@ def integral_multifield_source(src, measure: Measure = None):
 
 
 class MultiFieldAssembler:
-    """``SparseMatrixAssembler(X, Y, FullyAssembledRows())`` for multi-field spaces: the
-    scalar assembler of the shared space plus the field set (gd_mfield)."""
+    """``SparseMatrixAssembler(X, Y, strategy)`` for multi-field spaces (SubAssembledRows by
+    default, as the reference's): the scalar assembler of the shared space plus the field
+    set (gd_mfield)."""
 
     def __init__(self, X: DistributedMultiFieldFESpace, Y: DistributedMultiFieldFESpace, strategy=None):
-        strategy = strategy or FullyAssembledRows()
-        if not isinstance(strategy, FullyAssembledRows):
-            raise NotImplementedError("multi-field assembly: FullyAssembledRows")
+        strategy = strategy or SubAssembledRows()
         if X.num_fields() != Y.num_fields() or X.space is not Y.space:
             raise NotImplementedError("trial and test fields on one shared scalar space")
         if type(X.style) is not type(Y.style) or X.groups() != Y.groups():
@@ -239,19 +239,22 @@ class MultiFieldMatrix:
         nr, nc = len(self.rf), len(self.cf)
         out = []
         for p in range(V.model.num_parts):
-            a, b, n, g = (C.c_int64() for _ in range(4))
-            L.call("gd_mfmat_sizes", self.handle, p, C.byref(a), C.byref(b), C.byref(n), C.byref(g))
+            a, b, n, gr, g = (C.c_int64() for _ in range(5))
+            L.call("gd_mfmat_sizes", self.handle, p, C.byref(a), C.byref(b), C.byref(n), C.byref(gr), C.byref(g))
             rp = np.zeros(a.value + 1, dtype=np.int64)
             ci = np.zeros(n.value, dtype=np.int32)
             vv = np.zeros(n.value, dtype=np.float64)
+            rg = np.zeros(gr.value, dtype=np.int64)
+            ro = np.zeros(gr.value, dtype=np.int32)
             gg = np.zeros(g.value, dtype=np.int64)
             go = np.zeros(g.value, dtype=np.int32)
             bb = np.zeros(a.value, dtype=np.float64)
             L.call("gd_mfmat_export", self.handle, p, L.ptr(rp, C.c_int64), L.ptr(ci, C.c_int32),
-                   L.ptr(vv, C.c_double), L.ptr(gg, C.c_int64), L.ptr(go, C.c_int32), L.ptr(bb, C.c_double))
+                   L.ptr(vv, C.c_double), L.ptr(rg, C.c_int64), L.ptr(ro, C.c_int32), L.ptr(gg, C.c_int64),
+                   L.ptr(go, C.c_int32), L.ptr(bb, C.c_double))
             _, nown, first = V.local_sizes(p)
             rows = OwnAndGhostIndices(self.n_rows, p, np.arange(nr * first, nr * (first + nown), dtype=np.int64),
-                                      np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32))
+                                      rg, ro)
             cols = OwnAndGhostIndices(self.n_cols, p, np.arange(nc * first, nc * (first + nown), dtype=np.int64),
                                       gg, go)
             mat = sps.csr_matrix((vv, ci, rp), shape=(a.value, b.value))

@@ -376,14 +376,16 @@ int gd_solve_learned(gd_asm* a, gd_learned* net, double rtol, int maxit, double*
                      gd_solve_stats* stats, int32_t* fallback_used);
 
 /* ---- Multi-field systems (src/MultiField.jl, test/BlockSparseMatrixAssemblersTests.jl) ----
- * n fields (n <= 8) that share the test/trial spaces of one FullyAssembledRows
- * assembler (after gd_assemble_symbolic).  The bilinear form is
+ * n fields (n <= 8) that share the test/trial spaces of one scalar assembler (after
+ * gd_assemble_symbolic); its strategy is the multi-field system's: SubAssembledRows (the
+ * default of the reference's multi-field assemblers, MultiField.jl:473-479) or
+ * FullyAssembledRows.  The bilinear form is
  *   sum_ij int( stiff[i*n+j] grad(u_j).grad(v_i) + mass[i*n+j] u_j v_i ) kappa dOmega
  * (kappa per cell as in gd_coeffs, NULL = 1; f_nodal must be NULL), the linear form
  * sum_i int( src[i] v_i ) dOmega minus the Dirichlet lifting of every field with the
  * trial space's values.  Blocks with stiff = mass = 0 are not touched (no entries).
- * Replaces the assembly behind MultiFieldFESpace + SparseMatrixAssembler(X, Y,
- * FullyAssembledRows()) + AffineFEOperator (MultiField.jl:283-560). */
+ * Replaces the assembly behind MultiFieldFESpace + SparseMatrixAssembler(X, Y, strategy)
+ * + AffineFEOperator (MultiField.jl:283-560). */
 typedef struct gd_mfield gd_mfield;
 typedef struct gd_mfmat gd_mfmat;
 int gd_mfield_create(gd_asm* a, int nfields, gd_mfield** out);
@@ -407,10 +409,16 @@ int gd_mfmat_destroy(gd_mfmat* x);
 /* values and right-hand side from the latest gd_mfield_assemble (same touched blocks) */
 int gd_mfmat_refresh(gd_mfmat* x);
 int gd_mfmat_counts(const gd_mfmat* x, int64_t* nrows, int64_t* nnz);
+/* Rows of one part: the owned rows and, under SubAssembledRows, the touched ghost rows
+ * (explicit zeros, row field outer, local order); columns: the owned ones, then the ghost
+ * ones (FullyAssembledRows: each touched field's in local order, field by field;
+ * SubAssembledRows: first-appearance order -- the scalar ghost columns grouped by the cell
+ * that first meets them, field by field inside a group). */
 int gd_mfmat_sizes(const gd_mfmat* x, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
-                   int64_t* n_ghost_cols);
+                   int64_t* n_ghost_rows, int64_t* n_ghost_cols);
 int gd_mfmat_export(const gd_mfmat* x, int part, int64_t* rowptr, int32_t* colidx, double* vals,
-                    int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs);
+                    int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
+                    int32_t* ghost_col_owners, double* rhs);
 /* y = A x (mul!, BlockPartitionedArrays.jl:330-350 per block): x over the column group's
  * global numbering, y over the row group's. */
 int gd_mfmat_spmv(const gd_mfmat* x, const double* xin, double* y, int where);
@@ -425,6 +433,10 @@ int gd_dg_space_destroy(gd_dgspace* s);
 int gd_dg_num_free_dofs(const gd_dgspace* s, int64_t* n);
 int gd_dg_local_sizes(const gd_dgspace* s, int part, int64_t* nlocal, int64_t* nown, int64_t* first);
 int gd_dg_get_gids(const gd_dgspace* s, int part, int64_t* gid, int32_t* owner);
+/* The assembly strategy of the space's system (SparseMatrixAssembler(V, V, strategy),
+ * FESpaces.jl:819-862), before the first gd_dg_assemble; GD_SUB_ASSEMBLED_ROWS (the
+ * reference's default and this library's) or GD_FULLY_ASSEMBLED_ROWS. */
+int gd_dg_set_strategy(gd_dgspace* s, int strategy);
 /* The symmetric interior penalty form of the reference's DG Poisson test:
  *   a(u,v) = int grad(v).grad(u) + sum_Gd int((gamma/h) v u - v dn(u) - dn(v) u)
  *            + sum_Skeleton int((gamma/h) [[v n]].[[u n]] - [[v n]].{grad u} - {grad v}.[[u n]])
@@ -444,13 +456,20 @@ typedef struct gd_dg_form {
   const double* g_qp;
   int where;                       /* GD_HOST or GD_DEVICE for f_qp, ud_qp, g_qp */
 } gd_dg_form;
-/* Matrix and right-hand side of the owned rows (FullyAssembledRows: each owned row
- * summed by its part; columns: owned dofs, then the touched ghost dofs in local order). */
+/* Matrix and right-hand side (create_from_nz, Algebra.jl:537-646): every owned row summed
+ * completely.  FullyAssembledRows: owned rows only; columns: owned dofs, then the touched
+ * ghost dofs in local order.  SubAssembledRows: a part integrates the interior faces whose
+ * cell with the larger global id it owns (Geometry.jl:864-882); rows: owned dofs, then the
+ * touched ghost dofs (local order, explicit zeros); columns: owned dofs, then the ghost dofs
+ * in order of first appearance in the local and received triplets. */
 int gd_dg_assemble(gd_dgspace* s, const gd_dg_form* form);
 int gd_dg_matrix_sizes(const gd_dgspace* s, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
-                       int64_t* n_ghost_cols);
+                       int64_t* n_ghost_rows, int64_t* n_ghost_cols);
+/* One part: local CSR (owned rows, then ghost rows), the ghost parts of its row and column
+ * OwnAndGhostIndices, and the right-hand side over the rows (ghost rows 0). */
 int gd_dg_matrix_export(const gd_dgspace* s, int part, int64_t* rowptr, int32_t* colidx, double* vals,
-                        int64_t* ghost_col_gids, int32_t* ghost_col_owners, double* rhs);
+                        int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
+                        int32_t* ghost_col_owners, double* rhs);
 int gd_dg_spmv(const gd_dgspace* s, const double* x, double* y, int where);
 int gd_dg_solve(gd_dgspace* s, double rtol, int maxit, double* x, int where, gd_solve_stats* stats);
 /* sqrt(sum(int (u - uh)^2 dOmega)): u at the cells' Gauss points (layout of f_qp) */

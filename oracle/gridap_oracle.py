@@ -1146,14 +1146,18 @@ def multifield_gids(fe: FESpaceData, nfields: int):
     return out
 
 
-def assemble_multifield(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf):
-    """The FullyAssembledRows matrix and right-hand side of the multi-field form
+def assemble_multifield(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf, strategy="full"):
+    """The matrix and right-hand side of the multi-field form
     ``sum_ij int kappa (stiff[i][j] grad(u_j).grad(v_i) + mass[i][j] u_j v_i)``,
     ``sum_i int src[i] v_i`` (minus the Dirichlet lifting of every field) restricted to
     the row fields ``rf`` and column fields ``cf`` (a block of BlockMultiFieldStyle, or
     the ConsecutiveMultiFieldStyle matrix for rf = cf = all fields): one LocalMatrix per
     part, the local compression of FESpaces.jl:808-816 / Algebra.jl:549-579, 1245-1257 over
-    the multi-field index sets.  Blocks with stiff = mass = 0 add no entries."""
+    the multi-field index sets.  Blocks with stiff = mass = 0 add no entries.
+    ``strategy="sub"``: SubAssembledRows (the default of the reference's multi-field
+    assemblers, MultiField.jl:473-479), _multifield_sub_assembled."""
+    if strategy == "sub":
+        return _multifield_sub_assembled(pb, fe, stiff, mass, src, rf, cf)
     P, spaces, dofs = fe.P, fe.spaces, fe.dofs
     stiff = np.asarray(stiff, dtype=np.float64)
     mass = np.asarray(mass, dtype=np.float64)
@@ -1220,6 +1224,125 @@ def assemble_multifield(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf):
     return out
 
 
+def _multifield_sub_assembled(pb: Problem, fe: FESpaceData, stiff, mass, src, rf, cf):
+    """SubAssembledRows local parts of a multi-field system (Algebra.jl:593-646 over
+    the multi-field index sets):
+
+    * each part integrates its owned cells only (Triangulation(no_ghost));
+    * the COO follows Gridap's loops: cells in local order, and for a cell the block matrix
+      (rows: the row fields' cell dofs, columns: the column fields') walked column-major,
+      block columns outer and block rows inner over the touched blocks, each block
+      column-major (add_entries!); Dirichlet dofs skipped;
+    * triplets of rows owned by another part are copied to it and zeroed (not removed),
+      the owner appends them, senders in ascending order (Algebra.jl:1048-1131);
+    * rows: owned multi-field dofs, then the touched ghost dofs by local id (field-major:
+      group position * free dofs + scalar local id); columns: owned, then the ghost dofs in
+      order of first appearance (Algebra.jl:1210-1238); duplicates summed;
+    * b: owned rows complete (the vector assemble!), ghost rows zero."""
+    P, spaces, dofs = fe.P, fe.spaces, fe.dofs
+    stiff = np.asarray(stiff, dtype=np.float64)
+    mass = np.asarray(mass, dtype=np.float64)
+    nf = stiff.shape[0]
+    Kh, Mh, Fh = reference_matrices(pb.dim, pb.order, pb.h, pb.degree)
+    T = [[stiff[i, j] * Kh + mass[i, j] * Mh for j in range(nf)] for i in range(nf)]
+    touched = (stiff != 0.0) | (mass != 0.0)
+    S = [sum(T[i][j] for j in range(nf)) for i in range(nf)]
+    rg = multifield_gids(fe, len(rf))
+    cg = multifield_gids(fe, len(cf))
+    lnodes = np.array(cell_local_nodes(pb.dim, pb.order))
+    # global right-hand side per row-group gid (owned rows complete)
+    nrg = sum(len(d.own_to_global) for d in rg)
+    bglob = np.zeros(nrg)
+    coo = []
+    for p in range(P.nparts):
+        sp, di = spaces[p], dofs[p]
+        nfree = sp.nfree
+        owners = [P.cell_owner(P.cell_coords(int(g))) for g in sp.cells]
+        I, J, V = [], [], []
+        for ic, g in enumerate(sp.cells):
+            if owners[ic] != p:
+                continue
+            kap = pb.kappa[g]
+            cd = sp.cell_dofs[ic]
+            nd = len(cd)
+            ci = np.array(P_cell_coords(pb.n, int(g)))
+            X = pb.order * ci[None, :] + lnodes
+            for jj, j in enumerate(cf):              # block columns outer
+                for ii, i in enumerate(rf):          # block rows inner
+                    if not touched[i, j]:
+                        continue
+                    Ke = kap * T[i][j]
+                    for c in range(nd):              # column-major inside the block
+                        gj = cd[c]
+                        if gj < 0:
+                            continue
+                        for a in range(nd):
+                            gi = cd[a]
+                            if gi < 0:
+                                continue
+                            I.append(ii * nfree + gi); J.append(jj * nfree + gj); V.append(Ke[a, c])
+            for ii, i in enumerate(rf):
+                be = src[i] * Fh
+                if pb.u_dir is not None:
+                    ud = np.where(cd < 0, pb.u_dir[pb.node_lin(X)], 0.0)
+                    be = be - kap * (S[i] @ ud)
+                for a in range(nd):
+                    gi = cd[a]
+                    if gi >= 0:
+                        bglob[rg[p].ldof_to_gdof[ii * nfree + gi]] += be[a]
+        I = np.array(I, dtype=np.int64); J = np.array(J, dtype=np.int64)
+        coo.append((rg[p].ldof_to_gdof[I] if len(I) else I, cg[p].ldof_to_gdof[J] if len(J) else J,
+                    np.array(V, dtype=np.float64)))
+    row_owner = {}
+    for p in range(P.nparts):
+        for gg, o in zip(rg[p].ldof_to_gdof, rg[p].ldof_to_owner):
+            row_owner[int(gg)] = int(o)
+    col_owner = {}
+    for p in range(P.nparts):
+        for gg, o in zip(cg[p].ldof_to_gdof, cg[p].ldof_to_owner):
+            col_owner[int(gg)] = int(o)
+    sent, kept = {}, []
+    for p in range(P.nparts):
+        Ig, Jg, V = coo[p]
+        Vk = V.copy()
+        for t in range(len(Ig)):
+            q = row_owner[int(Ig[t])]
+            if q != p:
+                sent.setdefault((p, q), []).append((int(Ig[t]), int(Jg[t]), float(V[t])))
+                Vk[t] = 0.0
+        kept.append((Ig, Jg, Vk))
+    out = []
+    for p in range(P.nparts):
+        Ig, Jg, V = kept[p]
+        trip = list(zip(Ig.tolist(), Jg.tolist(), V.tolist()))
+        for q in range(P.nparts):
+            trip += sent.get((q, p), [])
+        rdi, cdi = rg[p], cg[p]
+        rown, cown = rdi.own_to_global, cdi.own_to_global
+        rlid = {int(gg): l for l, gg in enumerate(rdi.ldof_to_gdof)}
+        ghost_rows = sorted({rlid[r] for (r, c, v) in trip if row_owner[r] != p})
+        grow_g = np.array([int(rdi.ldof_to_gdof[l]) for l in ghost_rows], dtype=np.int64)
+        gcol_g, seen = [], set()
+        for (r, c, v) in trip:
+            if col_owner[c] != p and c not in seen:
+                seen.add(c); gcol_g.append(c)
+        gcol_g = np.array(gcol_g, dtype=np.int64)
+        rmap = {int(x): k for k, x in enumerate(rown)}
+        rmap.update({int(x): len(rown) + k for k, x in enumerate(grow_g)})
+        cmap = {int(x): k for k, x in enumerate(cown)}
+        cmap.update({int(x): len(cown) + k for k, x in enumerate(gcol_g)})
+        Il = np.array([rmap[r] for (r, c, v) in trip], dtype=np.int64)
+        Jl = np.array([cmap[c] for (r, c, v) in trip], dtype=np.int64)
+        Vl = np.array([v for (r, c, v) in trip], dtype=np.float64)
+        nrows, ncols = len(rown) + len(grow_g), len(cown) + len(gcol_g)
+        rowptr, colidx, vals = _compress(nrows, Il, Jl, Vl, ncols)
+        own = lambda gs, m: np.array([m[int(x)] for x in gs], dtype=np.int32)
+        out.append(LocalMatrix(p, nrows, ncols, rowptr, colidx, vals, rown, grow_g, own(grow_g, row_owner),
+                               cown, gcol_g, own(gcol_g, col_owner),
+                               np.concatenate([bglob[rown], np.zeros(len(grow_g))])))
+    return out
+
+
 # --------------------------------------------------------------------------------------
 # Discontinuous Galerkin (test/PoissonTests.jl:47-77)
 # --------------------------------------------------------------------------------------
@@ -1243,7 +1366,8 @@ def _shape_ref(dim, k, lnodes, xi):
     return phi, grad
 
 
-def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neumann_sides, u_dir, g_neu):
+def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neumann_sides, u_dir, g_neu,
+              strategy="full"):
     """Symmetric interior penalty system of test/PoissonTests.jl:47-77 on a Cartesian
     model, assembled the way a finite-element code does it: cell loops for the volume
     terms, one loop over the interior faces (each face once, its 2x2-block matrix with
@@ -1287,6 +1411,7 @@ def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neuman
 
     rows, cols, vals = [], [], []
     b = np.zeros(ndofs)
+    terms = {"cell": {}, "bnd": {}, "facet": {}}   # per owned-cell / boundary-face / interior-face matrices
 
     def add(c1, c2, M):
         for a in range(nn):
@@ -1304,6 +1429,7 @@ def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neuman
             Ke += w * gr @ gr.T
             be += w * f * phi
         add(c, c, Ke)
+        terms["cell"][c] = Ke
         b[gid0[c]:gid0[c] + nn] += be
     pen = gamma / hpen
     for c in range(ncells):
@@ -1338,6 +1464,7 @@ def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neuman
                         A += w * (pen * np.outer(jv, jv) - np.outer(jv, mg) - np.outer(mg, jv))
                     add(c, c, A[:nn, :nn]); add(c, cn, A[:nn, nn:])
                     add(cn, c, A[nn:, :nn]); add(cn, cn, A[nn:, nn:])
+                    terms["facet"][(c, cn)] = A     # rows/cols [lower cell dofs, upper cell dofs]
                     continue
                 s = 2 * d + side
                 if not (dirichlet_sides[s] or neumann_sides[s]):
@@ -1357,7 +1484,10 @@ def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neuman
                         be += w * phi * g_neu(*x, *normal)
                 if dirichlet_sides[s]:
                     add(c, c, A)
+                    terms["bnd"][(c, s)] = A
                 b[gid0[c]:gid0[c] + nn] += be
+    if strategy == "sub":
+        return _dg_sub_assembled(P, n, nn, first, ncell_own, gid0, terms, b), gid0, ndofs
     I = np.array(rows, dtype=np.int64); J = np.array(cols, dtype=np.int64); V = np.array(vals)
     # FullyAssembledRows local parts
     out = []
@@ -1383,6 +1513,130 @@ def dg_system(np_, n, domain, k, degree, gamma, hpen, f, dirichlet_sides, neuman
                                np.zeros(0, dtype=np.int64), np.zeros(0, dtype=np.int32),
                                own_g, gg, gown, b[own0:own1].copy()))
     return out, gid0, ndofs
+
+
+def _dg_facet_order(P, p, n):
+    """Interior faces of part p's local model in Gridap's face numbering: faces are
+    numbered as the local cells (local-box order) meet them, each cell's faces in the
+    n-cube's order (2D: y-, y+, x-, x+; 3D: z-, z+, y-, y+, x-, x+), so an interior face
+    gets its number at its lower cell, as that cell's upper face in direction d.
+    Returns [(lower cell, upper cell)] global ids, in that order."""
+    dim = len(n)
+    lcells = P.local_cells(p)
+    in_local = set(int(c) for c in lcells)
+    out = []
+    for c in lcells:
+        ci = P.cell_coords(int(c))
+        for d in reversed(range(dim)):           # upper faces in the order z+, y+, x+
+            nb = list(ci); nb[d] += 1
+            if nb[d] < n[d]:
+                cn = P.cell_gid(tuple(nb))
+                if cn in in_local:
+                    out.append((int(c), int(cn)))
+    return out
+
+
+def _dg_sub_assembled(P, n, nn, first, ncell_own, gid0, terms, b):
+    """SubAssembledRows local parts of the SIPG system (Algebra.jl:593-646 over the local
+    loops of Gridap's numeric assembly):
+
+    * part p integrates its owned cells, the boundary faces of its owned cells and the
+      interior faces it owns: a face belongs to the part owning the adjacent cell with the
+      larger global id (Geometry.jl:864-882, _find_owned_skeleton_facets);
+    * the local COO follows Gridap's loops: terms in the order of the form (cells,
+      Dirichlet faces, skeleton), faces in the local face numbering (_dg_facet_order); an
+      interior face's 2x2 block matrix has plus = the cell with the lower local id, and
+      add_entries! walks blocks and entries column-major;
+    * triplets of rows owned by another part are copied to it and zeroed (not removed)
+      locally (Algebra.jl:1048-1131); the owner appends them, senders in ascending order;
+    * rows: owned dofs, then the touched ghost dofs sorted by local id; columns: owned
+      dofs, then the ghost dofs in order of first appearance in the (local + received)
+      COO (Algebra.jl:1210-1238); duplicates summed (sparse()).
+    b: owned rows complete, ghost rows zero (assemble!)."""
+    cell_owner = {}
+    for c in range(len(gid0)):
+        cell_owner[c] = P.cell_owner(P.cell_coords(c))
+
+    def blocks_colmajor(rows_cells, cols_cells, M):
+        """(row gid, col gid, value) of a block matrix over the cells' dofs, column-major."""
+        R = np.concatenate([np.arange(gid0[c], gid0[c] + nn) for c in rows_cells])
+        Cc = np.concatenate([np.arange(gid0[c], gid0[c] + nn) for c in cols_cells])
+        out = []
+        nb = len(cols_cells)
+        for jb in range(nb):                    # block columns
+            for ib in range(len(rows_cells)):   # block rows
+                for j in range(nn):
+                    for i in range(nn):
+                        out.append((int(R[ib * nn + i]), int(Cc[jb * nn + j]),
+                                    float(M[ib * nn + i, jb * nn + j])))
+        return out
+
+    local_coo = []
+    for p in range(P.nparts):
+        coo = []
+        lcells = [int(c) for c in P.local_cells(p)]
+        for c in lcells:                                           # Omega (no_ghost)
+            if cell_owner[c] == p and c in terms["cell"]:
+                coo += blocks_colmajor([c], [c], terms["cell"][c])
+        lpos = {c: i for i, c in enumerate(lcells)}
+        mine = [(key, A) for key, A in terms["bnd"].items() if cell_owner[key[0]] == p]
+        for (c, sd), A in sorted(mine, key=lambda t: (lpos[t[0][0]], t[0][1])):   # Gamma_d (no_ghost)
+            coo += blocks_colmajor([c], [c], A)
+        for (cl, cu) in _dg_facet_order(P, p, n):                  # Lambda (owned faces)
+            if cell_owner[max(cl, cu)] != p:
+                continue
+            A = terms["facet"][(cl, cu)]                           # plus = lower local id = cl
+            coo += blocks_colmajor([cl, cu], [cl, cu], A)
+        local_coo.append(coo)
+    row_owner = lambda g: int(np.searchsorted(first, g, side="right") - 1)
+    sent = {}
+    kept = []
+    for p in range(P.nparts):
+        k_ = []
+        for (r, c, v) in local_coo[p]:
+            q = row_owner(r)
+            if q != p:
+                sent.setdefault((p, q), []).append((r, c, v))
+                k_.append((r, c, 0.0))
+            else:
+                k_.append((r, c, v))
+        kept.append(k_)
+    out = []
+    for p in range(P.nparts):
+        coo = list(kept[p])
+        for q in range(P.nparts):
+            coo += sent.get((q, p), [])
+        own0, own1 = int(first[p]), int(first[p] + nn * ncell_own[p])
+        lcells = [int(c) for c in P.local_cells(p)]
+        lid_of = {}
+        for i, cg in enumerate(lcells):
+            for a in range(nn):
+                lid_of[int(gid0[cg]) + a] = i * nn + a
+        ghost_rows = sorted({lid_of[r] for (r, c, v) in coo if not (own0 <= r < own1)})
+        lid_gid = {l: g for g, l in lid_of.items()}
+        grow_g = np.array([lid_gid[l] for l in ghost_rows], dtype=np.int64)
+        gcol_g = []
+        seen = set()
+        for (r, c, v) in coo:
+            if not (own0 <= c < own1) and c not in seen:
+                seen.add(c); gcol_g.append(c)
+        gcol_g = np.array(gcol_g, dtype=np.int64)
+        nown = own1 - own0
+        rmap = {g: i for i, g in enumerate(range(own0, own1))}
+        rmap.update({int(g): nown + i for i, g in enumerate(grow_g)})
+        cmap = {g: i for i, g in enumerate(range(own0, own1))}
+        cmap.update({int(g): nown + i for i, g in enumerate(gcol_g)})
+        I = np.array([rmap[r] for (r, c, v) in coo], dtype=np.int64)
+        J = np.array([cmap[c] for (r, c, v) in coo], dtype=np.int64)
+        V = np.array([v for (r, c, v) in coo])
+        nrows, ncols = nown + len(grow_g), nown + len(gcol_g)
+        rowptr, colidx, vv = _compress(nrows, I, J, V, ncols)
+        own_g = np.arange(own0, own1, dtype=np.int64)
+        gown = lambda gs: np.array([row_owner(int(g)) for g in gs], dtype=np.int32)
+        out.append(LocalMatrix(p, nrows, ncols, rowptr, colidx, vv, own_g, grow_g, gown(grow_g),
+                               own_g, gcol_g, gown(gcol_g),
+                               np.concatenate([b[own0:own1], np.zeros(len(grow_g))])))
+    return out
 
 
 def dg_l2_error(np_, n, domain, k, degree, x, gid0, u):

@@ -5,7 +5,9 @@
   h = 2, Nitsche Dirichlet data on the bottom/left sides and g = n.grad(u) on the
   top/right sides reproduces u = (x+y)^2: L2 error < 1e-9, through the Python mirror.
 - The assembled local parts against the oracle's restatement (tests/test_oracle_dg.py
-  pins it to the same known answer): pattern, ghost column gids and owners bit-exact;
+  pins it to the same known answer), for both strategies: pattern, ghost row and ghost
+  column gids and owners bit-exact (SubAssembledRows: the faces a part owns, the zeroed
+  ghost rows and the first-appearance column order of the oracle's loop restatement);
   values |gpu - oracle| <= 1e-12 * max |oracle| in the row; right-hand side <= 1e-12.
 - The DG dof numbering (gids and owners of every part's local dofs) bit-exact.
 """
@@ -29,7 +31,7 @@ def backend():
     be.close()
 
 
-def gpu_dg(be, parts, n, domain, k, gamma, hpen, f, dsides, nsides, u, g):
+def gpu_dg(be, parts, n, domain, k, gamma, hpen, f, dsides, nsides, u, g, strategy=None):
     import gridap_gb300 as G
     ranks = be.distribute(range(int(np.prod(parts))))
     model = G.CartesianDiscreteModel(ranks, parts, domain, n)
@@ -43,7 +45,10 @@ def gpu_dg(be, parts, n, domain, k, gamma, hpen, f, dsides, nsides, u, g):
         if any(nsides) else None
     a = G.integral_sipg(gamma, hpen, dO, dGd, dL)
     l = G.integral_sipg_source(f, u, g, gamma, hpen, dO, dGn, dGd)
-    return model, V, G.AffineFEOperator(a, l, V, V), dO
+    assem = None
+    if strategy is not None:
+        assem = G.SparseMatrixAssembler(V, V, G.SubAssembledRows() if strategy == "sub" else G.FullyAssembledRows())
+    return model, V, G.AffineFEOperator(a, l, V, V, assem), dO
 
 
 @pytest.mark.parametrize("parts", [(1, 1), (2, 2), (2, 1), (1, 2)])
@@ -73,8 +78,9 @@ def case_id(c):
     return f"{len(c['n'])}d_q{c['k']}_{'x'.join(map(str, c['n']))}_p{''.join(map(str, c['parts']))}"
 
 
+@pytest.mark.parametrize("strategy", ["sub", "full"])
 @pytest.mark.parametrize("case", CASES, ids=case_id)
-def test_dg_parts_match_oracle(backend, case):
+def test_dg_parts_match_oracle(backend, case, strategy):
     dim = len(case["n"])
     if dim == 2:
         u = lambda x, y: np.sin(x) + x * y
@@ -84,14 +90,17 @@ def test_dg_parts_match_oracle(backend, case):
         g = lambda x, y, z, nx, ny, nz: 1.0 + x * ny - z * nz
     gamma, hpen, f = 7.5, 0.8, 1.25
     model, V, op, _ = gpu_dg(backend, case["parts"], case["n"], case["domain"], case["k"], gamma, hpen, f,
-                             case["dsides"], case["nsides"], u, g)
+                             case["dsides"], case["nsides"], u, g, strategy)
     ref, gid0, ndofs = go.dg_system(case["parts"], case["n"], case["domain"], case["k"], 2 * case["k"], gamma, hpen,
-                                    f, case["dsides"], case["nsides"], u, g)
+                                    f, case["dsides"], case["nsides"], u, g, strategy=strategy)
     assert V.num_free_dofs() == ndofs
     A = op.matrix
-    for p, (M, (rp, ci, vv), cols, b) in enumerate(zip(ref, A.csr_parts(), A.col_partition, A.rhs_parts())):
+    for p, (M, (rp, ci, vv), rows, cols, b) in enumerate(zip(ref, A.csr_parts(), A.row_partition, A.col_partition,
+                                                              A.rhs_parts())):
         assert np.array_equal(rp, M.rowptr), f"rowptr part {p}"
         assert np.array_equal(ci, M.colidx), f"colidx part {p}"
+        assert np.array_equal(rows.ghost_to_global, M.row_ghost_gids), f"ghost rows part {p}"
+        assert np.array_equal(rows.ghost_to_owner, M.row_ghost_owner)
         assert np.array_equal(cols.ghost_to_global, M.col_ghost_gids), f"ghost cols part {p}"
         assert np.array_equal(cols.ghost_to_owner, M.col_ghost_owner)
         assert row_scaled_error(vv, M.vals, M.rowptr) <= VAL_TOL
@@ -108,6 +117,6 @@ def test_dg_parts_match_oracle(backend, case):
     y = A.mul(x)
     for M in ref:
         gcols = np.concatenate([M.col_own_gids, M.col_ghost_gids])
-        for r in range(M.nrows):
+        for r in range(len(M.row_own_gids)):
             s = sum(M.vals[e] * x[gcols[M.colidx[e]]] for e in range(M.rowptr[r], M.rowptr[r + 1]))
             assert abs(y[M.row_own_gids[r]] - s) <= 1e-12 * max(1.0, abs(s))

@@ -2,10 +2,12 @@
 test/BlockSparseMatrixAssemblersTests.jl:98-120: 8x8 Q1 on the unit square, Dirichlet
 on the boundary with u = x + y, biform2/liform2 and biform3/liform3, styles
 ConsecutiveMultiFieldStyle, BlockMultiFieldStyle() and BlockMultiFieldStyle(2, (1, n-1)),
-FullyAssembledRows, parts (2,2), (2,1), (1,2).
+FullyAssembledRows (the strategy the test passes) and SubAssembledRows (the default of its
+AffineFEOperator(biform, liform, X, Y) calls), parts (2,2), (2,1), (1,2).
 
-Bit-exact: row/column index sets (local CSR pattern, ghost column gids and owners) and
-the multi-field gids.  FP64 values: |gpu - oracle| <= 1e-12 * (max |oracle| in the row);
+Bit-exact: row/column index sets (local CSR pattern, ghost row and ghost column gids and
+owners; under SubAssembledRows the zeroed ghost rows and first-appearance columns of the
+oracle's loop restatement) and the multi-field gids.  FP64 values: |gpu - oracle| <= 1e-12 * (max |oracle| in the row);
 right-hand sides <= 1e-12 * max |b|.  Block vs monolithic (the reference's own check):
 mul! with all-ones inputs and the right-hand sides agree field by field to 1e-10.
 """
@@ -36,7 +38,7 @@ def styles(nf):
             "block_1_rest": G.BlockMultiFieldStyle(2, (1, nf - 1))}
 
 
-def gpu_system(backend, parts, nf, style, stiff=None, mass=None, src=None):
+def gpu_system(backend, parts, nf, style, stiff=None, mass=None, src=None, strategy="full"):
     import gridap_gb300 as G
     ranks = backend.distribute(range(int(np.prod(parts))))
     model = G.CartesianDiscreteModel(ranks, parts, (0, 1, 0, 1), (8, 8))
@@ -48,7 +50,10 @@ def gpu_system(backend, parts, nf, style, stiff=None, mass=None, src=None):
     st, ms, sr = FORMS[nf]
     a = G.integral_multifield(st if stiff is None else stiff, ms if mass is None else mass, dO)
     l = G.integral_multifield_source(sr if src is None else src, dO)
-    assem = G.SparseMatrixAssembler(X, Y, G.FullyAssembledRows())
+    if strategy == "default":   # AffineFEOperator(biform, liform, X, Y): the default assembler
+        op = G.AffineFEOperator(a, l, X, Y)
+        return model, V, op.assem, op
+    assem = G.SparseMatrixAssembler(X, Y, G.FullyAssembledRows() if strategy == "full" else G.SubAssembledRows())
     op = G.AffineFEOperator(a, l, X, Y, assem)
     return model, V, assem, op
 
@@ -59,9 +64,12 @@ def oracle(parts):
 
 
 def check_matrix(mat, ref):
-    for p, (M, (rp, ci, vv), cols, b) in enumerate(zip(ref, mat.csr_parts(), mat.col_partition, mat.rhs_parts())):
+    for p, (M, (rp, ci, vv), rows, cols, b) in enumerate(zip(ref, mat.csr_parts(), mat.row_partition,
+                                                              mat.col_partition, mat.rhs_parts())):
         assert np.array_equal(rp, M.rowptr), f"rowptr part {p}"
         assert np.array_equal(ci, M.colidx), f"colidx part {p}"
+        assert np.array_equal(rows.ghost_to_global, M.row_ghost_gids), f"ghost rows part {p}"
+        assert np.array_equal(rows.ghost_to_owner, M.row_ghost_owner)
         assert np.array_equal(cols.own_to_global, M.col_own_gids)
         assert np.array_equal(cols.ghost_to_global, M.col_ghost_gids), f"ghost cols part {p}"
         assert np.array_equal(cols.ghost_to_owner, M.col_ghost_owner)
@@ -70,37 +78,43 @@ def check_matrix(mat, ref):
         assert np.abs(b - M.b).max() <= VAL_TOL * scale
 
 
+@pytest.mark.parametrize("strategy", ["full", "sub", "default"])
 @pytest.mark.parametrize("parts", PARTS)
 @pytest.mark.parametrize("nf", [2, 3])
 @pytest.mark.parametrize("style", ["consecutive", "block", "block_1_rest"])
-def test_multifield_matches_oracle(backend, parts, nf, style):
+def test_multifield_matches_oracle(backend, parts, nf, style, strategy):
     import gridap_gb300 as G
-    _, V, assem, op = gpu_system(backend, parts, nf, styles(nf)[style])
+    _, V, assem, op = gpu_system(backend, parts, nf, styles(nf)[style], strategy=strategy)
     pb, fe = oracle(parts)
     st, ms, sr = FORMS[nf]
     groups = op.assem.Y.groups()
+    strat = "full" if strategy == "full" else "sub"
     if style == "consecutive":
         assert isinstance(op.matrix, G.multifield.MultiFieldMatrix)
-        check_matrix(op.matrix, go.assemble_multifield(pb, fe, st, ms, sr, groups[0], groups[0]))
+        check_matrix(op.matrix, go.assemble_multifield(pb, fe, st, ms, sr, groups[0], groups[0], strategy=strat))
     else:
         assert isinstance(op.matrix, G.BlockPMatrix)
         for I, gI in enumerate(groups):
             for J, gJ in enumerate(groups):
-                check_matrix(op.matrix.blocks[I][J], go.assemble_multifield(pb, fe, st, ms, sr, gI, gJ))
+                check_matrix(op.matrix.blocks[I][J],
+                             go.assemble_multifield(pb, fe, st, ms, sr, gI, gJ, strategy=strat))
 
 
+@pytest.mark.parametrize("strategy", ["full", "default"])
 @pytest.mark.parametrize("parts", PARTS)
 @pytest.mark.parametrize("nf", [2, 3])
-def test_block_equals_monolithic(backend, parts, nf):
-    """is_same_matrix / is_same_vector of test/BlockSparseMatrixAssemblersTests.jl:17-39."""
+def test_block_equals_monolithic(backend, parts, nf, strategy):
+    """is_same_matrix / is_same_vector of test/BlockSparseMatrixAssemblersTests.jl:17-39
+    (with its explicit FullyAssembledRows assemblers and its default-assembler
+    AffineFEOperator calls)."""
     import gridap_gb300 as G
-    _, V, _, mono = gpu_system(backend, parts, nf, G.ConsecutiveMultiFieldStyle())
+    _, V, _, mono = gpu_system(backend, parts, nf, G.ConsecutiveMultiFieldStyle(), strategy=strategy)
     Y = mono.assem.Y
     n = V.num_free_dofs()
     y_mono = mono.matrix.mul(np.ones(nf * n))
     b_mono = mono.vector.global_values()
     for style in ("block", "block_1_rest"):
-        _, _, _, blk = gpu_system(backend, parts, nf, styles(nf)[style])
+        _, _, _, blk = gpu_system(backend, parts, nf, styles(nf)[style], strategy=strategy)
         Yb = blk.assem.Y
         groups = Yb.groups()
         ys = blk.matrix.mul([np.ones(len(g) * n) for g in groups])
@@ -143,10 +157,8 @@ def test_reassembly_refreshes_values(backend):
         assem.numeric(G.integral_multifield([[1, 1], [0, 0]], [[0, 0], [1, 1]], dO), None)
 
 
-def test_untouched_block_is_empty_and_sub_assembled_is_rejected(backend):
+@pytest.mark.parametrize("strategy", ["full", "sub"])
+def test_untouched_block_is_empty(backend, strategy):
     import gridap_gb300 as G
-    _, V, _, op = gpu_system(backend, (2, 2), 2, G.BlockMultiFieldStyle())
+    _, V, _, op = gpu_system(backend, (2, 2), 2, G.BlockMultiFieldStyle(), strategy=strategy)
     assert all(len(vv) == 0 for _, _, vv in op.matrix.blocks[0][1].csr_parts())   # u2 never meets v1
-    Y = G.MultiFieldFESpace([V, V])
-    with pytest.raises(NotImplementedError):
-        G.SparseMatrixAssembler(Y, Y, G.SubAssembledRows())

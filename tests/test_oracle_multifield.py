@@ -123,3 +123,45 @@ def test_multifield_gids(parts):
         if nf == 1:
             for p in range(len(g)):
                 assert np.array_equal(g[p].ldof_to_gdof, fe.dofs[p].ldof_to_gdof)
+
+
+@pytest.mark.parametrize("parts", [(2, 2), (2, 1), (1, 2)])
+@pytest.mark.parametrize("nf", [2, 3])
+def test_sub_assembled_rows_multifield(parts, nf):
+    """SubAssembledRows (the reference's default for multi-field assemblers): the owned rows
+    give the FullyAssembledRows operator, ghost rows are explicit zeros over the row fields'
+    copies of the scalar ghost rows, and each field's ghost columns keep the scalar
+    SubAssembledRows first-appearance order."""
+    pb = reference_problem(parts)
+    fe = go.build_fespace(pb)
+    stiff, mass, src = FORMS[nf]
+    allf = list(range(nf))
+    fa = go.assemble_multifield(pb, fe, stiff, mass, src, allf, allf, strategy="full")
+    sa = go.assemble_multifield(pb, fe, stiff, mass, src, allf, allf, strategy="sub")
+    x = np.random.default_rng(5).normal(size=nf * fe.dofs[0].ngdofs)
+    y_fa, y_sa = global_mul(fa, x), global_mul_owned(sa, x)
+    assert all(abs(y_fa[k] - y_sa[k]) <= 1e-12 * max(1.0, abs(y_fa[k])) for k in y_fa)
+    assert rhs_map(fa) == pytest.approx(rhs_map_owned(sa), rel=1e-13, abs=1e-13)
+    scalar = go.assemble(pb, fe, "sub")
+    for p, (M, Sc) in enumerate(zip(sa, scalar)):
+        nown = len(M.row_own_gids)
+        assert np.all(M.vals[M.rowptr[nown]:] == 0.0) and np.all(M.b[nown:] == 0.0)
+        want_rows = np.concatenate([[group_gid(fe, nf, jj, g) for g in Sc.row_ghost_gids] for jj in range(nf)])
+        assert np.array_equal(M.row_ghost_gids, want_rows.astype(np.int64))
+        for jj in range(nf):
+            mine = [g for g in M.col_ghost_gids if any(group_gid(fe, nf, jj, s) == g for s in Sc.col_ghost_gids)]
+            want = [group_gid(fe, nf, jj, s) for s in Sc.col_ghost_gids]
+            assert mine == want
+
+
+def global_mul_owned(mats, x):
+    y = {}
+    for M in mats:
+        cols = np.concatenate([M.col_own_gids, M.col_ghost_gids])
+        for r in range(len(M.row_own_gids)):
+            y[int(M.row_own_gids[r])] = sum(M.vals[e] * x[cols[M.colidx[e]]] for e in range(M.rowptr[r], M.rowptr[r + 1]))
+    return y
+
+
+def rhs_map_owned(mats):
+    return {int(g): float(b) for M in mats for g, b in zip(M.row_own_gids, M.b[:len(M.row_own_gids)])}
