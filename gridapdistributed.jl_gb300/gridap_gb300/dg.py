@@ -214,7 +214,9 @@ class DGVector:
         return self.matrix.rhs_parts()
 
     def global_values(self):
-        return np.concatenate(self.matrix.rhs_parts())
+        """The owned entries of every part in gid order (ghost rows left out)."""
+        rows = self.matrix.row_partition
+        return np.concatenate([b[:len(r.own_to_global)] for b, r in zip(self.matrix.rhs_parts(), rows)])
 
 
 def assemble_dg(V: DistributedDGFESpace, a: SIPGForm, l: SIPGSource, strategy=None):
