@@ -791,18 +791,15 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   return GD_OK;
 }
 
-// ---- 2D Q_k (k = 2, 3): values and right-hand side in one kernel ---------------------------
-// A 2D row has at most (2k+1)^2 entries (25 for Q2), so TPR = 4 threads form a row: each
-// decodes the row node's (at most 4) cells, then walks every TPR-th of the row's CSR
-// entries (the stencil code of each entry gives the offset and the cells that hold both
-// nodes through the shared-memory entry table, as in qk_matrix_rows); the first thread
-// of the row also forms the right-hand side (source term and Dirichlet lifting with the
-// same cells).  Consecutive thread groups own consecutive rows, so a warp's values are one
-// contiguous range of the CSR value array.  The coefficient check runs on the integer
-// pipe (bit tests): GB300's FP64 pipe is the scarce unit here.
-constexpr int kR2dThreads = 128, kR2dTPR = 4;
+// ---- 2D Q_k (k = 2, 3): values and right-hand side in one kernel, one thread per row ----
+// A 2D row has at most (2k+1)^2 entries (25 for Q2), so one thread forms its whole row:
+// it decodes its node's (at most 4) cells once, then walks its CSR entries (the stencil
+// code of each entry gives the offset and the cells that hold both nodes through the
+// shared-memory entry table, as in qk_matrix_rows) and finally the right-hand side (source
+// term and Dirichlet lifting with the same cells).  Consecutive threads own consecutive
+// rows, so a warp's values are one contiguous range of the CSR value array.
 template <int K, typename CodeT, bool FN, bool UD>
-__global__ void __launch_bounds__(kR2dThreads)
+__global__ void __launch_bounds__(128)
 k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
                const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
                const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
@@ -810,91 +807,92 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
                double* __restrict__ rhs, int32_t* __restrict__ bad) {
   using L = Lat<2, K>;
   constexpr int NN = L::NN;
-  constexpr int RPB = kR2dThreads / kR2dTPR;   // rows per block
   __shared__ double s_K[NN * NN];
   __shared__ double s_M[FN ? NN * NN : 1];
   __shared__ double s_F[NN];
   __shared__ uint16_t s_tab[EntryTab<2, K>::SIZE];
-  __shared__ double s_kap[4][RPB];   // per row: coefficient and local index of its 4 slots
-  __shared__ int s_lx[4][RPB];       // (shared, not local, memory: they are indexed at run time)
+  __shared__ double s_kap[4][128];   // per thread: coefficient and local index of its 4 slots
+  __shared__ int s_lx[4][128];       // (shared, not local, memory: they are indexed at run time)
   for (int i = threadIdx.x; i < NN * NN; i += blockDim.x) {
     s_K[i] = Khat[i];
     if (FN) s_M[i] = Mhat[i];
   }
   for (int i = threadIdx.x; i < NN; i += blockDim.x) s_F[i] = Fhat[i];
   build_entry_tab<2, K>(s_tab);
-  const int t = threadIdx.x / kR2dTPR, sub = threadIdx.x % kR2dTPR;
-  const int64_t r = (int64_t)blockIdx.x * RPB + t;
-  const bool live = r < nrows_own;
+  __syncthreads();
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= nrows_own) return;
   const uint32_t N0 = (uint32_t)g.N[0];
-  const uint32_t lin = live ? (uint32_t)row_node[r] : 0u;
+  const uint32_t lin = (uint32_t)row_node[r];
   const int X0 = (int)(lin % N0), X1 = (int)(lin / N0);
   const int rm0 = X0 % K, rm1 = X1 % K;
   const int onb = (rm0 == 0 ? 1 : 0) | (rm1 == 0 ? 2 : 0);
+  const int t = threadIdx.x;
   uint32_t vmask = 0;
   int nbad = 0;
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     const int s0 = a & 1, s1 = (a >> 1) & 1;
     const int c0 = s0 ? X0 / K : X0 / K - 1, c1 = s1 ? X1 / K : X1 / K - 1;
-    const bool ok = live && (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
+    const bool ok = (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
                     c1 < (int)g.n[1];
+    const double k = ok ? __ldg(kappa + (int64_t)c1 * g.n[0] + c0) : 0.0;
+    if (ok) {   // finite and positive, tested on the bits (integer pipe, not GB300's scarce FP64 one)
+      const unsigned long long bits = (unsigned long long)__double_as_longlong(k);
+      nbad += (bits >> 63) != 0ull || ((bits >> 52) & 0x7FFull) == 0x7FFull || bits == 0ull;
+    }
+    s_kap[a][t] = k;
+    s_lx[a][t] = (s0 ? rm0 : K) + L::KP1 * (s1 ? rm1 : K);
     vmask |= (uint32_t)ok << a;
-    if (sub == a) {   // thread `a` of the row loads slot a
-      const double k = ok ? __ldg(kappa + (int64_t)c1 * g.n[0] + c0) : 0.0;
-      if (ok) {
-        const unsigned long long bits = (unsigned long long)__double_as_longlong(k);
-        nbad += (bits >> 63) != 0ull || ((bits >> 52) & 0x7FFull) == 0x7FFull || bits == 0ull;
-      }
-      s_kap[a][t] = k;
-      s_lx[a][t] = (s0 ? rm0 : K) + L::KP1 * (s1 ? rm1 : K);
-    }
   }
-  __syncthreads();
-  if (live) {
-    const uint16_t* et = s_tab + onb * EntryTab<2, K>::E;
-    const int64_t e0 = rowptr[r];
-    const int len = (int)(rowptr[r + 1] - e0);
-    for (int i = sub; i < len; i += kR2dTPR) {
-      const int info = et[(int)__ldg(code + e0 + i)];
-      const int off = (info & 255) - 128;
-      const int fixed = (info >> 8) & 7, both = (info >> 11) & 7;
-      double v = 0.0;
-      int sb = both;
-      while (true) {
-        const int a = fixed | sb;
-        if ((vmask >> a) & 1u) v = fma(s_kap[a][t], s_K[s_lx[a][t] * (NN + 1) + off], v);
-        if (sb == 0) break;
-        sb = (sb - 1) & both;
-      }
-      vals[e0 + i] = v;
-    }
-    // right-hand side: source over the node's cells minus the lifting of the Dirichlet values
-    if (sub == 0) {
-      double b = 0.0;
+  const uint16_t* et = s_tab + onb * EntryTab<2, K>::E;
+  const int64_t e0 = rowptr[r];
+  const int len = (int)(rowptr[r + 1] - e0);
+  // all stencil codes of the row first (independent loads, one memory latency), then the
+  // entries; a 2D row has at most MAXE of them
+  constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
+  int cv[MAXE];
 #pragma unroll
-      for (int a = 0; a < 4; ++a) {
-        if (!((vmask >> a) & 1u)) continue;
-        const int la = s_lx[a][t];
-        if (!FN) b += f_const * s_F[la];
-        if (FN || UD) {
-          const double ka = s_kap[a][t];
-          const int64_t c0 = (a & 1) ? X0 / K : X0 / K - 1, c1 = (a & 2) ? X1 / K : X1 / K - 1;
-          for (int lj = 0; lj < NN; ++lj) {
-            const int64_t Y0 = (int64_t)K * c0 + lj % L::KP1, Y1 = (int64_t)K * c1 + lj / L::KP1;
-            const int64_t ylin = Y1 * g.N[0] + Y0;
-            if (FN) b += s_M[la * NN + lj] * __ldg(f_nodal + ylin);
-            if (UD) {
-              const bool dir = (g.dsides[0] && Y0 == 0) || (g.dsides[1] && Y0 == g.N[0] - 1) ||
-                               (g.dsides[2] && Y1 == 0) || (g.dsides[3] && Y1 == g.N[1] - 1);
-              if (dir) b -= ka * s_K[la * NN + lj] * __ldg(u_dir + ylin);
-            }
-          }
+  for (int i = 0; i < MAXE; ++i) cv[i] = i < len ? (int)__ldg(code + e0 + i) : 0;
+#pragma unroll
+  for (int i = 0; i < MAXE; ++i) {
+    if (i >= len) break;
+    const int info = et[cv[i]];
+    const int off = (info & 255) - 128;
+    const int fixed = (info >> 8) & 7, both = (info >> 11) & 7;
+    double v = 0.0;
+    int sb = both;
+    while (true) {
+      const int a = fixed | sb;
+      if ((vmask >> a) & 1u) v = fma(s_kap[a][t], s_K[s_lx[a][t] * (NN + 1) + off], v);
+      if (sb == 0) break;
+      sb = (sb - 1) & both;
+    }
+    vals[e0 + i] = v;
+  }
+  // right-hand side: source over the node's cells minus the lifting of the Dirichlet values
+  double b = 0.0;
+#pragma unroll
+  for (int a = 0; a < 4; ++a) {
+    if (!((vmask >> a) & 1u)) continue;
+    const int la = s_lx[a][t];
+    if (!FN) b += f_const * s_F[la];
+    if (FN || UD) {
+      const double ka = s_kap[a][t];
+      const int64_t c0 = (a & 1) ? X0 / K : X0 / K - 1, c1 = (a & 2) ? X1 / K : X1 / K - 1;
+      for (int lj = 0; lj < NN; ++lj) {
+        const int64_t Y0 = (int64_t)K * c0 + lj % L::KP1, Y1 = (int64_t)K * c1 + lj / L::KP1;
+        const int64_t ylin = Y1 * g.N[0] + Y0;
+        if (FN) b += s_M[la * NN + lj] * __ldg(f_nodal + ylin);
+        if (UD) {
+          const bool dir = (g.dsides[0] && Y0 == 0) || (g.dsides[1] && Y0 == g.N[0] - 1) ||
+                           (g.dsides[2] && Y1 == 0) || (g.dsides[3] && Y1 == g.N[1] - 1);
+          if (dir) b -= ka * s_K[la * NN + lj] * __ldg(u_dir + ylin);
         }
       }
-      rhs[r] = b;
     }
   }
+  rhs[r] = b;
   if (nbad) atomicAdd(bad, nbad);
 }
 
@@ -904,12 +902,10 @@ static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_no
   const Geom& g = A->test->geom;
   const int64_t R = A->ngdofs;
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
-  constexpr int RPB = kR2dThreads / kR2dTPR;
-  const unsigned nb = (unsigned)((R + RPB - 1) / RPB);
+  const unsigned nb = (unsigned)((R + 127) / 128);
   const CodeT* code = reinterpret_cast<const CodeT*>(A->code.p);
 #define GD_R2D(FNV, UDV)                                                                                          \
-  k_rows2d_fused<K, CodeT, FNV, UDV><<<nb, kR2dThreads, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa,   \
-                                                                 A->Khat.p,                                       \
+  k_rows2d_fused<K, CodeT, FNV, UDV><<<nb, 128, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa, A->Khat.p, \
                                                          A->Mhat.p, A->Fhat.p, f_const, f_nodal, udir, A->vals.p,  \
                                                          A->rhs.p, bad)
   if (f_nodal && udir) GD_R2D(true, true);
