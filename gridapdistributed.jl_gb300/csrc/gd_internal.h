@@ -229,9 +229,9 @@ struct MixedState {
   // persistent Jacobi-CG on the padded lattice: x r z p q dinv w
   DBuf<float> plat;
   int64_t plat_epoch = -1;
-  // captured batch of flexible-CG steps (lattice path, external preconditioner) and the
-  // preconditioner key, buffers and sizes it was captured with
-  cudaGraphExec_t fcg_graph = nullptr;
+  // captured batches of flexible-CG steps (16, 8, 4 and 2 steps; lattice path, external
+  // preconditioner) and the preconditioner key, buffers and sizes they were captured with
+  cudaGraphExec_t fcg_graph[4] = {nullptr, nullptr, nullptr, nullptr};
   uint64_t fcg_key[5] = {0, 0, 0, 0, 0};
   int64_t lat_epoch = -1;
 };

@@ -1037,7 +1037,6 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
       GD_CUDA_TRY(cudaGetLastError());
     }
     int it = 0;
-    const int batch = 16;
     bool inner_stall = false;
     double check_res = 1.0;
     int check_it = 0;
@@ -1058,34 +1057,41 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
       GD_CUDA_TRY(cudaGetLastError());
       return GD_OK;
     };
+    // Batches of 16, 8, 4 or 2 steps between convergence checks: after each batch the
+    // observed per-step reduction of the residual estimates the steps still needed, and
+    // the next batch is the largest size not above that estimate, so the last batch of a
+    // refinement step does few steps past the tolerance (each costs a preconditioner
+    // application).  Every size is even, so z and p return to the same buffers and one
+    // captured graph per size replays every batch of that size of every outer step.  The
+    // first batch of a solve runs uncaptured (the preconditioner's first-use setup).
+    constexpr int kBatchSizes[4] = {16, 8, 4, 2};
+    int bi = 0;
+    double res_prev = 1.0;   // the inner residual is relative to the normalised start
     while (it < inner_max) {
-      const int nstep = std::min(batch, inner_max - it);
-      // A full batch is an even number of steps, so z and p return to the same buffers:
-      // one captured graph of a batch replays every full batch of every outer step.  The
-      // first batch of a solve runs uncaptured (the preconditioner's first-use setup).
+      const int nstep = std::min(kBatchSizes[bi], inner_max - it);
       const uint64_t key[5] = {ext ? precond->graph_key : 0, (uint64_t)(uintptr_t)M.lat.p,
                                (uint64_t)(uintptr_t)R, (uint64_t)nlat, (uint64_t)gb};
-      const bool graphable = ext && precond->graph_key != 0 && nstep == batch;
-      const bool have = M.fcg_graph && std::equal(key, key + 5, M.fcg_key);
-      if (graphable && !have && (it > 0 || total_inner > 0)) {
-        if (M.fcg_graph) cudaGraphExecDestroy(M.fcg_graph);
-        M.fcg_graph = nullptr;
+      const bool graphable = ext && precond->graph_key != 0 && nstep == kBatchSizes[bi];
+      if (!std::equal(key, key + 5, M.fcg_key)) {   // other buffers or preconditioner: drop all graphs
+        for (auto& gx : M.fcg_graph) {
+          if (gx) cudaGraphExecDestroy(gx);
+          gx = nullptr;
+        }
+        if (graphable && (it > 0 || total_inner > 0)) std::copy(key, key + 5, M.fcg_key);
+      }
+      if (graphable && !M.fcg_graph[bi] && (it > 0 || total_inner > 0) && std::equal(key, key + 5, M.fcg_key)) {
         cudaGraph_t g = nullptr;
         if (cudaStreamBeginCapture(st, cudaStreamCaptureModeRelaxed) == cudaSuccess) {
           const int rc = enqueue(nstep);
           const cudaError_t ce = cudaStreamEndCapture(st, &g);
-          if (rc == GD_OK && ce == cudaSuccess && g &&
-              cudaGraphInstantiate(&M.fcg_graph, g, 0) == cudaSuccess) {
-            std::copy(key, key + 5, M.fcg_key);
-          } else {
-            M.fcg_graph = nullptr;
-          }
+          if (!(rc == GD_OK && ce == cudaSuccess && g && cudaGraphInstantiate(&M.fcg_graph[bi], g, 0) == cudaSuccess))
+            M.fcg_graph[bi] = nullptr;
           if (g) cudaGraphDestroy(g);
         }
         cudaGetLastError();   // a failed capture leaves the uncaptured path below
       }
-      if (graphable && M.fcg_graph && std::equal(key, key + 5, M.fcg_key)) {
-        GD_CUDA_TRY(cudaGraphLaunch(M.fcg_graph, st));
+      if (graphable && M.fcg_graph[bi] && std::equal(key, key + 5, M.fcg_key)) {
+        GD_CUDA_TRY(cudaGraphLaunch(M.fcg_graph[bi], st));
       } else {
         GD_TRY(enqueue(nstep));
       }
@@ -1096,15 +1102,24 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
         inner_stall = ext;
         break;
       }
-      if (std::sqrt(h.rr) <= tol_in) break;
+      const double res = std::sqrt(h.rr);
+      if (res <= tol_in) break;
       if (ext && it - check_it >= 64) {
-        if (std::sqrt(h.rr) > 0.5 * check_res) {
+        if (res > 0.5 * check_res) {
           inner_stall = true;
           break;
         }
-        check_res = std::sqrt(h.rr);
+        check_res = res;
         check_it = it;
       }
+      // next batch size from the per-step reduction factor of this batch
+      const double rho = res_prev > 0.0 && res < res_prev ? std::pow(res / res_prev, 1.0 / nstep) : 1.0;
+      bi = 0;
+      if (rho < 1.0) {
+        const double need = std::log(tol_in / res) / std::log(rho);
+        while (bi < 3 && kBatchSizes[bi] > need) ++bi;
+      }
+      res_prev = res;
     }
     total_inner += it;
     if (inner_stall) {

@@ -627,8 +627,10 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->mx.lat);
   dfreeb(A->mx.latred);
   dfreeb(A->mx.plat);
-  if (A->mx.fcg_graph) cudaGraphExecDestroy(A->mx.fcg_graph);
-  A->mx.fcg_graph = nullptr;
+  for (auto& gx : A->mx.fcg_graph) {
+    if (gx) cudaGraphExecDestroy(gx);
+    gx = nullptr;
+  }
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
   delete A;
