@@ -596,54 +596,65 @@ def run_qp(args, be, stream, dev):
 
 
 # ------------------------------------------------------------------------------------
-# learned preconditioner vs Jacobi (96^3 lognormal diffusion)
+# learned preconditioner vs Jacobi (96^3 and 192^3 lognormal diffusion)
 # ------------------------------------------------------------------------------------
 def run_learned(args, be, dev):
+    """The learned flexible CG against FP64 Jacobi-PCG and the mixed-precision Jacobi
+    refinement on the same system, each timed on its second (warm) solve, at 96^3 (the
+    size the network was trained at; latency-bound: the solve takes a few ms) and 192^3.
+    The learned solution is compared with the mixed-precision Jacobi one."""
     import torch
     import gridap_gb300 as G
     from gridap_gb300.learned import LearnedPreconditioner
-    from gridap_gb300.synthetic import DIFFUSION3D_96, lognormal_kappa
-    w = DIFFUSION3D_96
+    from gridap_gb300.synthetic import DIFFUSION3D_96, DIFFUSION3D_192, lognormal_kappa
     path = PKG / "gridap_gb300" / "weights" / "diffusion3d_q1.gdlp"
     if not path.exists():
         return None
-    cells = w["cells"]
-    ranks = be.distribute(range(int(np.prod(w["parts"]))))
-    model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], cells)
-    V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 1), dirichlet_tags="boundary")
-    U = G.TrialFESpace(0.0, V)
-    dO = G.Measure(G.Triangulation(model), 2)
-    kap = lognormal_kappa(cells, w["sigma"], w["corr_len"], seed=w["seed"] + 1)
-    f = np.random.default_rng(w["seed"] + 100).standard_normal(int(np.prod([c + 1 for c in cells])))
-    op = G.AffineFEOperator(G.integral_grad_grad(kap, dO), G.integral_source(f, dO), U, V)
-    levels, cs = LearnedPreconditioner.file_spec(path)
-    net = LearnedPreconditioner(op.matrix, seed=0, levels=levels, coarse_start=cs)
-    net.load(path)
-    out = {"workload": w["name"], "rtol": 1e-8, "weights": path.name, "levels": net.levels, "coarse_start": cs,
-           "params": net.num_params}
-    runs = {}
-    for name, fn in (("jacobi_pcg_fp64", lambda: op.matrix.solve(rtol=1e-8, method="jacobi_pcg")),
-                     ("mixed_ir_jacobi", lambda: op.matrix.solve(rtol=1e-8, method="mixed_ir")),
-                     ("learned_fcg", lambda: net.solve(rtol=1e-8))):
-        fn()   # warm
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        r = fn()
-        t = time.perf_counter() - t0
-        if name == "learned_fcg":
-            x, st, fb = r
-            runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
-                          "converged": bool(st.converged), "fallback_to_jacobi": fb}
-        else:
-            st = op.matrix.last_stats
-            runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
-                          "converged": bool(st.converged)}
-    out.update(runs)
-    tl = runs["learned_fcg"]["seconds"]
-    out["speedup_vs_jacobi_pcg_fp64"] = runs["jacobi_pcg_fp64"]["seconds"] / tl
-    out["speedup_vs_mixed_ir_jacobi"] = runs["mixed_ir_jacobi"]["seconds"] / tl
-    net.close()
-    return out
+    results = []
+    for w in (DIFFUSION3D_96, DIFFUSION3D_192):
+        cells = w["cells"]
+        ranks = be.distribute(range(int(np.prod(w["parts"]))))
+        model = G.CartesianDiscreteModel(ranks, w["parts"], w["domain"], cells)
+        V = G.TestFESpace(model, G.ReferenceFE(G.lagrangian, float, 1), dirichlet_tags="boundary")
+        U = G.TrialFESpace(0.0, V)
+        dO = G.Measure(G.Triangulation(model), 2)
+        kap = lognormal_kappa(cells, w["sigma"], w["corr_len"], seed=w["seed"] + 1)
+        f = np.random.default_rng(w["seed"] + 100).standard_normal(int(np.prod([c + 1 for c in cells])))
+        op = G.AffineFEOperator(G.integral_grad_grad(kap, dO), G.integral_source(f, dO), U, V)
+        levels, cs = LearnedPreconditioner.file_spec(path)
+        net = LearnedPreconditioner(op.matrix, seed=0, levels=levels, coarse_start=cs)
+        net.load(path)
+        out = {"workload": w["name"], "rtol": 1e-8, "weights": path.name, "levels": net.levels,
+               "coarse_start": cs, "params": net.num_params, "timing": "second solve (warm), host clock"}
+        runs, xs = {}, {}
+        for name, fn in (("jacobi_pcg_fp64", lambda: op.matrix.solve(rtol=1e-8, method="jacobi_pcg")),
+                         ("mixed_ir_jacobi", lambda: op.matrix.solve(rtol=1e-8, method="mixed_ir")),
+                         ("learned_fcg", lambda: net.solve(rtol=1e-8))):
+            fn()   # warm
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            r = fn()
+            t = time.perf_counter() - t0
+            if name == "learned_fcg":
+                x, st, fb = r
+                runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                              "converged": bool(st.converged), "fallback_to_jacobi": fb}
+            else:
+                x = r
+                st = op.matrix.last_stats
+                runs[name] = {"seconds": t, "iterations": st.iterations, "rel_residual": st.rel_residual,
+                              "converged": bool(st.converged)}
+            xs[name] = np.asarray(x)
+        out.update(runs)
+        tl = runs["learned_fcg"]["seconds"]
+        out["speedup_vs_jacobi_pcg_fp64"] = runs["jacobi_pcg_fp64"]["seconds"] / tl
+        out["speedup_vs_mixed_ir_jacobi"] = runs["mixed_ir_jacobi"]["seconds"] / tl
+        ref = xs["mixed_ir_jacobi"]
+        out["max_rel_diff_vs_mixed_ir"] = float(np.abs(xs["learned_fcg"] - ref).max() / np.abs(ref).max())
+        net.close()
+        del op, model, V, U
+        results.append(out)
+    return results
 
 
 # ------------------------------------------------------------------------------------

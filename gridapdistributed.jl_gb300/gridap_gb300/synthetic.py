@@ -102,12 +102,13 @@ def gaussian_random_field_torch(cells, sigma=1.0, corr_len=0.1, seed=0, domain_l
     return field.reshape(-1).contiguous()
 
 
-# Learned-preconditioner workload: 96^3 Q1 cells on the unit cube, parts (2,2,2),
-# kappa = exp(g) (sigma 1.5, correlation length 0.05), load M f with f ~ N(0,1) per node,
-# homogeneous Dirichlet, solve to 1e-8 FP64 relative residual.
+# Learned-preconditioner workloads: 96^3 and 192^3 Q1 cells on the unit cube, parts
+# (2,2,2), kappa = exp(g) (sigma 1.5, correlation length 0.05), load M f with f ~ N(0,1)
+# per node, homogeneous Dirichlet, solve to 1e-8 FP64 relative residual.
 DIFFUSION3D_96 = dict(name="diffusion3d_q1_96^3_parts2x2x2_sigma1.5", dim=3, cells=(96, 96, 96), parts=(2, 2, 2),
                       domain=(0.0, 1.0, 0.0, 1.0, 0.0, 1.0), order=1, degree=2, sigma=1.5, corr_len=0.05,
                       seed=5000)
+DIFFUSION3D_192 = dict(DIFFUSION3D_96, name="diffusion3d_q1_192^3_parts2x2x2_sigma1.5", cells=(192, 192, 192))
 
 
 # Batched uneven workload: 64 independent 3D diffusion problems, cells per direction
