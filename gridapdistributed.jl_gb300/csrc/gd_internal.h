@@ -322,6 +322,16 @@ struct gd_asm {
   gd::DBuf<uint8_t> pat;
   int q1_grid = 0;
   int q1_shape = -1;            // autotuned launch shape (-1: not tuned yet)
+  int64_t q1_rows[2] = {0, -1};   // owned-row range of the next Q1 launch (hi < 0: all rows)
+  // pipelined download (gd_assemble_download): host destinations of the values and the
+  // rhs while active, the copy stream, one event per row range, the row ranges and
+  // their first CSR entries
+  bool dl_active = false;
+  double* dl_rhs = nullptr;
+  double* dl_vals = nullptr;
+  cudaStream_t dl_stream = nullptr;
+  std::vector<cudaEvent_t> dl_events;
+  std::vector<int64_t> dl_rows, dl_nnz;
   float q1_shape_ms[8] = {0};
   gd::DBuf<double> w_cells;   // prescaled coefficients (cube Q1 path)
   std::string q1c_blob;        // cached Q1 class constants for the current reference element

@@ -665,14 +665,18 @@ static int launch_q1_inst(gd_asm* A, const Q1Const& q, const double* kappa, cons
     GD_CUDA_TRY(cudaDeviceGetAttribute(&num_sms, cudaDevAttrMultiProcessorCount, dev));
     if (blocks_per_sm < 1) blocks_per_sm = 1;
   }
-  const int64_t n = A->ngdofs;
+  // owned rows r0 .. r1-1: the row-indexed arrays are offset; rowptr holds absolute
+  // positions in vals, so the kernel needs no row offset of its own
+  const int64_t r0 = A->q1_rows[0], r1 = A->q1_rows[1] >= 0 ? A->q1_rows[1] : A->ngdofs;
+  const int64_t n = r1 - r0;
+  if (n <= 0) return GD_OK;
   const int64_t nchunks = (n + ROWS - 1) / ROWS;
   int64_t grid = (int64_t)blocks_per_sm * num_sms;   // persistent: one wave of resident CTAs
   if (grid > nchunks) grid = nchunks;
   A->q1_grid = (int)grid;
-  kern<<<(unsigned)grid, ROWS, Q::SMEM, st>>>(A->test->geom, q, n, nchunks, A->rowptr.p, A->row_node.p,
-                                               A->row_pat.p, A->pat.p, kappa, f_nodal, udir, A->vals.p, A->rhs.p,
-                                               bad);
+  kern<<<(unsigned)grid, ROWS, Q::SMEM, st>>>(A->test->geom, q, n, nchunks, A->rowptr.p + r0, A->row_node.p + r0,
+                                               A->row_pat.p + r0, A->pat.p, kappa, f_nodal, udir, A->vals.p,
+                                               A->rhs.p + r0, bad);
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
 }
@@ -755,9 +759,34 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
     A->q1_shape = best_shape;
   }
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[1], st));
-  int s = cube ? launch_q1_mode<DIM, true>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st)
-               : launch_q1_mode<DIM, false>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st);
-  if (s != GD_OK) return s;
+  if (A->dl_active) {
+    // pipelined download: one launch per row range; the copy stream takes each range's
+    // values and rhs to the host while the next range is assembled
+    const size_t nr = A->dl_rows.size() - 1;
+    for (size_t k = 0; k < nr; ++k) {
+      A->q1_rows[0] = A->dl_rows[k];
+      A->q1_rows[1] = A->dl_rows[k + 1];
+      const int s2 = cube ? launch_q1_mode<DIM, true>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st)
+                          : launch_q1_mode<DIM, false>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st);
+      A->q1_rows[0] = 0;
+      A->q1_rows[1] = -1;
+      if (s2 != GD_OK) return s2;
+      GD_CUDA_TRY(cudaEventRecord(A->dl_events[k], st));
+      GD_CUDA_TRY(cudaStreamWaitEvent(A->dl_stream, A->dl_events[k], 0));
+      const int64_t e0 = A->dl_nnz[k], e1 = A->dl_nnz[k + 1];
+      const int64_t q0 = A->dl_rows[k], q1 = A->dl_rows[k + 1];
+      if (A->dl_vals && e1 > e0)
+        GD_CUDA_TRY(cudaMemcpyAsync(A->dl_vals + e0, A->vals.p + e0, sizeof(double) * (e1 - e0),
+                                    cudaMemcpyDeviceToHost, A->dl_stream));
+      if (A->dl_rhs && q1 > q0)
+        GD_CUDA_TRY(cudaMemcpyAsync(A->dl_rhs + q0, A->rhs.p + q0, sizeof(double) * (q1 - q0),
+                                    cudaMemcpyDeviceToHost, A->dl_stream));
+    }
+  } else {
+    const int s = cube ? launch_q1_mode<DIM, true>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st)
+                       : launch_q1_mode<DIM, false>(A, A->q1_shape, q, coef, f_nodal, udir, bad, st);
+    if (s != GD_OK) return s;
+  }
   if (A->profiling) {   // one fused kernel: the rhs phase is empty
     GD_CUDA_TRY(cudaEventRecord(A->ev[2], st));
     GD_CUDA_TRY(cudaEventRecord(A->ev[3], st));
@@ -1164,4 +1193,53 @@ extern "C" int gd_assemble_vector(gd_asm* A, const gd_coeffs* c, double* b, int 
 }
 
 extern "C" int gd_assemble_numeric(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, true); }
+
+// Numeric assembly followed by the download of the rhs and the owned-row values, with
+// the download overlapped with the assembly on the Q1 path: the owned rows are assembled
+// in kDownloadRanges launches, and each range's values and rhs go to the host on a second
+// stream while the next range is assembled.  Other paths assemble, then download.
+extern "C" int gd_assemble_download(gd_asm* A, const gd_coeffs* c, double* rhs, double* owned_vals) {
+  using namespace gd;
+  constexpr int kDownloadRanges = 8;
+  if (!A || !c) return fail(GD_ERR_ARG, "gd_assemble_download: null argument");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_assemble_download: run gd_assemble_symbolic first");
+  if (!A->fast_q1 || A->bs > 1 || A->ngdofs == 0) {
+    GD_TRY(numeric_impl(A, c, true));
+    return gd_system_download(A, rhs, owned_vals);
+  }
+  cudaStream_t st = A->test->model->ctx->stream;
+  if (!A->dl_stream) GD_CUDA_TRY(cudaStreamCreateWithFlags(&A->dl_stream, cudaStreamNonBlocking));
+  if (A->dl_rows.empty()) {   // row ranges and their first entries, once per assembler
+    const int64_t n = A->ngdofs;
+    std::vector<int64_t> rows(kDownloadRanges + 1), nnz(kDownloadRanges + 1);
+    for (int k = 0; k <= kDownloadRanges; ++k) rows[k] = n * k / kDownloadRanges;
+    for (int k = 0; k <= kDownloadRanges; ++k)
+      GD_CUDA_TRY(cudaMemcpyAsync(&nnz[k], A->rowptr.p + rows[k], sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+    GD_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int k = 0; k < kDownloadRanges; ++k) {
+      cudaEvent_t e;
+      GD_CUDA_TRY(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      A->dl_events.push_back(e);
+    }
+    A->dl_rows = rows;
+    A->dl_nnz = nnz;
+  }
+  // the copies of a previous call are done (that call synchronised), so the values may be
+  // rewritten
+  A->dl_active = true;
+  A->dl_rhs = rhs;
+  A->dl_vals = owned_vals;
+  const int s = numeric_impl(A, c, false);
+  A->dl_active = false;
+  A->dl_rhs = A->dl_vals = nullptr;
+  const cudaError_t e1 = cudaStreamSynchronize(A->dl_stream);
+  if (s != GD_OK) return s;
+  if (e1 != cudaSuccess) return fail(GD_ERR_CUDA, std::string("gd_assemble_download: ") + cudaGetErrorString(e1));
+  int32_t hbad = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, A->dred.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (hbad)
+    return fail(GD_ERR_NUMERIC, "numeric: kappa is not finite and positive in " + std::to_string(hbad) + " cell visits");
+  return GD_OK;
+}
 extern "C" int gd_assemble_numeric_async(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, false); }

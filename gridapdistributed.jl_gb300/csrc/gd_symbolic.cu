@@ -633,6 +633,8 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   }
   for (int i = 0; i < 4; ++i)
     if (A->ev[i]) cudaEventDestroy(A->ev[i]);
+  for (cudaEvent_t e : A->dl_events) cudaEventDestroy(e);
+  if (A->dl_stream) cudaStreamDestroy(A->dl_stream);
   delete A;
   return GD_OK;
 }

@@ -272,6 +272,12 @@ int gd_system_device_ptrs(const gd_asm* a, const int64_t** rowptr, const int32_t
                           const double** vals, const double** rhs, int64_t* ngdofs);
 /* Copy the global rhs (ngdofs) and optionally all owned-row values to host. */
 int gd_system_download(const gd_asm* a, double* rhs, double* owned_vals);
+/* gd_assemble_numeric followed by gd_system_download (either host pointer may be NULL),
+ * the download overlapped with the assembly where the Q1 kernel assembles the rows
+ * (it runs over 8 ranges of owned rows; each range's values and rhs are copied to the
+ * host on a second stream while the next range is assembled).  Same results as the two
+ * calls; the copies are complete when it returns.  Host buffers should be pinned. */
+int gd_assemble_download(gd_asm* a, const gd_coeffs* coeffs, double* rhs, double* owned_vals);
 
 /* ---- A14-A16: mul!, `\`, FEFunction ------------------------------------------ */
 /* y = A*x over global vectors (ngdofs), PSparseMatrix mul! semantics. */
