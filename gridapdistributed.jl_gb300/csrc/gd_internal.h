@@ -322,6 +322,11 @@ struct gd_asm {
   gd::DBuf<uint8_t> pat;
   int q1_grid = 0;
   int q1_shape = -1;            // autotuned launch shape (-1: not tuned yet)
+  // 2D Q_k rows: the reference tables are reflection-invariant (cached per reference
+  // element), and whether the class-sum rows may use it (on by default)
+  bool r2d_sym = false;
+  int r2d_sym_degree = -1;
+  bool r2d_class_sums = true;
   int64_t q1_rows[2] = {0, -1};   // owned-row range of the next Q1 launch (hi < 0: all rows)
   // pipelined download (gd_assemble_download): host destinations of the values and the
   // rhs while active, the copy stream, one event per row range, the row ranges and
@@ -342,6 +347,9 @@ struct gd_asm {
   gd::DBuf<double> Khat, Mhat, Fhat;
   int ref_degree = -1;
   gd::DBuf<double> kappa_dev, f_dev;   // staging for host inputs
+  // cell visits whose coefficient failed the check in the numeric kernels since the last
+  // synchronous report (zero unless one failed; reset after it is reported)
+  gd::DBuf<int32_t> nbad;
   // profiling events: start, after ghost zeroing, after matrix, after rhs
   bool profiling = false;
   cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};

@@ -827,7 +827,15 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
 // shared-memory entry table, as in qk_matrix_rows) and finally the right-hand side (source
 // term and Dirichlet lifting with the same cells).  Consecutive threads own consecutive
 // rows, so a warp's values are one contiguous range of the CSR value array.
-template <int K, typename CodeT, bool FN, bool UD>
+// CS (class sums): when the reference tables are invariant under the square's reflections
+// (checked on the host), the cells that hold both nodes of an entry are reflections of
+// one another across the node's cell boundaries and give the same table value, so the
+// entry is that value times the sum of their coefficients: the thread forms the 9 subset
+// sums of its (at most 4) cell coefficients once (left, right or both cells per
+// direction; 5 FP64 additions) and each entry costs one FP64 multiply, where the exact
+// per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
+// of its FP32 rate, and this kernel is bound by it.
+template <int K, typename CodeT, bool FN, bool UD, bool CS>
 __global__ void __launch_bounds__(128)
 k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
                const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
@@ -839,26 +847,30 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   __shared__ double s_K[NN * NN];
   __shared__ double s_M[FN ? NN * NN : 1];
   __shared__ double s_F[NN];
+  __shared__ double s_Fn[CS && !FN ? NN * 5 : 1];   // f_const F[l] n for n = 0..4 valid cells
   __shared__ uint16_t s_tab[EntryTab<2, K>::SIZE];
   __shared__ double s_kap[4][128];   // per thread: coefficient and local index of its 4 slots
   __shared__ int s_lx[4][128];       // (shared, not local, memory: they are indexed at run time)
+  __shared__ double s_S[CS ? 9 : 1][128];   // per thread: subset sums, index ox + 3 oy (0 left, 1 right, 2 both)
   for (int i = threadIdx.x; i < NN * NN; i += blockDim.x) {
     s_K[i] = Khat[i];
     if (FN) s_M[i] = Mhat[i];
   }
   for (int i = threadIdx.x; i < NN; i += blockDim.x) s_F[i] = Fhat[i];
+  if (CS && !FN)
+    for (int i = threadIdx.x; i < NN * 5; i += blockDim.x) s_Fn[i] = f_const * __ldg(Fhat + i / 5) * (double)(i % 5);
   build_entry_tab<2, K>(s_tab);
   __syncthreads();
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= nrows_own) return;
+  const int t = threadIdx.x;
+  int nbad = 0;
   const uint32_t N0 = (uint32_t)g.N[0];
   const uint32_t lin = (uint32_t)row_node[r];
   const int X0 = (int)(lin % N0), X1 = (int)(lin / N0);
   const int rm0 = X0 % K, rm1 = X1 % K;
   const int onb = (rm0 == 0 ? 1 : 0) | (rm1 == 0 ? 2 : 0);
-  const int t = threadIdx.x;
   uint32_t vmask = 0;
-  int nbad = 0;
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     const int s0 = a & 1, s1 = (a >> 1) & 1;
@@ -873,6 +885,19 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     s_kap[a][t] = k;
     s_lx[a][t] = (s0 ? rm0 : K) + L::KP1 * (s1 ? rm1 : K);
     vmask |= (uint32_t)ok << a;
+  }
+  if (CS) {   // slot a = s0 | 2 s1 (s = 1: the cell on the upper side of the node)
+    const double k00 = s_kap[0][t], k10 = s_kap[1][t], k01 = s_kap[2][t], k11 = s_kap[3][t];
+    const double lo2 = k00 + k10, hi2 = k01 + k11;
+    s_S[0][t] = k00;
+    s_S[1][t] = k10;
+    s_S[2][t] = lo2;
+    s_S[3][t] = k01;
+    s_S[4][t] = k11;
+    s_S[5][t] = hi2;
+    s_S[6][t] = k00 + k01;
+    s_S[7][t] = k10 + k11;
+    s_S[8][t] = lo2 + hi2;
   }
   const uint16_t* et = s_tab + onb * EntryTab<2, K>::E;
   const int64_t e0 = rowptr[r];
@@ -890,30 +915,41 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     const int off = (info & 255) - 128;
     const int fixed = (info >> 8) & 7, both = (info >> 11) & 7;
     double v = 0.0;
-    int sb = both;
-    while (true) {
-      const int a = fixed | sb;
-      if ((vmask >> a) & 1u) v = fma(s_kap[a][t], s_K[s_lx[a][t] * (NN + 1) + off], v);
-      if (sb == 0) break;
-      sb = (sb - 1) & both;
+    if (CS) {
+      const int ox = (both & 1) ? 2 : (fixed & 1), oy = (both & 2) ? 2 : ((fixed >> 1) & 1);
+      v = s_K[s_lx[fixed][t] * (NN + 1) + off] * s_S[ox + 3 * oy][t];
+    } else {
+      int sb = both;
+      while (true) {
+        const int a = fixed | sb;
+        if ((vmask >> a) & 1u) v = fma(s_kap[a][t], s_K[s_lx[a][t] * (NN + 1) + off], v);
+        if (sb == 0) break;
+        sb = (sb - 1) & both;
+      }
     }
     vals[e0 + i] = v;
   }
   // right-hand side: source over the node's cells minus the lifting of the Dirichlet values
-  double b = 0.0;
+  // (CS: the source value of the node's local position is the same in all its cells; slot
+  // 3, the cell on the upper side in both directions, always holds the node)
+  double b = CS && !FN ? s_Fn[s_lx[3][t] * 5 + __popc(vmask)] : 0.0;
 #pragma unroll
   for (int a = 0; a < 4; ++a) {
     if (!((vmask >> a) & 1u)) continue;
     const int la = s_lx[a][t];
-    if (!FN) b += f_const * s_F[la];
-    if (FN || UD) {
+    if (!FN && !CS) b += f_const * s_F[la];
+    const int64_t c0 = (a & 1) ? X0 / K : X0 / K - 1, c1 = (a & 2) ? X1 / K : X1 / K - 1;
+    // Dirichlet nodes of a cell lie on its sides that are Dirichlet sides of the domain:
+    // cells away from them have nothing to lift (most rows)
+    const bool lift = UD && ((g.dsides[0] && c0 == 0) || (g.dsides[1] && c0 == g.n[0] - 1) ||
+                             (g.dsides[2] && c1 == 0) || (g.dsides[3] && c1 == g.n[1] - 1));
+    if (FN || lift) {
       const double ka = s_kap[a][t];
-      const int64_t c0 = (a & 1) ? X0 / K : X0 / K - 1, c1 = (a & 2) ? X1 / K : X1 / K - 1;
       for (int lj = 0; lj < NN; ++lj) {
         const int64_t Y0 = (int64_t)K * c0 + lj % L::KP1, Y1 = (int64_t)K * c1 + lj / L::KP1;
         const int64_t ylin = Y1 * g.N[0] + Y0;
         if (FN) b += s_M[la * NN + lj] * __ldg(f_nodal + ylin);
-        if (UD) {
+        if (lift) {
           const bool dir = (g.dsides[0] && Y0 == 0) || (g.dsides[1] && Y0 == g.N[0] - 1) ||
                            (g.dsides[2] && Y1 == 0) || (g.dsides[3] && Y1 == g.N[1] - 1);
           if (dir) b -= ka * s_K[la * NN + lj] * __ldg(u_dir + ylin);
@@ -925,6 +961,42 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   if (nbad) atomicAdd(bad, nbad);
 }
 
+// True when the 2D Q_k reference stiffness and load tables are invariant under the
+// reflections of the square (K[R(i)][R(j)] = K[i][j], F[R(i)] = F[i] to 1e-14 relative for
+// the reflection of x and the reflection of y), the condition of the class-sum rows.
+// Cached per reference element.
+static int rows2d_symmetric(gd_asm* A, int K, bool* sym) {
+  if (A->r2d_sym_degree == A->ref_degree) {
+    *sym = A->r2d_sym;
+    return GD_OK;
+  }
+  const int KP1 = K + 1, NN = KP1 * KP1;
+  cudaStream_t st = A->test->model->ctx->stream;
+  std::vector<double> Kh(NN * NN), Fh(NN);
+  GD_CUDA_TRY(cudaMemcpyAsync(Kh.data(), A->Khat.p, sizeof(double) * NN * NN, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaMemcpyAsync(Fh.data(), A->Fhat.p, sizeof(double) * NN, cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  double kmax = 0.0, fmax = 0.0;
+  for (double v : Kh) kmax = std::max(kmax, std::fabs(v));
+  for (double v : Fh) fmax = std::max(fmax, std::fabs(v));
+  bool ok = true;
+  for (int refl = 0; refl < 2 && ok; ++refl) {
+    auto R = [&](int i) {
+      const int x = i % KP1, y = i / KP1;
+      return refl == 0 ? (K - x) + KP1 * y : x + KP1 * (K - y);
+    };
+    for (int i = 0; i < NN && ok; ++i) {
+      if (std::fabs(Fh[R(i)] - Fh[i]) > 1e-14 * fmax) ok = false;
+      for (int j = 0; j < NN && ok; ++j)
+        if (std::fabs(Kh[R(i) * NN + R(j)] - Kh[i * NN + j]) > 1e-14 * kmax) ok = false;
+    }
+  }
+  A->r2d_sym = ok;
+  A->r2d_sym_degree = A->ref_degree;
+  *sym = ok;
+  return GD_OK;
+}
+
 template <int K, typename CodeT>
 static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_nodal, double f_const, int32_t* bad,
                               cudaStream_t st) {
@@ -933,14 +1005,24 @@ static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_no
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
   const unsigned nb = (unsigned)((R + 127) / 128);
   const CodeT* code = reinterpret_cast<const CodeT*>(A->code.p);
-#define GD_R2D(FNV, UDV)                                                                                          \
-  k_rows2d_fused<K, CodeT, FNV, UDV><<<nb, 128, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa, A->Khat.p, \
-                                                         A->Mhat.p, A->Fhat.p, f_const, f_nodal, udir, A->vals.p,  \
-                                                         A->rhs.p, bad)
-  if (f_nodal && udir) GD_R2D(true, true);
-  else if (f_nodal) GD_R2D(true, false);
-  else if (udir) GD_R2D(false, true);
-  else GD_R2D(false, false);
+  bool cs = false;
+  GD_TRY(rows2d_symmetric(A, K, &cs));
+  cs = cs && A->r2d_class_sums;
+#define GD_R2D(FNV, UDV, CSV)                                                                                     \
+  k_rows2d_fused<K, CodeT, FNV, UDV, CSV><<<nb, 128, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa,      \
+                                                              A->Khat.p, A->Mhat.p, A->Fhat.p, f_const, f_nodal,   \
+                                                              udir, A->vals.p, A->rhs.p, bad)
+  if (cs) {
+    if (f_nodal && udir) GD_R2D(true, true, true);
+    else if (f_nodal) GD_R2D(true, false, true);
+    else if (udir) GD_R2D(false, true, true);
+    else GD_R2D(false, false, true);
+  } else {
+    if (f_nodal && udir) GD_R2D(true, true, false);
+    else if (f_nodal) GD_R2D(true, false, false);
+    else if (udir) GD_R2D(false, true, false);
+    else GD_R2D(false, false, false);
+  }
 #undef GD_R2D
   GD_CUDA_TRY(cudaGetLastError());
   return GD_OK;
@@ -1018,6 +1100,18 @@ int launch_rhs_table(gd_asm* A, const double* kappa, const double* table, double
   return fail(GD_ERR_UNSUPPORTED, "numeric: unsupported dim/order");
 }
 
+// Reads the coefficient-check count after the stream's work; a failure is reported once
+// (the count is reset).
+static int numeric_report(gd_asm* A, cudaStream_t st) {
+  int32_t hbad = 0;
+  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, A->nbad.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  if (!hbad) return GD_OK;
+  GD_CUDA_TRY(cudaMemsetAsync(A->nbad.p, 0, sizeof(int32_t), st));
+  GD_CUDA_TRY(cudaStreamSynchronize(st));
+  return fail(GD_ERR_NUMERIC, "numeric: kappa is not finite and positive in " + std::to_string(hbad) + " cell visits");
+}
+
 int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   if (!A || !c) return fail(GD_ERR_ARG, "gd_assemble_numeric: null argument");
   if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_assemble_numeric: run gd_assemble_symbolic first");
@@ -1052,10 +1146,13 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
     GD_CUDA_TRY(cudaStreamSynchronize(st));
     kappa = A->kappa_dev.p;
   }
-  // reduction/flag scratch lives in dred[0] (as int)
-  if (!A->dred.p) GD_TRY(dalloc(A->dred, 4096));
-  int32_t* bad = (int32_t*)A->dred.p;
-  GD_CUDA_TRY(cudaMemsetAsync(bad, 0, sizeof(int32_t), st));
+  // the coefficient-check count: zeroed when allocated and after a reported failure, so a
+  // numeric assembly is its kernels alone
+  if (!A->nbad.p) {
+    GD_TRY(dalloc(A->nbad, 1));
+    GD_CUDA_TRY(cudaMemsetAsync(A->nbad.p, 0, sizeof(int32_t), st));
+  }
+  int32_t* bad = A->nbad.p;
   // Ghost rows (SubAssembledRows) hold explicit zeros: they were cleared by the symbolic
   // phase and no numeric kernel writes them.
   if (A->profiling) GD_CUDA_TRY(cudaEventRecord(A->ev[0], st));
@@ -1069,13 +1166,7 @@ int numeric_impl(gd_asm* A, const gd_coeffs* c, bool sync) {
   else if (g.dim == 3 && g.k == 2) s = launch_numeric<3, 2>(A, kappa, fn, c->f_const, bad, st);
   else if (g.dim == 3 && g.k == 3) s = launch_numeric<3, 3>(A, kappa, fn, c->f_const, bad, st);
   if (s != GD_OK) return s == GD_ERR_UNSUPPORTED ? fail(s, "numeric: unsupported dim/order") : s;
-  if (sync) {
-    int32_t hbad = 0;
-    GD_CUDA_TRY(cudaMemcpyAsync(&hbad, bad, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-    GD_CUDA_TRY(cudaStreamSynchronize(st));
-    if (hbad) return fail(GD_ERR_NUMERIC, "numeric: kappa is not finite and positive in " + std::to_string(hbad) +
-                                              " cell visits");
-  }
+  if (sync) GD_TRY(numeric_report(A, st));
   A->numeric_done = true;
   A->qp_values = false;
   ++A->numeric_epoch;
@@ -1121,6 +1212,12 @@ extern "C" int gd_assembler_set_shape(gd_asm* A, int shape) {
   if (!A->fast_q1) return gd::fail(GD_ERR_UNSUPPORTED, "gd_assembler_set_shape: the assembler does not use the Q1 kernel");
   if (shape < -1 || shape >= gd::kNumQ1Shapes) return gd::fail(GD_ERR_ARG, "gd_assembler_set_shape: shape out of range");
   A->q1_shape = shape;   // -1: the next numeric assembly times every shape again
+  return GD_OK;
+}
+
+extern "C" int gd_assembler_set_class_sums(gd_asm* A, int on) {
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_set_class_sums: null assembler");
+  A->r2d_class_sums = on != 0;
   return GD_OK;
 }
 
@@ -1235,11 +1332,6 @@ extern "C" int gd_assemble_download(gd_asm* A, const gd_coeffs* c, double* rhs, 
   const cudaError_t e1 = cudaStreamSynchronize(A->dl_stream);
   if (s != GD_OK) return s;
   if (e1 != cudaSuccess) return fail(GD_ERR_CUDA, std::string("gd_assemble_download: ") + cudaGetErrorString(e1));
-  int32_t hbad = 0;
-  GD_CUDA_TRY(cudaMemcpyAsync(&hbad, A->dred.p, sizeof(int32_t), cudaMemcpyDeviceToHost, st));
-  GD_CUDA_TRY(cudaStreamSynchronize(st));
-  if (hbad)
-    return fail(GD_ERR_NUMERIC, "numeric: kappa is not finite and positive in " + std::to_string(hbad) + " cell visits");
-  return GD_OK;
+  return numeric_report(A, st);
 }
 extern "C" int gd_assemble_numeric_async(gd_asm* A, const gd_coeffs* c) { return gd::numeric_impl(A, c, false); }

@@ -606,6 +606,7 @@ extern "C" int gd_assembler_destroy(gd_asm* A) {
   dfreeb(A->Fhat);
   dfreeb(A->kappa_dev);
   dfreeb(A->f_dev);
+  dfreeb(A->nbad);
   dfreeb(A->w);
   dfreeb(A->dred);
   dfreeb(A->dinv);

@@ -111,6 +111,7 @@ SIGNATURES = {
     "gd_vector_export": [P, C.c_int, DP],
     "gd_system_device_ptrs": [P, PP, PP, PP, PP, I64P],
     "gd_system_download": [P, DP, DP],
+    "gd_assembler_set_class_sums": [P, C.c_int],
     "gd_assemble_download": [P, C.POINTER(gd_coeffs), DP, DP],
     "gd_spmv": [P, P, P, C.c_int],
     "gd_solve": [P, C.c_int, C.c_double, C.c_int, P, C.c_int, C.POINTER(gd_solve_stats)],

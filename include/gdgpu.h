@@ -152,7 +152,9 @@ typedef struct gd_coeffs {
 /* assemble_matrix_and_vector! into the symbolic pattern: matrix values and the
  * right-hand side of every part.  Deterministic (no floating-point atomics). */
 int gd_assemble_numeric(gd_asm* a, const gd_coeffs* c);
-/* Same, without the final stream synchronisation (for timing loops). */
+/* Same, without the final stream synchronisation (for timing loops).  A coefficient
+ * that fails the check (not finite and positive) is reported by the next synchronous
+ * numeric call of the assembler. */
 int gd_assemble_numeric_async(gd_asm* a, const gd_coeffs* c);
 /* assemble_vector(assem, collect_cell_vector(V, l)) for l(v) = int(v f) (Gridap's
  * assemble_vector, called at test/FESpacesTests.jl:65-69): the load vector without
@@ -251,6 +253,11 @@ int gd_assembler_tuning(const gd_asm* a, int32_t* shape, int32_t* rows, int32_t*
  * again.  Every shape writes the same values; this exists to check that.  GD_ERR_UNSUPPORTED
  * when the assembler does not use the Q1 kernel. */
 int gd_assembler_set_shape(gd_asm* a, int shape);
+/* 2D Q_k rows (k = 2, 3): on != 0 (the default) forms each entry as one reference value
+ * times the sum of the coefficients of the cells that hold both nodes, when the reference
+ * tables are invariant under the square's reflections (checked); 0 sums the cells' terms
+ * one by one.  The two agree to rounding; this exists to compare them. */
+int gd_assembler_set_class_sums(gd_asm* a, int on);
 
 /* Sizes of one part's local matrix: rows (owned + ghost), columns (owned + ghost),
  * stored entries, ghost rows, ghost columns. */

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import gridap_oracle as go
-from helpers import gpu_system, make_problem, row_scaled_error
+from helpers import export_part, gpu_system, make_problem, row_scaled_error
 
 pytestmark = pytest.mark.gpu
 
@@ -277,3 +277,40 @@ def test_nonpositive_kappa_is_rejected(backend):
     with pytest.raises(G._lib.GdError) as e:
         gpu_system(backend, pb, "sub")
     assert e.value.status == 8
+
+
+CLASS_SUM_CASES = [
+    dict(dim=2, n=(37, 29), parts=(2, 2), order=2, seed=61),
+    dict(dim=2, n=(23, 31), parts=(2, 1), order=3, sides=(1, 0, 1, 1), seed=62, domain=(0, 1.0, 0, 0.6)),
+    dict(dim=2, n=(30, 26), parts=(2, 2), order=2, seed=63, f_nodal=True, u=lambda x, y: 1.0 + x * x - y),
+    dict(dim=2, n=(40, 40), parts=(2, 2), order=2, u=lambda x, y: (x + y) ** 2),
+]
+
+
+@pytest.mark.parametrize("case", CLASS_SUM_CASES, ids=["q2", "q3_rect_sides", "q2_fn_ud", "q2_c1_like"])
+def test_2d_class_sum_rows_match_per_cell_rows(backend, case):
+    """2D Q2/Q3 rows: one reference value times the sum of the shared cells' coefficients
+    (the default) against the per-cell sum, on square and rectangular cells, with partial
+    Dirichlet sides, nodal sources and Dirichlet lifting: values within 1e-14 x max|row|,
+    rhs within 1e-14 x max|b|; both against the oracle at the parity tolerance."""
+    import gridap_gb300 as G
+    pb = make_problem(**case)
+    fe = go.build_fespace(pb)
+    ref = go.assemble(pb, fe, "sub")
+    _, V, U, op = gpu_system(backend, pb, "sub")
+    assem = op.matrix.assem
+    got = {}
+    for cs in (1, 0):
+        G._lib.call("gd_assembler_set_class_sums", assem.handle, cs)
+        assem.numeric(op.a, op.l)
+        got[cs] = [export_part(assem.handle, p) for p in range(int(np.prod(pb.np)))]
+    G._lib.call("gd_assembler_set_class_sums", assem.handle, 1)
+    for p, M in enumerate(ref):
+        a, b = got[1][p], got[0][p]
+        assert np.array_equal(a["rowptr"], b["rowptr"]) and np.array_equal(a["colidx"], b["colidx"])
+        assert row_scaled_error(a["vals"], b["vals"], a["rowptr"]) <= 1e-14
+        bscale = max(np.abs(b["b"]).max(initial=0.0), 1e-300)
+        assert np.abs(a["b"] - b["b"]).max(initial=0.0) <= 1e-14 * bscale
+        for g in (a, b):
+            assert row_scaled_error(g["vals"], M.vals, M.rowptr) <= VAL_TOL
+            assert np.abs(g["b"] - M.b).max(initial=0.0) <= VAL_TOL * max(np.abs(M.b).max(initial=0.0), 1e-300)
