@@ -948,7 +948,7 @@ static int net_loss(gd_learned* N, const float* z, const float* e, double* loss,
 
 // levels with fewer voxels than this use the direct convolution (one thread per voxel and
 // output channel) instead of the shared-memory tiles
-constexpr int64_t kDirectConvVoxels = 60000;
+constexpr int64_t kDirectConvVoxels = 10000;
 // levels below this (but above the direct limit) use 2 voxels per thread: twice the
 // threads per tile, so a level of ~10^5 voxels still fills the SMs
 constexpr int64_t kWideTileVoxels = 400000;

@@ -6,7 +6,7 @@
 // prescaled coefficients w = K2*kappa of its cells and the search direction at its 21
 // non-edge neighbours (edge neighbours of a cube Q1 stiffness are exactly zero).
 // One Jacobi-CG iteration is two phases:
-//   apply : p <- z + beta p (fused, ping-pong buffers), q = A p, alpha = rz / p.q
+//   apply : p <- z + beta p (ping-pong buffers), q <- A z + beta q (= A p), alpha = rz / p.q
 //   update: x += alpha p, r -= alpha q, z = D^-1 r, beta = r.z_new / r.z_old
 // The Jacobi solve runs all iterations in one cooperative launch (k_pad_cg, grid
 // barriers between the phases); the flexible CG around an external preconditioner runs
@@ -137,11 +137,11 @@ __device__ inline bool lat_dirichlet(const LatGeom& g, int x, int y, int z) {
          (g.ds[4] && z == 0) || (g.ds[5] && z == g.N[2] - 1);
 }
 
-// r = r64[gid] * inv, x = 0, p = 0 (z = D^-1 r for Jacobi); sums r.z, r.r; beta = 0
+// r = r64[gid] * inv, x = p = q = 0 (z = D^-1 r for Jacobi); sums r.z, r.r; beta = 0
 __global__ void __launch_bounds__(kLatThreads)
 k_lat_start(int nlat, const int32_t* __restrict__ node_gid, const double* __restrict__ r64, double inv,
             const float* __restrict__ dinvl, float* __restrict__ x, float* __restrict__ r, float* __restrict__ z,
-            float* __restrict__ p, int jacobi, LatRed* R) {
+            float* __restrict__ p, float* __restrict__ q, int jacobi, LatRed* R) {
   float a = 0.f, b = 0.f;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nlat; i += gridDim.x * blockDim.x) {
     const int32_t g = node_gid[i];
@@ -149,6 +149,7 @@ k_lat_start(int nlat, const int32_t* __restrict__ node_gid, const double* __rest
     r[i] = ri;
     x[i] = 0.f;
     p[i] = 0.f;
+    q[i] = 0.f;
     if (jacobi) {
       const float zi = dinvl[i] * ri;
       z[i] = zi;
@@ -165,15 +166,16 @@ k_lat_start(int nlat, const int32_t* __restrict__ node_gid, const double* __rest
   }
 }
 
-// pn = z + beta p_old (written to p_new), q = A pn, alpha = rz / pn.q.
+// pn = z + beta p_old (written to p_new), q <- A z + beta q (= A pn, since q held A p_old),
+// alpha = rz / pn.q; only z is read at the neighbours, p and q at the node itself.
 // A thread takes 4 consecutive nodes of one lattice row (groups never wrap a row).  Each
 // of the 9 neighbour rows is read once (6 values shared by the 4 nodes and their three
 // x-offsets) and the 5x2x2 cell coefficients around the group once.  Every thread runs
 // the same code: loads outside the lattice are predicated off and read as 0, which is
 // exact, since a neighbour outside the lattice shares only outside cells (w = 0) with the
-// node.  Dirichlet nodes get q = 0.  (Measured against a per-node variant with bounds
-// checks, which diverged in nearly every warp, and against 2.5D shared-memory blocking,
-// whose plane staging cost more instructions than it saved.)
+// node.  Dirichlet nodes get A z = 0 (q stays 0 there).  (Measured against a per-node
+// variant with bounds checks, which diverged in nearly every warp, and against 2.5D
+// shared-memory blocking, whose plane staging cost more instructions than it saved.)
 //
 // Body of k_lat_apply over the groups gi = g0, g0 + gs, ...; returns the thread's p.q partial.
 __device__ __forceinline__ float lat_apply_groups(const LatGeom& lg, const float* __restrict__ wf, float ratio,
@@ -220,7 +222,7 @@ __device__ __forceinline__ float lat_apply_groups(const LatGeom& lg, const float
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
           const bool need = nyz != 0 || (k >= 1 && k <= 4);   // the centre row needs the own nodes only
-          v[k] = need && rin && xin[k] ? fmaf(beta, __ldg(p_old + base + k), __ldg(z + base + k)) : 0.f;
+          v[k] = need && rin && xin[k] ? __ldg(z + base + k) : 0.f;
         }
         const int a1 = (o1 + 1) >> 1, a2 = (o2 + 1) >> 1;
 #pragma unroll
@@ -256,10 +258,11 @@ __device__ __forceinline__ float lat_apply_groups(const LatGeom& lg, const float
       const int X = X0 + j;
       if (X >= N0) break;
       const bool dir = ydir || (lg.ds[0] && X == 0) || (lg.ds[1] && X == N0 - 1);
-      const float qv = dir ? 0.f : acc[j];
-      p_new[i0 + j] = own[j];
+      const float qv = fmaf(beta, q[i0 + j], dir ? 0.f : acc[j]);
+      const float pv = fmaf(beta, p_old[i0 + j], own[j]);
+      p_new[i0 + j] = pv;
       q[i0 + j] = qv;
-      dot = fmaf(own[j], qv, dot);
+      dot = fmaf(pv, qv, dot);
     }
   }
   return dot;
@@ -1029,7 +1032,8 @@ int mixed_solve_lattice(gd_asm* A, double rtol, int maxit, double* x_out, int wh
       continue;
     }
     int zc = 0, pc = 0;   // current z and p buffers
-    k_lat_start<<<gb, kLatThreads, 0, st>>>(nlat, M.node_gid.p, r64, 1.0 / rnorm, dinvl, x, r, zb[zc], pb[pc], !ext, R);
+    k_lat_start<<<gb, kLatThreads, 0, st>>>(nlat, M.node_gid.p, r64, 1.0 / rnorm, dinvl, x, r, zb[zc], pb[pc], q, !ext,
+                                            R);
     GD_CUDA_TRY(cudaGetLastError());
     if (ext) {
       GD_TRY(precond->apply_lattice(precond->ctx, A, r, zb[zc], st));
