@@ -861,9 +861,11 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     for (int i = threadIdx.x; i < NN * 5; i += blockDim.x) s_Fn[i] = f_const * __ldg(Fhat + i / 5) * (double)(i % 5);
   build_entry_tab<2, K>(s_tab);
   __syncthreads();
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  // two lanes per row: both decode the row's cells, each forms every other entry, the
+  // first also the right-hand side (twice the warps of one lane per row, to hide latency)
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 1;
   if (r >= nrows_own) return;
-  const int t = threadIdx.x;
+  const int t = threadIdx.x, sub = t & 1;
   int nbad = 0;
   const uint32_t N0 = (uint32_t)g.N[0];
   const uint32_t lin = (uint32_t)row_node[r];
@@ -878,7 +880,7 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     const bool ok = (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
                     c1 < (int)g.n[1];
     const double k = ok ? __ldg(kappa + (int64_t)c1 * g.n[0] + c0) : 0.0;
-    if (ok) {   // finite and positive, tested on the bits (integer pipe, not GB300's scarce FP64 one)
+    if (ok && sub == 0) {   // finite and positive, tested on the bits (integer pipe, not GB300's scarce FP64 one)
       const unsigned long long bits = (unsigned long long)__double_as_longlong(k);
       nbad += (bits >> 63) != 0ull || ((bits >> 52) & 0x7FFull) == 0x7FFull || bits == 0ull;
     }
@@ -905,13 +907,18 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   // all stencil codes of the row first (independent loads, one memory latency), then the
   // entries; a 2D row has at most MAXE of them
   constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
-  int cv[MAXE];
+  constexpr int MAXH = (MAXE + 1) / 2;   // entries of one lane
+  int cv[MAXH];
 #pragma unroll
-  for (int i = 0; i < MAXE; ++i) cv[i] = i < len ? (int)__ldg(code + e0 + i) : 0;
+  for (int h = 0; h < MAXH; ++h) {
+    const int i = 2 * h + sub;
+    cv[h] = i < len ? (int)__ldg(code + e0 + i) : 0;
+  }
 #pragma unroll
-  for (int i = 0; i < MAXE; ++i) {
+  for (int h = 0; h < MAXH; ++h) {
+    const int i = 2 * h + sub;
     if (i >= len) break;
-    const int info = et[cv[i]];
+    const int info = et[cv[h]];
     const int off = (info & 255) - 128;
     const int fixed = (info >> 8) & 7, both = (info >> 11) & 7;
     double v = 0.0;
@@ -929,12 +936,14 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     }
     vals[e0 + i] = v;
   }
-  // right-hand side: source over the node's cells minus the lifting of the Dirichlet values
-  // (CS: the source value of the node's local position is the same in all its cells; slot
-  // 3, the cell on the upper side in both directions, always holds the node)
-  double b = CS && !FN ? s_Fn[s_lx[3][t] * 5 + __popc(vmask)] : 0.0;
+  // right-hand side: source over the node's cells minus the lifting of the Dirichlet values;
+  // the two lanes take two cells each and add their parts (CS: the source value of the
+  // node's local position is the same in all its cells; slot 3, the cell on the upper side
+  // in both directions, always holds the node)
+  double b = CS && !FN && sub == 0 ? s_Fn[s_lx[3][t] * 5 + __popc(vmask)] : 0.0;
 #pragma unroll
-  for (int a = 0; a < 4; ++a) {
+  for (int h = 0; h < 2; ++h) {
+    const int a = 2 * sub + h;
     if (!((vmask >> a) & 1u)) continue;
     const int la = s_lx[a][t];
     if (!FN && !CS) b += f_const * s_F[la];
@@ -957,7 +966,8 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
       }
     }
   }
-  rhs[r] = b;
+  b += __shfl_xor_sync(3u << ((t & 31) & ~1), b, 1);   // the row's lane pair
+  if (sub == 0) rhs[r] = b;
   if (nbad) atomicAdd(bad, nbad);
 }
 
@@ -1003,7 +1013,7 @@ static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_no
   const Geom& g = A->test->geom;
   const int64_t R = A->ngdofs;
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
-  const unsigned nb = (unsigned)((R + 127) / 128);
+  const unsigned nb = (unsigned)((2 * R + 127) / 128);   // two lanes per row
   const CodeT* code = reinterpret_cast<const CodeT*>(A->code.p);
   bool cs = false;
   GD_TRY(rows2d_symmetric(A, K, &cs));

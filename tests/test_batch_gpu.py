@@ -69,7 +69,9 @@ def test_batch_matches_oracle(batch_setup):
 
 def test_batch_matches_single_problem_assembly(batch_setup):
     """Orders 2 and 3 run the same row bodies as the single-problem kernel with the cells'
-    terms summed one by one (the 2D class sums switched off): bit-exact."""
+    terms summed one by one (the 2D class sums switched off): values bit-exact; the rhs
+    bit-exact in 3D and within 1e-14 x max|b| in 2D, where the single-problem kernel adds
+    the halves of a row's cells formed by two lanes."""
     import gridap_gb300 as G
     be, pbs, built, B = batch_setup
     for pb, M, vec in zip(pbs, B.matrices, B.vectors):
@@ -81,7 +83,10 @@ def test_batch_matches_single_problem_assembly(batch_setup):
         for (rp, ci, vv), (rp2, ci2, vv2) in zip(M.csr_parts(), op.matrix.csr_parts()):
             assert np.array_equal(vv, vv2)
         for b1, b2 in zip(vec.partition, op.vector.partition):
-            assert np.array_equal(b1, b2)
+            if pb.dim == 3:
+                assert np.array_equal(b1, b2)
+            else:
+                assert np.abs(b1 - b2).max(initial=0.0) <= 1e-14 * max(np.abs(b2).max(initial=0.0), 1e-300)
 
 
 def test_batch_tuning_and_graph_replay_are_stable(batch_setup):
