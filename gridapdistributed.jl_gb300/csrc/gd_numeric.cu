@@ -835,6 +835,10 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
 // direction; 5 FP64 additions) and each entry costs one FP64 multiply, where the exact
 // per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
 // of its FP32 rate, and this kernel is bound by it.
+// lanes per row of k_rows2d_fused (1, 2 or 4; on the 128^2 Q2 case 2 lanes took 14.3 us,
+// 1 lane 16.8 us and 4 lanes 16.0 us)
+constexpr int kR2dLanes = 2;
+
 template <int K, typename CodeT, bool FN, bool UD, bool CS>
 __global__ void __launch_bounds__(128)
 k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
@@ -861,11 +865,13 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     for (int i = threadIdx.x; i < NN * 5; i += blockDim.x) s_Fn[i] = f_const * __ldg(Fhat + i / 5) * (double)(i % 5);
   build_entry_tab<2, K>(s_tab);
   __syncthreads();
-  // two lanes per row: both decode the row's cells, each forms every other entry, the
-  // first also the right-hand side (twice the warps of one lane per row, to hide latency)
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 1;
+  // kR2dLanes lanes per row: all decode the row's cells, each forms every kR2dLanes-th
+  // entry and a share of the node's cells for the rhs (more warps than one lane per row,
+  // to hide latency)
+  constexpr int LPR = kR2dLanes;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
   if (r >= nrows_own) return;
-  const int t = threadIdx.x, sub = t & 1;
+  const int t = threadIdx.x, sub = t % LPR;
   int nbad = 0;
   const uint32_t N0 = (uint32_t)g.N[0];
   const uint32_t lin = (uint32_t)row_node[r];
@@ -907,16 +913,16 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   // all stencil codes of the row first (independent loads, one memory latency), then the
   // entries; a 2D row has at most MAXE of them
   constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
-  constexpr int MAXH = (MAXE + 1) / 2;   // entries of one lane
+  constexpr int MAXH = (MAXE + LPR - 1) / LPR;   // entries of one lane
   int cv[MAXH];
 #pragma unroll
   for (int h = 0; h < MAXH; ++h) {
-    const int i = 2 * h + sub;
+    const int i = LPR * h + sub;
     cv[h] = i < len ? (int)__ldg(code + e0 + i) : 0;
   }
 #pragma unroll
   for (int h = 0; h < MAXH; ++h) {
-    const int i = 2 * h + sub;
+    const int i = LPR * h + sub;
     if (i >= len) break;
     const int info = et[cv[h]];
     const int off = (info & 255) - 128;
@@ -937,13 +943,13 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     vals[e0 + i] = v;
   }
   // right-hand side: source over the node's cells minus the lifting of the Dirichlet values;
-  // the two lanes take two cells each and add their parts (CS: the source value of the
+  // the lanes take 4 / LPR cells each and add their parts (CS: the source value of the
   // node's local position is the same in all its cells; slot 3, the cell on the upper side
   // in both directions, always holds the node)
   double b = CS && !FN && sub == 0 ? s_Fn[s_lx[3][t] * 5 + __popc(vmask)] : 0.0;
 #pragma unroll
-  for (int h = 0; h < 2; ++h) {
-    const int a = 2 * sub + h;
+  for (int h = 0; h < 4 / LPR; ++h) {
+    const int a = (4 / LPR) * sub + h;
     if (!((vmask >> a) & 1u)) continue;
     const int la = s_lx[a][t];
     if (!FN && !CS) b += f_const * s_F[la];
@@ -966,7 +972,9 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
       }
     }
   }
-  b += __shfl_xor_sync(3u << ((t & 31) & ~1), b, 1);   // the row's lane pair
+  const unsigned gmask = ((1u << LPR) - 1u) << ((t & 31) & ~(LPR - 1));   // the row's lanes
+#pragma unroll
+  for (int o = LPR / 2; o > 0; o >>= 1) b += __shfl_xor_sync(gmask, b, o);
   if (sub == 0) rhs[r] = b;
   if (nbad) atomicAdd(bad, nbad);
 }
@@ -1013,7 +1021,7 @@ static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_no
   const Geom& g = A->test->geom;
   const int64_t R = A->ngdofs;
   const double* udir = A->trial->has_dirichlet_values ? A->trial->u_dir.p : nullptr;
-  const unsigned nb = (unsigned)((2 * R + 127) / 128);   // two lanes per row
+  const unsigned nb = (unsigned)((kR2dLanes * R + 127) / 128);
   const CodeT* code = reinterpret_cast<const CodeT*>(A->code.p);
   bool cs = false;
   GD_TRY(rows2d_symmetric(A, K, &cs));
