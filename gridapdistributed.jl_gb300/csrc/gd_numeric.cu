@@ -820,25 +820,26 @@ static int launch_numeric(gd_asm* A, const double* kappa, const double* f_nodal,
   return GD_OK;
 }
 
-// ---- 2D Q_k (k = 2, 3): values and right-hand side in one kernel, one thread per row ----
-// A 2D row has at most (2k+1)^2 entries (25 for Q2), so one thread forms its whole row:
-// it decodes its node's (at most 4) cells once, then walks its CSR entries (the stencil
-// code of each entry gives the offset and the cells that hold both nodes through the
-// shared-memory entry table, as in qk_matrix_rows) and finally the right-hand side (source
-// term and Dirichlet lifting with the same cells).  Consecutive threads own consecutive
-// rows, so a warp's values are one contiguous range of the CSR value array.
-// CS (class sums): when the reference tables are invariant under the square's reflections
-// (checked on the host), the cells that hold both nodes of an entry are reflections of
-// one another across the node's cell boundaries and give the same table value, so the
-// entry is that value times the sum of their coefficients: the thread forms the 9 subset
-// sums of its (at most 4) cell coefficients once (left, right or both cells per
-// direction; 5 FP64 additions) and each entry costs one FP64 multiply, where the exact
-// per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
-// of its FP32 rate, and this kernel is bound by it.
+// ---- 2D Q_k (k = 2, 3): values and right-hand side in one kernel, a lane pair per row ----
 // lanes per row of k_rows2d_fused (1, 2 or 4; on the 128^2 Q2 case 2 lanes took 14.3 us,
 // 1 lane 16.8 us and 4 lanes 16.0 us)
 constexpr int kR2dLanes = 2;
 
+// A 2D row has at most (2k+1)^2 entries (25 for Q2), so kR2dLanes lanes form a whole row:
+// each decodes the node's (at most 4) cells, takes every kR2dLanes-th CSR entry (the
+// stencil code of each entry gives the offset and the cells that hold both nodes through
+// the shared-memory entry table, as in qk_matrix_rows) and a share of the node's cells
+// for the right-hand side (source term and Dirichlet lifting, only in cells on a Dirichlet
+// side), summed over the lanes by shuffles.  Consecutive lane groups own consecutive rows,
+// so a warp's values are one contiguous range of the CSR value array.
+// CS (class sums): when the reference tables are invariant under the square's reflections
+// (checked on the host), the cells that hold both nodes of an entry are reflections of
+// one another across the node's cell boundaries and give the same table value, so the
+// entry is that value times the sum of their coefficients: each lane forms the 9 subset
+// sums of the (at most 4) cell coefficients once (left, right or both cells per
+// direction; 5 FP64 additions) and an entry costs one FP64 multiply, where the exact
+// per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
+// of its FP32 rate (the per-cell form kept its FP64 pipe 56 % busy, the class sums 36 %).
 template <int K, typename CodeT, bool FN, bool UD, bool CS>
 __global__ void __launch_bounds__(128)
 k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
