@@ -35,7 +35,7 @@ def sources():
 
 def _compile(src: Path) -> tuple[Path, str]:
     obj = BUILD / (src.stem + ".o")
-    dep_mtime = max(p.stat().st_mtime for p in list(CSRC.glob("*.h")) + [src] + [HERE.parent / "include" / "gdgpu.h"])
+    dep_mtime = max(p.stat().st_mtime for p in list(CSRC.glob("*.h")) + list(CSRC.glob("*.cuh")) + [src] + [HERE.parent / "include" / "gdgpu.h"])
     if obj.exists() and obj.stat().st_mtime > dep_mtime:
         return obj, ""
     cmd = [_nvcc(), *NVCC_FLAGS, "-I", str(HERE.parent / "include"), "-c", str(src), "-o", str(obj)]

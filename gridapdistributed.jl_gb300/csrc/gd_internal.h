@@ -327,6 +327,7 @@ struct gd_asm {
   bool r2d_sym = false;
   int r2d_sym_degree = -1;
   bool r2d_class_sums = true;
+  std::vector<double> r2d_F;      // the reference load table, copied with the symmetry check
   int64_t q1_rows[2] = {0, -1};   // owned-row range of the next Q1 launch (hi < 0: all rows)
   // pipelined download (gd_assemble_download): host destinations of the values and the
   // rhs while active, the copy stream, one event per row range, the row ranges and

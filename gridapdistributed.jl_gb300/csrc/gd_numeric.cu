@@ -728,16 +728,18 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
     coef = A->w_cells.p;
   }
   // autotune the launch shape once per assembler: time every shape with CUDA events
-  // (each run writes the same values) and keep the fastest
+  // (each run writes the same values), the shapes in turn over several rounds so that a
+  // drift of the clocks or the memory state does not favour one of them, and keep the
+  // fastest by its best time (the first round only warms up)
   if (A->q1_shape < 0) {
+    constexpr int kRounds = 6;
     cudaEvent_t e0, e1;
     GD_CUDA_TRY(cudaEventCreate(&e0));
     GD_CUDA_TRY(cudaEventCreate(&e1));
-    float best = 1e30f;
-    int best_shape = 0;
-    for (int sh = 0; sh < kNumQ1Shapes; ++sh) {
-      float ms_sum = 0.f;
-      for (int rep = 0; rep < 3; ++rep) {
+    float best_ms[kNumQ1Shapes];
+    for (int sh = 0; sh < kNumQ1Shapes; ++sh) best_ms[sh] = 1e30f;
+    for (int rep = 0; rep < kRounds; ++rep) {
+      for (int sh = 0; sh < kNumQ1Shapes; ++sh) {
         GD_CUDA_TRY(cudaEventRecord(e0, st));
         int s2 = cube ? launch_q1_mode<DIM, true>(A, sh, q, coef, f_nodal, udir, bad, st)
                       : launch_q1_mode<DIM, false>(A, sh, q, coef, f_nodal, udir, bad, st);
@@ -746,13 +748,13 @@ static int launch_q1(gd_asm* A, const double* kappa, const double* f_nodal, doub
         GD_CUDA_TRY(cudaEventSynchronize(e1));
         float ms = 0.f;
         GD_CUDA_TRY(cudaEventElapsedTime(&ms, e0, e1));
-        if (rep > 0) ms_sum += ms;
+        if (rep > 0) best_ms[sh] = std::min(best_ms[sh], ms);
       }
-      A->q1_shape_ms[sh] = ms_sum / 2;
-      if (ms_sum < best) {
-        best = ms_sum;
-        best_shape = sh;
-      }
+    }
+    int best_shape = 0;
+    for (int sh = 0; sh < kNumQ1Shapes; ++sh) {
+      A->q1_shape_ms[sh] = best_ms[sh];
+      if (best_ms[sh] < best_ms[best_shape]) best_shape = sh;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
@@ -840,11 +842,21 @@ constexpr int kR2dLanes = 2;
 // direction; 5 FP64 additions) and an entry costs one FP64 multiply, where the exact
 // per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
 // of its FP32 rate (the per-cell form kept its FP64 pipe 56 % busy, the class sums 36 %).
+// Memory order: the row's node and CSR range are loaded before the block's tables are set
+// up, and its stencil codes and cell coefficients together right after, so a row waits for
+// two memory round trips instead of a chain of five (tables, node, coefficients, CSR range,
+// codes).
+// Source table: s_Fn[5 l + n] = f_const F[l] n, the load of local node l summed over n valid
+// cells, formed on the host (no FP64 work per block).
+struct R2dFn {
+  double v[16 * 5];   // NN * 5 for K <= 3
+};
+
 template <int K, typename CodeT, bool FN, bool UD, bool CS>
 __global__ void __launch_bounds__(128)
 k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, const int32_t* __restrict__ row_node,
                const CodeT* __restrict__ code, const double* __restrict__ kappa, const double* __restrict__ Khat,
-               const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const,
+               const double* __restrict__ Mhat, const double* __restrict__ Fhat, double f_const, const R2dFn fn,
                const double* __restrict__ f_nodal, const double* __restrict__ u_dir, double* __restrict__ vals,
                double* __restrict__ rhs, int32_t* __restrict__ bad) {
   using L = Lat<2, K>;
@@ -857,25 +869,36 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   __shared__ double s_kap[4][128];   // per thread: coefficient and local index of its 4 slots
   __shared__ int s_lx[4][128];       // (shared, not local, memory: they are indexed at run time)
   __shared__ double s_S[CS ? 9 : 1][128];   // per thread: subset sums, index ox + 3 oy (0 left, 1 right, 2 both)
-  for (int i = threadIdx.x; i < NN * NN; i += blockDim.x) {
-    s_K[i] = Khat[i];
-    if (FN) s_M[i] = Mhat[i];
-  }
-  for (int i = threadIdx.x; i < NN; i += blockDim.x) s_F[i] = Fhat[i];
-  if (CS && !FN)
-    for (int i = threadIdx.x; i < NN * 5; i += blockDim.x) s_Fn[i] = f_const * __ldg(Fhat + i / 5) * (double)(i % 5);
-  build_entry_tab<2, K>(s_tab);
-  __syncthreads();
   // kR2dLanes lanes per row: all decode the row's cells, each forms every kR2dLanes-th
   // entry and a share of the node's cells for the rhs (more warps than one lane per row,
   // to hide latency)
   constexpr int LPR = kR2dLanes;
-  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) / LPR;
-  if (r >= nrows_own) return;
   const int t = threadIdx.x, sub = t % LPR;
+  const int64_t r = ((int64_t)blockIdx.x * blockDim.x + t) / LPR;
+  const bool live = r < nrows_own;
+  const uint32_t lin = live ? (uint32_t)row_node[r] : 0u;
+  const int64_t e0 = live ? rowptr[r] : 0;
+  const int len = live ? (int)(rowptr[r + 1] - e0) : 0;
+  for (int i = t; i < NN * NN; i += blockDim.x) {
+    s_K[i] = Khat[i];
+    if (FN) s_M[i] = Mhat[i];
+  }
+  for (int i = t; i < NN; i += blockDim.x) s_F[i] = Fhat[i];
+  if (CS && !FN)
+    for (int i = t; i < NN * 5; i += blockDim.x) s_Fn[i] = fn.v[i];
+  build_entry_tab<2, K>(s_tab);
+  // all stencil codes of the row (independent loads), then the cell coefficients; a 2D
+  // row has at most MAXE entries
+  constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
+  constexpr int MAXH = (MAXE + LPR - 1) / LPR;   // entries of one lane
+  int cv[MAXH];
+#pragma unroll
+  for (int h = 0; h < MAXH; ++h) {
+    const int i = LPR * h + sub;
+    cv[h] = i < len ? (int)__ldg(code + e0 + i) : 0;
+  }
   int nbad = 0;
   const uint32_t N0 = (uint32_t)g.N[0];
-  const uint32_t lin = (uint32_t)row_node[r];
   const int X0 = (int)(lin % N0), X1 = (int)(lin / N0);
   const int rm0 = X0 % K, rm1 = X1 % K;
   const int onb = (rm0 == 0 ? 1 : 0) | (rm1 == 0 ? 2 : 0);
@@ -884,7 +907,7 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
   for (int a = 0; a < 4; ++a) {
     const int s0 = a & 1, s1 = (a >> 1) & 1;
     const int c0 = s0 ? X0 / K : X0 / K - 1, c1 = s1 ? X1 / K : X1 / K - 1;
-    const bool ok = (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
+    const bool ok = live && (s0 || rm0 == 0) && (s1 || rm1 == 0) && c0 >= 0 && c0 < (int)g.n[0] && c1 >= 0 &&
                     c1 < (int)g.n[1];
     const double k = ok ? __ldg(kappa + (int64_t)c1 * g.n[0] + c0) : 0.0;
     if (ok && sub == 0) {   // finite and positive, tested on the bits (integer pipe, not GB300's scarce FP64 one)
@@ -895,32 +918,41 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
     s_lx[a][t] = (s0 ? rm0 : K) + L::KP1 * (s1 ? rm1 : K);
     vmask |= (uint32_t)ok << a;
   }
+  __syncthreads();
+  if (!live) return;
+  const unsigned gmask = ((1u << LPR) - 1u) << ((t & 31) & ~(LPR - 1));   // the row's lanes
   if (CS) {   // slot a = s0 | 2 s1 (s = 1: the cell on the upper side of the node)
     const double k00 = s_kap[0][t], k10 = s_kap[1][t], k01 = s_kap[2][t], k11 = s_kap[3][t];
-    const double lo2 = k00 + k10, hi2 = k01 + k11;
+    double lo2, hi2, s6, s7;
+    if (LPR == 2) {
+      // the lane pair splits the four two-cell sums (lane 0: k00 + k10 and k00 + k01,
+      // lane 1: k01 + k11 and k10 + k11; the same operands in the same order, so the same
+      // bits) and swaps them: two FP64 additions per lane instead of four
+      const double xa = sub ? k01 : k00, xb = sub ? k11 : k10;
+      const double ya = sub ? k10 : k00, yb = sub ? k11 : k01;
+      const double x = xa + xb, y = ya + yb;
+      const double xo = __shfl_xor_sync(gmask, x, 1), yo = __shfl_xor_sync(gmask, y, 1);
+      lo2 = sub ? xo : x;
+      hi2 = sub ? x : xo;
+      s6 = sub ? yo : y;
+      s7 = sub ? y : yo;
+    } else {
+      lo2 = k00 + k10;
+      hi2 = k01 + k11;
+      s6 = k00 + k01;
+      s7 = k10 + k11;
+    }
     s_S[0][t] = k00;
     s_S[1][t] = k10;
     s_S[2][t] = lo2;
     s_S[3][t] = k01;
     s_S[4][t] = k11;
     s_S[5][t] = hi2;
-    s_S[6][t] = k00 + k01;
-    s_S[7][t] = k10 + k11;
+    s_S[6][t] = s6;
+    s_S[7][t] = s7;
     s_S[8][t] = lo2 + hi2;
   }
   const uint16_t* et = s_tab + onb * EntryTab<2, K>::E;
-  const int64_t e0 = rowptr[r];
-  const int len = (int)(rowptr[r + 1] - e0);
-  // all stencil codes of the row first (independent loads, one memory latency), then the
-  // entries; a 2D row has at most MAXE of them
-  constexpr int MAXE = (2 * K + 1) * (2 * K + 1);
-  constexpr int MAXH = (MAXE + LPR - 1) / LPR;   // entries of one lane
-  int cv[MAXH];
-#pragma unroll
-  for (int h = 0; h < MAXH; ++h) {
-    const int i = LPR * h + sub;
-    cv[h] = i < len ? (int)__ldg(code + e0 + i) : 0;
-  }
 #pragma unroll
   for (int h = 0; h < MAXH; ++h) {
     const int i = LPR * h + sub;
@@ -973,7 +1005,6 @@ k_rows2d_fused(Geom g, int64_t nrows_own, const int64_t* __restrict__ rowptr, co
       }
     }
   }
-  const unsigned gmask = ((1u << LPR) - 1u) << ((t & 31) & ~(LPR - 1));   // the row's lanes
 #pragma unroll
   for (int o = LPR / 2; o > 0; o >>= 1) b += __shfl_xor_sync(gmask, b, o);
   if (sub == 0) rhs[r] = b;
@@ -1012,6 +1043,7 @@ static int rows2d_symmetric(gd_asm* A, int K, bool* sym) {
   }
   A->r2d_sym = ok;
   A->r2d_sym_degree = A->ref_degree;
+  A->r2d_F = Fh;
   *sym = ok;
   return GD_OK;
 }
@@ -1027,10 +1059,17 @@ static int launch_rows2d_code(gd_asm* A, const double* kappa, const double* f_no
   bool cs = false;
   GD_TRY(rows2d_symmetric(A, K, &cs));
   cs = cs && A->r2d_class_sums;
+  constexpr int NN = (K + 1) * (K + 1);
+  static_assert(NN * 5 <= (int)(sizeof(R2dFn::v) / sizeof(double)), "source table size");
+  R2dFn fn = {};
+  if (cs && !f_nodal) {   // the same products, in the same order, as f_const * F[l] * n on the device
+    if (A->r2d_F.size() != (size_t)NN) return fail(GD_ERR_STATE, "2D reference load table not cached");
+    for (int i = 0; i < NN * 5; ++i) fn.v[i] = f_const * A->r2d_F[i / 5] * (double)(i % 5);
+  }
 #define GD_R2D(FNV, UDV, CSV)                                                                                     \
   k_rows2d_fused<K, CodeT, FNV, UDV, CSV><<<nb, 128, 0, st>>>(g, R, A->rowptr.p, A->row_node.p, code, kappa,      \
-                                                              A->Khat.p, A->Mhat.p, A->Fhat.p, f_const, f_nodal,   \
-                                                              udir, A->vals.p, A->rhs.p, bad)
+                                                              A->Khat.p, A->Mhat.p, A->Fhat.p, f_const, fn,       \
+                                                              f_nodal, udir, A->vals.p, A->rhs.p, bad)
   if (cs) {
     if (f_nodal && udir) GD_R2D(true, true, true);
     else if (f_nodal) GD_R2D(true, false, true);

@@ -245,7 +245,8 @@ int gd_assembler_counts(const gd_asm* a, int64_t* ngdofs, int64_t* nnz_owned, in
 
 /* Launch shape the autotuner chose for the Q1 numeric kernel on the first numeric
  * assembly (-1 before it ran, or when the generic kernel is used): index, rows per
- * chunk, staging buffers, and the measured ms of each of the `nshapes` candidates. */
+ * chunk, staging buffers, and the measured ms of each of the `nshapes` candidates (the
+ * best of 5 timed launches, the candidates timed in turn after one warm-up round). */
 int gd_assembler_tuning(const gd_asm* a, int32_t* shape, int32_t* rows, int32_t* nbuf, float* ms_per_shape,
                         int32_t* nshapes);
 /* Fix the launch shape of the Q1 numeric kernel (0 .. nshapes-1 of gd_assembler_tuning)
