@@ -837,10 +837,11 @@ constexpr int kR2dLanes = 2;
 // CS (class sums): when the reference tables are invariant under the square's reflections
 // (checked on the host), the cells that hold both nodes of an entry are reflections of
 // one another across the node's cell boundaries and give the same table value, so the
-// entry is that value times the sum of their coefficients: each lane forms the 9 subset
-// sums of the (at most 4) cell coefficients once (left, right or both cells per
-// direction; 5 FP64 additions) and an entry costs one FP64 multiply, where the exact
-// per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
+// entry is that value times the sum of their coefficients: the row's lanes form the 9
+// subset sums of the (at most 4) cell coefficients once (left, right or both cells per
+// direction: five sums of two or four coefficients, split over a lane pair so that each
+// lane executes three FP64 additions) and an entry costs one FP64 multiply, where the
+// exact per-cell form costs one FMA per cell (up to 4).  GB300 issues FP64 at a small fraction
 // of its FP32 rate (the per-cell form kept its FP64 pipe 56 % busy, the class sums 36 %).
 // Memory order: the row's node and CSR range are loaded before the block's tables are set
 // up, and its stencil codes and cell coefficients together right after, so a row waits for
