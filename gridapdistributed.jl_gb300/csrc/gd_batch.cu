@@ -452,7 +452,8 @@ extern "C" int gd_batch_create(gd_asm* const* asms, const gd_coeffs* coeffs, int
   gd_ctx* ctx = nullptr;
   for (int p = 0; p < nprobs; ++p) {
     gd_asm* A = asms[p];
-    if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_batch_create: every assembler needs its symbolic phase");
+    if (!A) return fail(GD_ERR_ARG, "gd_batch_create: null assembler");
+    if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_batch_create: every assembler needs its symbolic phase");
     if (A->test->geom.k < 1 || A->test->geom.k > 3) return fail(GD_ERR_UNSUPPORTED, "gd_batch_create: order 1..3");
     if (A->bs != 1) return fail(GD_ERR_UNSUPPORTED, "gd_batch_create: scalar spaces only");
     const Geom& g = A->test->geom;

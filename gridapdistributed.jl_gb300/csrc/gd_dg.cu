@@ -820,7 +820,8 @@ extern "C" int gd_dg_assemble(gd_dgspace* S, const gd_dg_form* F) {
 
 extern "C" int gd_dg_matrix_sizes(const gd_dgspace* S, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
                                   int64_t* n_ghost_rows, int64_t* n_ghost_cols) {
-  if (!S || !S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_sizes: assemble first");
+  if (!S) return fail(GD_ERR_ARG, "gd_dg_matrix_sizes: null DG space");
+  if (!S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_sizes: assemble first");
   if (part < 0 || part >= (int)S->parts.size()) return fail(GD_ERR_ARG, "gd_dg_matrix_sizes: bad part");
   const DgPart& P = S->parts[part];
   cudaStream_t st = S->model->ctx->stream;
@@ -860,7 +861,8 @@ static void dg_local_cell_gid(const gd_dgspace* S, const DgPart& P, int64_t key,
 extern "C" int gd_dg_matrix_export(const gd_dgspace* S, int part, int64_t* rowptr, int32_t* colidx, double* vals,
                                    int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
                                    int32_t* ghost_col_owners, double* rhs) {
-  if (!S || !S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_export: assemble first");
+  if (!S) return fail(GD_ERR_ARG, "gd_dg_matrix_export: null DG space");
+  if (!S->assembled) return fail(GD_ERR_STATE, "gd_dg_matrix_export: assemble first");
   if (part < 0 || part >= (int)S->parts.size()) return fail(GD_ERR_ARG, "gd_dg_matrix_export: bad part");
   const DgPart& P = S->parts[part];
   cudaStream_t st = S->model->ctx->stream;

@@ -388,7 +388,8 @@ extern "C" int gd_mfield_assemble(gd_mfield* M, const double* stiff, const doubl
 // Values of block (i, j) over the owned rows of `part` (the scalar pattern of the part,
 // gd_matrix_export order), and field i's right-hand side over the part's owned rows.
 extern "C" int gd_mfield_block_export(const gd_mfield* M, int i, int j, int part, double* vals, double* rhs) {
-  if (!M || !M->assembled) return fail(GD_ERR_STATE, "gd_mfield_block_export: assemble first");
+  if (!M) return fail(GD_ERR_ARG, "gd_mfield_block_export: null multi-field system");
+  if (!M->assembled) return fail(GD_ERR_STATE, "gd_mfield_block_export: assemble first");
   const gd_asm* A = M->A;
   if (i < 0 || j < 0 || i >= M->nf || j >= M->nf || part < 0 || part >= (int)A->parts.size())
     return fail(GD_ERR_ARG, "gd_mfield_block_export: bad index");

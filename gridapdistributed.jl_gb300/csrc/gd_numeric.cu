@@ -1243,7 +1243,8 @@ extern "C" int gd_assembler_set_profiling(gd_asm* A, int on) {
 }
 
 extern "C" int gd_assembler_phase_times(const gd_asm* A, double* ms0, double* ms1, double* ms2) {
-  if (!A || !A->ev[0]) return gd::fail(GD_ERR_STATE, "gd_assembler_phase_times: profiling was not enabled");
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_phase_times: null assembler");
+  if (!A->ev[0]) return gd::fail(GD_ERR_STATE, "gd_assembler_phase_times: profiling was not enabled");
   GD_CUDA_TRY(cudaEventSynchronize(A->ev[3]));
   float t[3] = {0, 0, 0};
   for (int i = 0; i < 3; ++i) GD_CUDA_TRY(cudaEventElapsedTime(&t[i], A->ev[i], A->ev[i + 1]));
@@ -1267,7 +1268,8 @@ extern "C" int gd_assembler_tuning(const gd_asm* A, int32_t* shape, int32_t* row
 }
 
 extern "C" int gd_assembler_set_shape(gd_asm* A, int shape) {
-  if (!A || !A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_set_shape: run gd_assemble_symbolic first");
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_set_shape: null assembler");
+  if (!A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_set_shape: run gd_assemble_symbolic first");
   if (!A->fast_q1) return gd::fail(GD_ERR_UNSUPPORTED, "gd_assembler_set_shape: the assembler does not use the Q1 kernel");
   if (shape < -1 || shape >= gd::kNumQ1Shapes) return gd::fail(GD_ERR_ARG, "gd_assembler_set_shape: shape out of range");
   A->q1_shape = shape;   // -1: the next numeric assembly times every shape again
@@ -1282,7 +1284,8 @@ extern "C" int gd_assembler_set_class_sums(gd_asm* A, int on) {
 
 extern "C" int gd_assembler_counts(const gd_asm* A, int64_t* ngdofs, int64_t* nnz_owned, int64_t* nnz_total,
                                    int32_t* kernels) {
-  if (!A || !A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_counts: run gd_assemble_symbolic first");
+  if (!A) return gd::fail(GD_ERR_ARG, "gd_assembler_counts: null assembler");
+  if (!A->symbolic_done) return gd::fail(GD_ERR_STATE, "gd_assembler_counts: run gd_assemble_symbolic first");
   if (ngdofs) *ngdofs = A->ngdofs;
   if (nnz_owned) *nnz_owned = A->nnz_own;
   if (nnz_total) *nnz_total = A->nnz_total;

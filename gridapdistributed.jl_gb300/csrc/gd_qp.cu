@@ -910,7 +910,8 @@ extern "C" int gd_assemble_elasticity_qp(gd_asm* A, const gd_elasticity_qp* c) {
 
 extern "C" int gd_qp_info(const gd_asm* A, int32_t* points, int32_t* entries, int32_t* kpad, int32_t* etiles,
                           double* ms_element, double* ms_rows) {
-  if (!A || !A->qp) return fail(GD_ERR_STATE, "gd_qp_info: no quadrature-point assembly has run");
+  if (!A) return fail(GD_ERR_ARG, "gd_qp_info: null assembler");
+  if (!A->qp) return fail(GD_ERR_STATE, "gd_qp_info: no quadrature-point assembly has run");
   const QpState* Q = A->qp;
   if (points) *points = Q->nqt;
   if (entries) *entries = Q->nne;

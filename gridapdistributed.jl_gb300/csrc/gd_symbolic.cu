@@ -821,7 +821,8 @@ extern "C" int gd_assemble_symbolic(gd_asm* A) {
 // ---- exports ---------------------------------------------------------------------------
 extern "C" int gd_matrix_sizes(const gd_asm* A, int part, int64_t* nrows, int64_t* ncols, int64_t* nnz,
                                int64_t* n_ghost_rows, int64_t* n_ghost_cols) {
-  if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_matrix_sizes: run gd_assemble_symbolic first");
+  if (!A) return fail(GD_ERR_ARG, "gd_matrix_sizes: null assembler");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_matrix_sizes: run gd_assemble_symbolic first");
   if (part < 0 || part >= (int)A->parts.size()) return fail(GD_ERR_ARG, "gd_matrix_sizes: bad part");
   const DevPart& P = A->parts[part];
   cudaStream_t st = A->test->model->ctx->stream;
@@ -843,7 +844,8 @@ extern "C" int gd_matrix_sizes(const gd_asm* A, int part, int64_t* nrows, int64_
 extern "C" int gd_matrix_export(const gd_asm* A, int part, int64_t* rowptr, int32_t* colidx, double* vals,
                                 int64_t* ghost_row_gids, int32_t* ghost_row_owners, int64_t* ghost_col_gids,
                                 int32_t* ghost_col_owners) {
-  if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_matrix_export: run gd_assemble_symbolic first");
+  if (!A) return fail(GD_ERR_ARG, "gd_matrix_export: null assembler");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_matrix_export: run gd_assemble_symbolic first");
   if (part < 0 || part >= (int)A->parts.size()) return fail(GD_ERR_ARG, "gd_matrix_export: bad part");
   const DevPart& P = A->parts[part];
   const gd_space* S = A->test;
@@ -895,7 +897,8 @@ extern "C" int gd_matrix_export(const gd_asm* A, int part, int64_t* rowptr, int3
 }
 
 extern "C" int gd_vector_export(const gd_asm* A, int part, double* b) {
-  if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_vector_export: run gd_assemble_symbolic first");
+  if (!A) return fail(GD_ERR_ARG, "gd_vector_export: null assembler");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_vector_export: run gd_assemble_symbolic first");
   if (part < 0 || part >= (int)A->parts.size() || !b) return fail(GD_ERR_ARG, "gd_vector_export: bad argument");
   const DevPart& P = A->parts[part];
   cudaStream_t st = A->test->model->ctx->stream;
@@ -910,7 +913,8 @@ extern "C" int gd_vector_export(const gd_asm* A, int part, double* b) {
 
 extern "C" int gd_system_device_ptrs(const gd_asm* A, const int64_t** rowptr, const int32_t** colidx,
                                      const double** vals, const double** rhs, int64_t* ngdofs) {
-  if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_system_device_ptrs: run gd_assemble_symbolic first");
+  if (!A) return fail(GD_ERR_ARG, "gd_system_device_ptrs: null assembler");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_system_device_ptrs: run gd_assemble_symbolic first");
   if (rowptr) *rowptr = A->rowptr.p;
   if (colidx) *colidx = A->colgid.p;
   if (vals) *vals = A->vals.p;
@@ -920,7 +924,8 @@ extern "C" int gd_system_device_ptrs(const gd_asm* A, const int64_t** rowptr, co
 }
 
 extern "C" int gd_system_download(const gd_asm* A, double* rhs, double* owned_vals) {
-  if (!A || !A->symbolic_done) return fail(GD_ERR_STATE, "gd_system_download: run gd_assemble_symbolic first");
+  if (!A) return fail(GD_ERR_ARG, "gd_system_download: null assembler");
+  if (!A->symbolic_done) return fail(GD_ERR_STATE, "gd_system_download: run gd_assemble_symbolic first");
   cudaStream_t st = A->test->model->ctx->stream;
   if (rhs && A->ngdofs)
     GD_CUDA_TRY(cudaMemcpyAsync(rhs, A->rhs.p, sizeof(double) * A->ngdofs, cudaMemcpyDeviceToHost, st));

@@ -49,6 +49,9 @@ enum {
   GD_ERR_NUMERIC = 8,      /* NaN / Inf / non-positive coefficient in the input       */
   GD_ERR_NOTCONVERGED = 9  /* maximum iterations reached before the tolerance         */
 };
+/* Every function returns one of these (gd_last_error() and gd_version() return text).
+ * A null handle or a null required pointer is GD_ERR_ARG; a valid handle used out of
+ * order is GD_ERR_STATE; the *_destroy functions accept NULL and do nothing. */
 
 /* Assembly strategies (src/Algebra.jl:397-398). */
 enum { GD_SUB_ASSEMBLED_ROWS = 0, GD_FULLY_ASSEMBLED_ROWS = 1 };

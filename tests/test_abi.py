@@ -49,3 +49,43 @@ def test_no_gpu_context_fails_cleanly():
     h = ctypes.c_void_p()
     st = lib.gd_ctx_create(0, ctypes.byref(h))
     assert st != 0 and lib.gd_last_error()
+
+
+_NULL_PROBE = r'''
+import ctypes as C, json, sys
+import gridap_gb300._lib as L
+lib = L.load()
+ints = (C.c_int, C.c_int32, C.c_int64, C.c_uint32, C.c_uint64, C.c_size_t, C.c_long)
+out = {}
+for name, types in sorted(L.SIGNATURES.items()):
+    if name in ("gd_last_error", "gd_version"):
+        continue
+    args = [0 if t in ints else 0.0 if t in (C.c_double, C.c_float) else None for t in types]
+    out[name] = int(getattr(lib, name)(*args))
+print(json.dumps(out))
+'''
+
+
+def test_every_entry_point_rejects_null_arguments():
+    """Every C-ABI function called with null handles and pointers (zero sizes) returns
+    GD_ERR_ARG instead of crashing, and the destroy functions accept NULL (a no-op, as
+    free does), as include/gdgpu.h states.  All calls run in one child process, so a crash
+    fails this test instead of the test run."""
+    import json
+    import os
+    import subprocess
+    import sys
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is visible")
+    env = dict(os.environ, PYTHONPATH=os.pathsep.join([str(ROOT / "gridapdistributed.jl_gb300"),
+                                                       os.environ.get("PYTHONPATH", "")]))
+    p = subprocess.run([sys.executable, "-c", _NULL_PROBE], capture_output=True, text=True, env=env, timeout=300)
+    assert p.returncode == 0, p.stderr[-2000:]
+    status = json.loads(p.stdout.strip().splitlines()[-1])
+    assert len(status) >= 80
+    for name, st in status.items():
+        if name.endswith("_destroy"):
+            assert st == 0, name
+        else:
+            assert st == 1, (name, st)   # GD_ERR_ARG
