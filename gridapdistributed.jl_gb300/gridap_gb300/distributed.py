@@ -163,9 +163,14 @@ class VectorValue:
     with as many components as the model's dimension (VectorValue{D,Float64})."""
 
 
-def ReferenceFE(name, T, order):
+def ReferenceFE(name, T, order, space=None):
+    """``ReferenceFE(lagrangian, T, order; space)``: Lagrangian Q_k elements (``space`` the
+    default Q space).  The P space of a cube (``space=:P``, the discontinuous pressure of the
+    reference's Stokes test) is not built on the device and is refused, not replaced."""
     if name != lagrangian or T not in (float, np.float64, VectorValue):
         raise NotImplementedError("only Lagrangian Float64 and VectorValue reference FEs")
+    if space not in (None, "Q", ":Q"):
+        raise NotImplementedError(f"ReferenceFE(..., space={space}): only the Q space is built on the device")
     return ("lagrangian", VectorValue if T is VectorValue else float, int(order))
 
 
@@ -303,7 +308,10 @@ class DistributedSingleFieldFESpace:
             pass
 
 
-def TestFESpace(model, reffe, dirichlet_tags="boundary", conformity=None):
+def TestFESpace(model, reffe, dirichlet_tags="boundary", conformity=None, constraint=None):
+    if constraint is not None:
+        # ZeroMeanFESpace (FESpaces.jl:663-668, 872-910) is not built on the device
+        raise NotImplementedError(f"TestFESpace(..., constraint={constraint}): not built on the device")
     if conformity in ("L2", ":L2"):
         from .dg import DistributedDGFESpace
         if reffe[1] is not float:
